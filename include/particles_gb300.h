@@ -1,0 +1,165 @@
+/*
+ * particles_gb300.h -- C ABI of the GB300 test-particle integrator.
+ *
+ * One call of pt_integrate() replaces the reference's per-particle dispatch
+ * loop (sources/particles.F90:337-356):
+ *
+ *     do n = 1, nparticles
+ *       call integrate_rk5|integrate_dp853(nsteps, dm, params, time, uu, bb,
+ *                                          state(:,:,n), counter(:,n))
+ *     end do
+ *
+ * with the per-particle subroutines of sources/integrations.F90:57 (RK5) and
+ * :224 (DOP853), the force of sources/accelerations.F90:59 and the gather of
+ * sources/interpolations.F90:104 fused into one sm_103a kernel.  Arrays keep
+ * the Fortran layouts, so the Fortran driver passes its own arrays through
+ * ISO_C_BINDING without copies:
+ *
+ *   params[17]  params(1:17) as packed at particles.F90:317-333
+ *   time[m]     output times, time[0] = 0
+ *   uu, bb      uu(dm1,dm2,dm3,3), bb(...): x fastest, component slowest
+ *   state       state(8,m,np): element (c,n,p) at c + 8*(n + m*p), 0-based;
+ *               state(1:6,1,p) is the initial position and u = gamma v / c;
+ *               everything else is output
+ *   cnt         counter(3,np): all attempts, accepted, rejected
+ *
+ * All functions return PT_OK (0) or a negative PT_ERR_* code and never abort.
+ * pt_last_error() describes the most recent failure of the calling thread.
+ * No function is re-entrant on one pt_fields handle from several threads.
+ */
+#ifndef PARTICLES_GB300_H
+#define PARTICLES_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PT_ABI_VERSION 1
+
+/* Methods: the driver's `method` strings (particles.F90:337-338,347). */
+#define PT_METHOD_RK5     1   /* 'rk5' */
+#define PT_METHOD_DOP853  2   /* 'dop853', 'dp853', 'rk8' */
+
+/* Arithmetic of the fused kernel. */
+#define PT_PREC_FP64       0  /* FP64 throughout, no FMA: bit-identical to the CPU oracle */
+#define PT_PREC_FP64_FMA   1  /* FP64 throughout with FMA contraction */
+#define PT_PREC_FP32       2  /* FP32 fields, gather and force; FP64 RK sums, error, controller */
+#define PT_PREC_BF16       3  /* BF16 8^3 bricks with an FP32 scale per brick and component */
+
+/* Return codes. */
+#define PT_OK               0
+#define PT_ERR_ARG         -1  /* invalid argument */
+#define PT_ERR_CUDA        -2  /* CUDA runtime error (message in pt_last_error) */
+#define PT_ERR_NOMEM       -3  /* device allocation failed */
+#define PT_ERR_TIMEOUT     -4  /* the time budget expired; carry and status are consistent */
+#define PT_ERR_UNSUPPORTED -5  /* option combination not built */
+#define PT_ERR_PARTICLE    -6  /* at least one particle ended with a negative status */
+
+/* Per-particle status (pt_options.status / device status arrays). */
+#define PT_ST_DONE          0  /* t reached tmax */
+#define PT_ST_RUNNING       1  /* stopped at the window end t_stop < tmax; resumable */
+#define PT_ST_ESCAPED       2  /* crossed the open x boundary */
+#define PT_ST_NOT_RUN      -1  /* never started (time budget expired first) */
+#define PT_ST_STEP_LIMIT   -2  /* attempt cap reached (the reference loops forever) */
+#define PT_ST_DT_UNDERFLOW -3  /* dt <= 0 or t + dt == t (the reference loops forever) */
+#define PT_ST_NONFINITE    -4  /* NaN in the error norm */
+#define PT_ST_TIMEOUT      -5  /* interrupted by the time budget; resumable */
+
+/* Optional knobs.  A NULL pt_options, or a zero-filled one, gives the
+ * reference's behaviour (FP64, periodic, ideal E, classical controller). */
+typedef struct pt_options {
+    int32_t       struct_size;    /* sizeof(pt_options), or 0 */
+    int32_t       precision;      /* PT_PREC_* */
+    int32_t       open_x;         /* 1: particles escape through x = xmin / xmax of the domain */
+    int32_t       controller;     /* 0 classical; 1 learned trial step (needs a model) */
+    int64_t       max_steps;      /* attempt cap per particle; 0 = 1e9 */
+    double        eta;            /* resistivity: E = -U x B + eta J; 0 = ideal */
+    const double *jj;             /* J = curl B in the layout of bb; required iff eta != 0 */
+    double        t_stop;         /* integrate only while t < t_stop (window); 0 = tmax */
+    double        time_budget_s;  /* wall-clock budget of one kernel; 0 = 600 s */
+    int32_t      *status;         /* host: np per-particle PT_ST_* words, or NULL */
+    void         *carry;          /* host: pt_carry_bytes(np) bytes of controller memory
+                                     for resumable windows (zero-filled = fresh), or NULL */
+    const void   *model;          /* learned-controller weights (pt_mlp_*), or NULL */
+    int64_t       reserved[4];
+} pt_options;
+
+/* ---- one-shot, reference-shaped call ----------------------------------- */
+
+/* Replaces the dispatch loop: uploads the fields, integrates every particle
+ * and copies state/cnt back.  Host pointers throughout. */
+int pt_integrate(int32_t method, int64_t np, int32_t m, const int32_t dm[3],
+                 const double params[17], const double *time,
+                 const double *uu, const double *bb,
+                 double *state, int64_t *cnt, const pt_options *opt);
+
+/* 1 for 'rk5', 2 for 'dop853'/'dp853'/'rk8' (particles.F90:337-347), else 0. */
+int32_t pt_method_from_name(const char *name);
+
+/* ---- fields uploaded once (fields.F90:51-76 keeps its arrays; the GPU
+ *      holds a converted copy) ------------------------------------------- */
+
+typedef struct pt_fields pt_fields;
+
+/* Copies uu, bb (and jj when not NULL) from HOST memory to the device and
+ * converts them to the kernel layout for `precision`. */
+int pt_fields_create(const int32_t dm[3], const double *uu, const double *bb,
+                     const double *jj, int32_t precision, pt_fields **out);
+/* Same from DEVICE pointers (reference layout), on `stream`. */
+int pt_fields_create_device(const int32_t dm[3], const double *d_uu, const double *d_bb,
+                            const double *d_jj, int32_t precision, void *stream,
+                            pt_fields **out);
+int pt_fields_destroy(pt_fields *f);
+/* Device bytes held by the handle. */
+int64_t pt_fields_bytes(const pt_fields *f);
+
+/* Host-buffer run on uploaded fields; the same semantics as pt_integrate.
+ * With opt->carry and opt->t_stop it advances a resumable window: the
+ * first call starts from state(:,1,:), later calls continue from the carry. */
+int pt_integrate_fields(int32_t method, int64_t np, int32_t m, const pt_fields *f,
+                        const double params[17], const double *time,
+                        double *state, int64_t *cnt, const pt_options *opt);
+
+/* ---- device-resident run (inputs already in HBM) ------------------------ */
+
+/* Bytes of the controller-memory buffer for np particles. */
+int64_t pt_carry_bytes(int64_t np);
+
+/* All pointers are device pointers; launches on `stream` (NULL = default)
+ * and returns without synchronising.  d_status (np int32) and d_carry
+ * (pt_carry_bytes(np), zero = fresh) may be NULL.  opt->status, opt->carry
+ * and opt->jj are ignored here.  Completion errors (time budget, particle
+ * failures) are reported by pt_run_check() after the stream is synchronised. */
+int pt_run_device(int32_t method, int64_t np, int32_t m, const pt_fields *f,
+                  const double params[17], const double *d_time, double *d_state,
+                  int64_t *d_cnt, int32_t *d_status, void *d_carry,
+                  const pt_options *opt, void *stream);
+/* After synchronising the stream of the last pt_run_device on f: PT_OK,
+ * PT_ERR_TIMEOUT or PT_ERR_CUDA. */
+int pt_run_check(const pt_fields *f);
+
+/* ---- diagnostics --------------------------------------------------------- */
+
+const char *pt_last_error(void);
+int32_t pt_abi_version(void);
+/* The tableau compiled into the kernels (same packing as the oracle's
+ * or_tableau), so tests can compare coefficients bit for bit without a GPU. */
+int32_t pt_tableau(int32_t which, double *out);
+
+/* Throughput probe for roofline denominators: kind 0 FP64 FMA, 1 FP32 FMA;
+ * writes flop/s (FMA = 2 flops) measured on the current device. */
+int pt_probe_peak(int32_t kind, int32_t iters, double *flops_per_s);
+
+/* Device-side evaluation helpers for the parity tests (device pointers). */
+int pt_debug_pow(int64_t n, const double *d_x, const double *d_y, double *d_out, void *stream);
+int pt_debug_accel(const pt_fields *f, int64_t n, const double params[17],
+                   const double *d_vec, double *d_acc, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PARTICLES_GB300_H */

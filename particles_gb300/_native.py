@@ -1,0 +1,96 @@
+"""ctypes binding of ``libparticles_gb300.so`` (the C ABI in include/particles_gb300.h).
+
+The library is built in-tree by ``particles_gb300.build`` (nvcc, sm_103a).  If
+it is missing it is built on first use; if that fails, import fails loudly.
+There is no CPU fallback anywhere in the package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+from . import build as _build
+
+PT_METHOD_RK5, PT_METHOD_DOP853 = 1, 2
+PT_PREC_FP64, PT_PREC_FP64_FMA, PT_PREC_FP32, PT_PREC_BF16 = 0, 1, 2, 3
+PT_OK, PT_ERR_ARG, PT_ERR_CUDA, PT_ERR_NOMEM = 0, -1, -2, -3
+PT_ERR_TIMEOUT, PT_ERR_UNSUPPORTED, PT_ERR_PARTICLE = -4, -5, -6
+PT_ST_DONE, PT_ST_RUNNING, PT_ST_ESCAPED, PT_ST_NOT_RUN = 0, 1, 2, -1
+PT_ST_STEP_LIMIT, PT_ST_DT_UNDERFLOW, PT_ST_NONFINITE, PT_ST_TIMEOUT = -2, -3, -4, -5
+
+PRECISIONS = {"fp64": PT_PREC_FP64, "fp64_fma": PT_PREC_FP64_FMA,
+              "fp32": PT_PREC_FP32, "bf16": PT_PREC_BF16}
+
+# Every symbol include/particles_gb300.h declares (checked by the CPU tests).
+EXPORTS = [
+    "pt_integrate", "pt_method_from_name", "pt_fields_create", "pt_fields_create_device",
+    "pt_fields_destroy", "pt_fields_bytes", "pt_integrate_fields", "pt_carry_bytes",
+    "pt_run_device", "pt_run_check", "pt_last_error", "pt_abi_version", "pt_tableau",
+    "pt_debug_pow", "pt_debug_accel", "pt_probe_peak",
+]
+
+
+class PtOptions(C.Structure):
+    _fields_ = [
+        ("struct_size", C.c_int32), ("precision", C.c_int32), ("open_x", C.c_int32),
+        ("controller", C.c_int32), ("max_steps", C.c_int64), ("eta", C.c_double),
+        ("jj", C.c_void_p), ("t_stop", C.c_double), ("time_budget_s", C.c_double),
+        ("status", C.c_void_p), ("carry", C.c_void_p), ("model", C.c_void_p),
+        ("reserved", C.c_int64 * 4),
+    ]
+
+
+class PtError(RuntimeError):
+    def __init__(self, code: int, where: str, message: str):
+        super().__init__(f"{where}: code {code}: {message}")
+        self.code = code
+
+
+_lib = None
+
+
+def lib_path() -> Path:
+    return _build.LIB
+
+
+def load():
+    """Load (building first if needed) the native library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build()
+    L = C.CDLL(str(path))
+    vp, i32, i64, d = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+    L.pt_integrate.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.pt_method_from_name.argtypes = [C.c_char_p]
+    L.pt_method_from_name.restype = i32
+    L.pt_fields_create.argtypes = [vp, vp, vp, vp, i32, C.POINTER(vp)]
+    L.pt_fields_create_device.argtypes = [vp, vp, vp, vp, i32, vp, C.POINTER(vp)]
+    L.pt_fields_destroy.argtypes = [vp]
+    L.pt_fields_bytes.argtypes = [vp]
+    L.pt_fields_bytes.restype = i64
+    L.pt_integrate_fields.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp]
+    L.pt_carry_bytes.argtypes = [i64]
+    L.pt_carry_bytes.restype = i64
+    L.pt_run_device.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.pt_run_check.argtypes = [vp]
+    L.pt_last_error.restype = C.c_char_p
+    L.pt_abi_version.restype = i32
+    L.pt_tableau.argtypes = [i32, vp]
+    L.pt_tableau.restype = i32
+    L.pt_debug_pow.argtypes = [i64, vp, vp, vp, vp]
+    L.pt_debug_accel.argtypes = [vp, i64, vp, vp, vp, vp]
+    L.pt_probe_peak.argtypes = [i32, i32, C.POINTER(d)]
+    _lib = L
+    return L
+
+
+def check(rc: int, where: str) -> int:
+    if rc != PT_OK:
+        msg = load().pt_last_error().decode(errors="replace")
+        raise PtError(rc, where, msg)
+    return rc
+
+
+def last_error() -> str:
+    return load().pt_last_error().decode(errors="replace")

@@ -1,0 +1,89 @@
+"""Build recipe of the native library ``libparticles_gb300.so`` (sm_103a only).
+
+Plain ``nvcc`` invocations, one per translation unit, run in parallel, then
+one link.  The FP64 kernel source is compiled twice: ``exact`` with
+``--fmad=false`` (bit-identical to the CPU oracle) and ``fma`` with FMA
+contraction.  Host code is compiled with ``-ffp-contract=off`` so that host
+arithmetic (parameter unpacking) rounds the same on x86-64 and aarch64.
+Outputs go to ``particles_gb300/_build/`` (git-ignored).
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+OUT = PKG / "_build"
+LIB = OUT / "libparticles_gb300.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = [
+    "-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr",
+    "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math",
+    "-I", str(PKG.parent / "include"),
+]
+
+# (output object, source, extra flags)
+UNITS = [
+    ("pt_api.o", "pt_api.cu", ["--fmad=false"]),
+    ("pt_fp64_exact.o", "pt_fp64.cu", ["--fmad=false", "-DPT_SFX=exact"]),
+    ("pt_fp64_fma.o", "pt_fp64.cu", ["--fmad=true", "-DPT_SFX=fma"]),
+    ("pt_probe.o", "pt_probe.cu", ["--fmad=true"]),
+]
+
+
+def nvcc() -> str:
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(exe).exists():
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build particles_gb300")
+    return exe
+
+
+def _sources_newer_than(target: Path) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    deps = list(CSRC.glob("*")) + [PKG.parent / "include" / "particles_gb300.h", Path(__file__)]
+    return any(d.stat().st_mtime > t for d in deps if d.is_file())
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile and link the library if any source is newer; return its path."""
+    if not force and not _sources_newer_than(LIB):
+        return LIB
+    OUT.mkdir(parents=True, exist_ok=True)
+    exe = nvcc()
+    ptx_v = ["-Xptxas", "-v"] if verbose else []
+
+    def compile_unit(u):
+        obj, src, extra = u
+        cmd = [exe, *ARCH, *COMMON, *extra, *ptx_v, "-c", str(CSRC / src), "-o", str(OUT / obj)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        return obj, cmd, r
+
+    with ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+        results = list(ex.map(compile_unit, UNITS))
+    log = []
+    for obj, cmd, r in results:
+        log.append(f"$ {' '.join(cmd)}\n{r.stdout}{r.stderr}")
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {obj}:\n{r.stdout}\n{r.stderr}")
+    tmp = LIB.with_suffix(".so.tmp")
+    link = [exe, *ARCH, "-shared", "-o", str(tmp), *[str(OUT / u[0]) for u in UNITS]]
+    r = subprocess.run(link, capture_output=True, text=True)
+    log.append(f"$ {' '.join(link)}\n{r.stdout}{r.stderr}")
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    (OUT / "build.log").write_text("\n".join(log))
+    return LIB
+
+
+if __name__ == "__main__":
+    p = build(force="--force" in sys.argv, verbose="-v" in sys.argv)
+    print(p)

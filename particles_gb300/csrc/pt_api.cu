@@ -1,0 +1,452 @@
+/*
+ * pt_api.cu -- the C ABI (include/particles_gb300.h): field handles, argument
+ * checking, parameter unpacking, host/device transfers and kernel dispatch.
+ *
+ * The one-shot pt_integrate() is the drop-in for the reference's dispatch
+ * loop (sources/particles.F90:337-356 with its OpenACC data region
+ * `copy(state) copyin(dm,uu,bb,time)` at :340,349): it uploads the fields,
+ * runs the fused kernel over all particles and copies state and counters back.
+ * Nothing here calls a CPU fallback: without a usable GPU every entry point
+ * returns PT_ERR_CUDA.
+ */
+#include <cuda_runtime.h>
+
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+#include <strings.h>
+
+#include "pt_common.cuh"
+#include "pt_detmath.h"
+#include "pt_tableau.h"
+
+/* ---------------------------------------------------------------------- */
+/* errors                                                                 */
+/* ---------------------------------------------------------------------- */
+
+static thread_local char g_err[512] = "";
+
+static int set_err(int code, const char *fmt, const char *detail = nullptr)
+{
+    snprintf(g_err, sizeof g_err, fmt, detail ? detail : "");
+    return code;
+}
+
+static int cuda_err(cudaError_t e, const char *where)
+{
+    snprintf(g_err, sizeof g_err, "%s: %s", where, cudaGetErrorString(e));
+    return (e == cudaErrorMemoryAllocation) ? PT_ERR_NOMEM : PT_ERR_CUDA;
+}
+
+#define PT_CU(call)                                                   \
+    do {                                                              \
+        cudaError_t e_ = (call);                                      \
+        if (e_ != cudaSuccess) { rc = cuda_err(e_, #call); goto done; } \
+    } while (0)
+
+extern "C" const char *pt_last_error(void) { return g_err; }
+extern "C" int32_t pt_abi_version(void) { return PT_ABI_VERSION; }
+
+/* ---------------------------------------------------------------------- */
+/* field handles                                                          */
+/* ---------------------------------------------------------------------- */
+
+struct pt_fields {
+    int32_t dm[3];
+    int32_t precision;
+    int32_t nc;                 /* FP64 record width: 6 or 10 */
+    int32_t has_j;
+    int32_t device;
+    int64_t nodes;
+    double *rec64;              /* FP64 records */
+    int64_t bytes;
+    unsigned long long *scratch;   /* [0] queue head, [1] flags (2 x int32) */
+};
+
+/* Planar reference layout -> node records { U, B, (J, 0) }. */
+__global__ void k_pack_records64(int64_t nn, const double *__restrict__ uu,
+                                 const double *__restrict__ bb, const double *__restrict__ jj,
+                                 int nc, double *__restrict__ rec)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double v[10];
+        for (int c = 0; c < 3; ++c) { v[c] = uu[i + c * nn]; v[3 + c] = bb[i + c * nn]; }
+        if (nc == 10) {
+            for (int c = 0; c < 3; ++c) v[6 + c] = jj[i + c * nn];
+            v[9] = 0.0;
+        }
+        double2 *o = reinterpret_cast<double2 *>(rec + i * nc);
+        for (int c = 0; c < nc / 2; ++c) o[c] = make_double2(v[2 * c], v[2 * c + 1]);
+    }
+}
+
+static bool dims_ok(const int32_t dm[3])
+{
+    if (!dm) return false;
+    for (int i = 0; i < 3; ++i)
+        if (dm[i] < 1 || dm[i] > (1 << 16)) return false;
+    const int64_t n = (int64_t)dm[0] * dm[1] * dm[2];
+    return n * 10 < ((int64_t)1 << 40);
+}
+
+static int fields_create_impl(const int32_t dm[3], const double *uu, const double *bb,
+                              const double *jj, int32_t precision, bool on_device,
+                              cudaStream_t stream, pt_fields **out)
+{
+    if (!out) return set_err(PT_ERR_ARG, "pt_fields_create: out is NULL%s");
+    *out = nullptr;
+    if (!dims_ok(dm)) return set_err(PT_ERR_ARG, "pt_fields_create: bad dm%s");
+    if (!uu || !bb) return set_err(PT_ERR_ARG, "pt_fields_create: uu/bb is NULL%s");
+    if (precision != PT_PREC_FP64 && precision != PT_PREC_FP64_FMA)
+        return set_err(PT_ERR_UNSUPPORTED, "pt_fields_create: precision not built%s");
+
+    int rc = PT_OK;
+    pt_fields *f = new pt_fields();
+    double *d_uu = nullptr, *d_bb = nullptr, *d_jj = nullptr;
+    const int64_t nn = (int64_t)dm[0] * dm[1] * dm[2];
+    const size_t plane3 = (size_t)nn * 3 * sizeof(double);
+    for (int i = 0; i < 3; ++i) f->dm[i] = dm[i];
+    f->precision = precision;
+    f->has_j = jj != nullptr;
+    f->nc = f->has_j ? 10 : 6;
+    f->nodes = nn;
+    PT_CU(cudaGetDevice(&f->device));
+    PT_CU(cudaMalloc(&f->scratch, 256));
+    PT_CU(cudaMalloc(&f->rec64, (size_t)nn * f->nc * sizeof(double)));
+    f->bytes = (int64_t)nn * f->nc * sizeof(double) + 256;
+    if (on_device) {
+        d_uu = const_cast<double *>(uu);
+        d_bb = const_cast<double *>(bb);
+        d_jj = const_cast<double *>(jj);
+    } else {
+        PT_CU(cudaMalloc(&d_uu, plane3));
+        PT_CU(cudaMalloc(&d_bb, plane3));
+        PT_CU(cudaMemcpyAsync(d_uu, uu, plane3, cudaMemcpyHostToDevice, stream));
+        PT_CU(cudaMemcpyAsync(d_bb, bb, plane3, cudaMemcpyHostToDevice, stream));
+        if (jj) {
+            PT_CU(cudaMalloc(&d_jj, plane3));
+            PT_CU(cudaMemcpyAsync(d_jj, jj, plane3, cudaMemcpyHostToDevice, stream));
+        }
+    }
+    {
+        int64_t blocks = (nn + 255) / 256;
+        if (blocks > 65536) blocks = 65536;
+        k_pack_records64<<<(int)blocks, 256, 0, stream>>>(nn, d_uu, d_bb, d_jj, f->nc, f->rec64);
+        PT_CU(cudaGetLastError());
+    }
+    PT_CU(cudaStreamSynchronize(stream));
+done:
+    if (!on_device) {
+        cudaFree(d_uu);
+        cudaFree(d_bb);
+        cudaFree(d_jj);
+    }
+    if (rc != PT_OK) {
+        cudaFree(f->rec64);
+        cudaFree(f->scratch);
+        delete f;
+        return rc;
+    }
+    *out = f;
+    return PT_OK;
+}
+
+extern "C" int pt_fields_create(const int32_t dm[3], const double *uu, const double *bb,
+                                const double *jj, int32_t precision, pt_fields **out)
+{
+    return fields_create_impl(dm, uu, bb, jj, precision, false, (cudaStream_t)0, out);
+}
+
+extern "C" int pt_fields_create_device(const int32_t dm[3], const double *d_uu,
+                                       const double *d_bb, const double *d_jj,
+                                       int32_t precision, void *stream, pt_fields **out)
+{
+    return fields_create_impl(dm, d_uu, d_bb, d_jj, precision, true, (cudaStream_t)stream, out);
+}
+
+extern "C" int pt_fields_destroy(pt_fields *f)
+{
+    if (!f) return PT_OK;
+    cudaFree(f->rec64);
+    cudaFree(f->scratch);
+    delete f;
+    return PT_OK;
+}
+
+extern "C" int64_t pt_fields_bytes(const pt_fields *f) { return f ? f->bytes : 0; }
+
+extern "C" int64_t pt_carry_bytes(int64_t np)
+{
+    return np > 0 ? np * PT_CARRY_BYTES_PER_PARTICLE : 0;
+}
+
+extern "C" int32_t pt_method_from_name(const char *name)
+{
+    if (!name) return 0;
+    /* particles.F90:337-347 compares trim(method) case-sensitively */
+    char b[33];
+    size_t n = strlen(name);
+    while (n > 0 && name[n - 1] == ' ') --n;
+    if (n == 0 || n > 32) return 0;
+    memcpy(b, name, n);
+    b[n] = 0;
+    if (!strcmp(b, "rk5")) return PT_METHOD_RK5;
+    if (!strcmp(b, "dop853") || !strcmp(b, "dp853") || !strcmp(b, "rk8")) return PT_METHOD_DOP853;
+    return 0;
+}
+
+/* ---------------------------------------------------------------------- */
+/* runs                                                                   */
+/* ---------------------------------------------------------------------- */
+
+static void unpack_params(const double *p, const pt_fields *f, PtRun &R)
+{
+    memset(&R, 0, sizeof R);
+    R.qom = p[0]; R.vun = p[1]; R.tmx = p[2]; R.dtm = p[4];
+    R.atol = p[5]; R.rtol = p[6]; R.fcmn = p[7]; R.fcmx = p[8]; R.safe = p[9];
+    R.beta = p[10];
+    R.expo = 2.0e-01 * R.beta - 1.25e-01;                     /* integrations.F90:348 */
+    bool unit = true;
+    for (int i = 0; i < 3; ++i) {
+        R.xl[i] = p[11 + i];
+        R.xs[i] = p[14 + i];
+        R.dm[i] = f->dm[i];
+        R.dmr[i] = (double)f->dm[i];
+        R.inv_dm[i] = 1.0 / (double)f->dm[i];
+        unit = unit && (R.xl[i] == 0.0) && !signbit(R.xl[i]) && (R.xs[i] == 1.0);
+    }
+    R.unit_map = unit ? 1 : 0;
+}
+
+static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
+                    const double *params, const double *d_time, double *d_state, int64_t *d_cnt,
+                    int32_t *d_status, void *d_carry, const pt_options *opt, cudaStream_t s)
+{
+    if (method != PT_METHOD_RK5 && method != PT_METHOD_DOP853)
+        return set_err(PT_ERR_ARG, "unknown method%s");
+    if (!f) return set_err(PT_ERR_ARG, "fields handle is NULL%s");
+    if (np < 0 || m < 1) return set_err(PT_ERR_ARG, "np < 0 or m < 1%s");
+    if (!params) return set_err(PT_ERR_ARG, "params is NULL%s");
+    if (np > 0 && (!d_time || !d_state || !d_cnt)) return set_err(PT_ERR_ARG, "NULL buffer%s");
+    if ((int64_t)m * np * 8 > ((int64_t)1 << 62)) return set_err(PT_ERR_ARG, "state too large%s");
+    for (int i = 0; i < 17; ++i)
+        if (i != 3 && !isfinite(params[i])) return set_err(PT_ERR_ARG, "non-finite params%s");
+    if (params[14] == 0.0 || params[15] == 0.0 || params[16] == 0.0)
+        return set_err(PT_ERR_ARG, "zero domain size%s");
+
+    int32_t precision = f->precision;
+    double eta = 0.0, t_stop = 0.0, budget = 0.0;
+    int32_t open_x = 0;
+    int64_t max_steps = 0;
+    if (opt) {
+        if (opt->precision != f->precision)
+            return set_err(PT_ERR_ARG, "options precision differs from the field handle%s");
+        if (opt->controller != 0)
+            return set_err(PT_ERR_UNSUPPORTED, "learned controller not available for this precision%s");
+        eta = opt->eta;
+        t_stop = opt->t_stop;
+        budget = opt->time_budget_s;
+        open_x = opt->open_x;
+        max_steps = opt->max_steps;
+    }
+    if (eta != 0.0 && !f->has_j)
+        return set_err(PT_ERR_ARG, "eta != 0 needs a field handle created with J%s");
+    if (eta == 0.0 && f->has_j)
+        return set_err(PT_ERR_ARG, "field handle holds J but eta == 0%s");
+
+    PtRun R;
+    unpack_params(params, f, R);
+    R.eta = eta;
+    R.has_j = f->has_j;
+    R.open_x = open_x ? 1 : 0;
+    R.max_steps = max_steps > 0 ? max_steps : 1000000000LL;
+    R.tend = (t_stop > 0.0 && t_stop < R.tmx) ? t_stop : R.tmx;
+    R.budget_ns = (uint64_t)((budget > 0.0 ? budget : 600.0) * 1e9);
+    R.m = m;
+    R.np = np;
+    R.fld = f->rec64;
+    R.time = d_time;
+    R.state = d_state;
+    R.cnt = d_cnt;
+    R.status = d_status;
+    R.carry = static_cast<unsigned char *>(d_carry);
+    R.queue = f->scratch;
+    R.flags = reinterpret_cast<int32_t *>(f->scratch + 1);
+
+    cudaError_t e;
+    if (d_status && np > 0) {
+        e = cudaMemsetAsync(d_status, 0xff, (size_t)np * sizeof(int32_t), s);
+        if (e != cudaSuccess) return cuda_err(e, "status reset");
+    }
+    e = cudaMemsetAsync(f->scratch, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return cuda_err(e, "scratch reset");
+    if (precision == PT_PREC_FP64)
+        e = method == PT_METHOD_RK5 ? pt_launch_rk5_exact(R, f->nc, s) : pt_launch_dp853_exact(R, f->nc, s);
+    else
+        e = method == PT_METHOD_RK5 ? pt_launch_rk5_fma(R, f->nc, s) : pt_launch_dp853_fma(R, f->nc, s);
+    if (e != cudaSuccess) return cuda_err(e, "kernel launch");
+    return PT_OK;
+}
+
+extern "C" int pt_run_device(int32_t method, int64_t np, int32_t m, const pt_fields *f,
+                             const double params[17], const double *d_time, double *d_state,
+                             int64_t *d_cnt, int32_t *d_status, void *d_carry,
+                             const pt_options *opt, void *stream)
+{
+    return run_impl(method, np, m, f, params, d_time, d_state, d_cnt, d_status, d_carry, opt,
+                    (cudaStream_t)stream);
+}
+
+extern "C" int pt_run_check(const pt_fields *f)
+{
+    if (!f) return set_err(PT_ERR_ARG, "fields handle is NULL%s");
+    int32_t flags[2] = { 0, 0 };
+    cudaError_t e = cudaMemcpy(flags, f->scratch + 1, sizeof flags, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(e, "pt_run_check");
+    if (flags[0]) return set_err(PT_ERR_TIMEOUT, "time budget expired%s");
+    if (flags[1]) {
+        snprintf(g_err, sizeof g_err, "%d particle(s) ended with a negative status", flags[1]);
+        return PT_ERR_PARTICLE;
+    }
+    return PT_OK;
+}
+
+extern "C" int pt_integrate_fields(int32_t method, int64_t np, int32_t m, const pt_fields *f,
+                                   const double params[17], const double *time, double *state,
+                                   int64_t *cnt, const pt_options *opt)
+{
+    if (np < 0 || m < 1) return set_err(PT_ERR_ARG, "np < 0 or m < 1%s");
+    if (np > 0 && (!time || !state || !cnt)) return set_err(PT_ERR_ARG, "NULL buffer%s");
+    if (np == 0) return PT_OK;
+    int rc = PT_OK;
+    double *d_time = nullptr, *d_state = nullptr;
+    int64_t *d_cnt = nullptr;
+    int32_t *d_status = nullptr;
+    void *d_carry = nullptr;
+    const size_t sbytes = (size_t)8 * m * np * sizeof(double);
+    const size_t cbytes = (size_t)3 * np * sizeof(int64_t);
+    int32_t *h_status = opt ? opt->status : nullptr;
+    void *h_carry = opt ? opt->carry : nullptr;
+    cudaStream_t s = nullptr;
+    PT_CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    PT_CU(cudaMalloc(&d_time, (size_t)m * sizeof(double)));
+    PT_CU(cudaMalloc(&d_state, sbytes));
+    PT_CU(cudaMalloc(&d_cnt, cbytes));
+    PT_CU(cudaMalloc(&d_status, (size_t)np * sizeof(int32_t)));
+    PT_CU(cudaMemcpyAsync(d_time, time, (size_t)m * sizeof(double), cudaMemcpyHostToDevice, s));
+    PT_CU(cudaMemcpyAsync(d_state, state, sbytes, cudaMemcpyHostToDevice, s));
+    if (h_carry) {
+        PT_CU(cudaMalloc(&d_carry, (size_t)pt_carry_bytes(np)));
+        PT_CU(cudaMemcpyAsync(d_carry, h_carry, (size_t)pt_carry_bytes(np), cudaMemcpyHostToDevice, s));
+        PT_CU(cudaMemcpyAsync(d_cnt, cnt, cbytes, cudaMemcpyHostToDevice, s));
+    }
+    rc = run_impl(method, np, m, f, params, d_time, d_state, d_cnt, d_status, d_carry, opt, s);
+    if (rc != PT_OK) goto done;
+    PT_CU(cudaMemcpyAsync(state, d_state, sbytes, cudaMemcpyDeviceToHost, s));
+    PT_CU(cudaMemcpyAsync(cnt, d_cnt, cbytes, cudaMemcpyDeviceToHost, s));
+    if (h_status)
+        PT_CU(cudaMemcpyAsync(h_status, d_status, (size_t)np * sizeof(int32_t),
+                              cudaMemcpyDeviceToHost, s));
+    if (h_carry)
+        PT_CU(cudaMemcpyAsync(h_carry, d_carry, (size_t)pt_carry_bytes(np), cudaMemcpyDeviceToHost, s));
+    PT_CU(cudaStreamSynchronize(s));
+    rc = pt_run_check(f);
+done:
+    if (s) cudaStreamSynchronize(s);
+    cudaFree(d_time);
+    cudaFree(d_state);
+    cudaFree(d_cnt);
+    cudaFree(d_status);
+    cudaFree(d_carry);
+    if (s) cudaStreamDestroy(s);
+    return rc;
+}
+
+extern "C" int pt_integrate(int32_t method, int64_t np, int32_t m, const int32_t dm[3],
+                            const double params[17], const double *time, const double *uu,
+                            const double *bb, double *state, int64_t *cnt, const pt_options *opt)
+{
+    if (method != PT_METHOD_RK5 && method != PT_METHOD_DOP853)
+        return set_err(PT_ERR_ARG, "unknown method%s");
+    if (np < 0 || m < 1) return set_err(PT_ERR_ARG, "np < 0 or m < 1%s");
+    if (np == 0) return PT_OK;
+    const int32_t prec = opt ? opt->precision : PT_PREC_FP64;
+    const double *jj = (opt && opt->eta != 0.0) ? opt->jj : nullptr;
+    if (opt && opt->eta != 0.0 && !jj) return set_err(PT_ERR_ARG, "eta != 0 needs opt->jj%s");
+    pt_fields *f = nullptr;
+    int rc = pt_fields_create(dm, uu, bb, jj, prec, &f);
+    if (rc != PT_OK) return rc;
+    rc = pt_integrate_fields(method, np, m, f, params, time, state, cnt, opt);
+    pt_fields_destroy(f);
+    return rc;
+}
+
+/* ---------------------------------------------------------------------- */
+/* diagnostics                                                            */
+/* ---------------------------------------------------------------------- */
+
+extern "C" int32_t pt_tableau(int32_t which, double *out)
+{
+    using namespace pt_tab;
+    if (which == 1) {
+        const double v[37] = {
+            CK_B2_1, 0, 0, 0, 0,
+            CK_B3_1, CK_B3_2, 0, 0, 0,
+            CK_B4_1, CK_B4_2, CK_B4_3, 0, 0,
+            CK_B5_1, CK_B5_2, CK_B5_3, CK_B5_4, 0,
+            CK_B6_1, CK_B6_2, CK_B6_3, CK_B6_4, CK_B6_5,
+            CK_C1, CK_C2, CK_C3, CK_C4, CK_C5, CK_C6,
+            CK_D1, CK_D2, CK_D3, CK_D4, CK_D5, CK_D6 };
+        if (out) memcpy(out, v, sizeof v);
+        return 37;
+    }
+    if (which == 2) {
+        const double v[] = {
+            A0201, A0301, A0302, A0401, A0403, A0501, A0503, A0504, A0601, A0604, A0605,
+            A0701, A0704, A0705, A0706, A0801, A0804, A0805, A0806, A0807,
+            A0901, A0904, A0905, A0906, A0907, A0908,
+            A1001, A1004, A1005, A1006, A1007, A1008, A1009,
+            A1101, A1104, A1105, A1106, A1107, A1108, A1109, A1110,
+            A1201, A1204, A1205, A1206, A1207, A1208, A1209, A1210, A1211,
+            B01, B06, B07, B08, B09, B10, B11, B12, BH1, BH2, BH3,
+            ER01, ER06, ER07, ER08, ER09, ER10, ER11, ER12 };
+        if (out) memcpy(out, v, sizeof v);
+        return (int32_t)(sizeof v / sizeof v[0]);
+    }
+    return 0;
+}
+
+__global__ void k_debug_pow(int64_t n, const double *x, const double *y, double *o)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        o[i] = pt_det_pow(x[i], y[i]);
+}
+
+extern "C" int pt_debug_pow(int64_t n, const double *d_x, const double *d_y, double *d_out,
+                            void *stream)
+{
+    if (n <= 0) return PT_OK;
+    if (!d_x || !d_y || !d_out) return set_err(PT_ERR_ARG, "NULL buffer%s");
+    const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    k_debug_pow<<<grid, 256, 0, (cudaStream_t)stream>>>(n, d_x, d_y, d_out);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_pow");
+}
+
+extern "C" int pt_debug_accel(const pt_fields *f, int64_t n, const double params[17],
+                              const double *d_vec, double *d_acc, void *stream)
+{
+    if (!f || !params) return set_err(PT_ERR_ARG, "NULL argument%s");
+    if (n <= 0) return PT_OK;
+    PtRun R;
+    unpack_params(params, f, R);
+    R.fld = f->rec64;
+    R.has_j = f->has_j;
+    R.eta = 0.0;
+    cudaError_t e = (f->precision == PT_PREC_FP64)
+        ? pt_launch_accel_exact(R, f->nc, n, d_vec, d_acc, (cudaStream_t)stream)
+        : pt_launch_accel_fma(R, f->nc, n, d_vec, d_acc, (cudaStream_t)stream);
+    return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_accel");
+}

@@ -1,0 +1,125 @@
+/*
+ * pt_common.cuh -- definitions shared by the kernels and the C ABI.
+ *
+ * Device data layout (all in HBM, written once per field handle):
+ *   FP64 field records: for node (i,j,k), x fastest, one record of NC doubles
+ *     { Ux, Uy, Uz, Bx, By, Bz }            NC = 6  (48 B, 3 x 16-B loads)
+ *     { Ux, Uy, Uz, Bx, By, Bz, Jx, Jy, Jz, 0 } NC = 10 (80 B, with eta J)
+ *   so one trilinear corner is 2-3 contiguous 32-B sectors instead of the 6
+ *   separate planes of the reference layout uu(dm1,dm2,dm3,3), bb(...).
+ *   Particle state keeps the reference layout state(8,m,np); each output
+ *   sample is one aligned 64-B row.  The controller memory (carry) is SoA.
+ */
+#ifndef PT_COMMON_CUH
+#define PT_COMMON_CUH
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#include "../../include/particles_gb300.h"
+
+/* Everything a particle-integration kernel reads, by value in the launch. */
+struct PtRun {
+    /* params(1:17) unpacked as integrations.F90:103-118,330-346 */
+    double qom, vun, tmx, dtm, atol, rtol, fcmn, fcmx, safe, beta, expo;
+    double xl[3], xs[3];
+    /* grid */
+    double inv_dm[3], dmr[3];
+    int32_t dm[3];
+    int32_t unit_map;      /* xl == +0 and xs == 1: (pos - xl) / xs == pos exactly */
+    /* extensions */
+    double eta;
+    int32_t has_j;
+    int32_t open_x;
+    int64_t max_steps;
+    double tend;           /* min(t_stop, tmx) */
+    uint64_t budget_ns;
+    /* sizes */
+    int32_t m;
+    int64_t np;
+    /* device pointers */
+    const double *fld;     /* FP64 records */
+    const float *fld32;    /* FP32 records (mixed precision) */
+    const double *time;
+    double *state;
+    int64_t *cnt;
+    int32_t *status;
+    unsigned char *carry;  /* SoA carry or NULL */
+    unsigned long long *queue;  /* work-queue head */
+    int32_t *flags;        /* [0] time budget hit, [1] particles with negative status */
+};
+
+/* Carry (controller memory) SoA layout inside one buffer of 80*np bytes:
+ *   double t[np], dt[np], errold[np], si[6][np]; int32 n[np], flags[np]
+ * flags bit0 = started, bit1 = the previous DOP853 attempt was rejected. */
+struct PtCarry {
+    double *t, *dt, *errold, *si;
+    int32_t *n, *flags;
+};
+
+__host__ __device__ inline PtCarry pt_carry_view(unsigned char *base, int64_t np)
+{
+    PtCarry c;
+    double *d = reinterpret_cast<double *>(base);
+    c.t = d;
+    c.dt = d + np;
+    c.errold = d + 2 * np;
+    c.si = d + 3 * np;
+    int32_t *i = reinterpret_cast<int32_t *>(d + 9 * np);
+    c.n = i;
+    c.flags = i + np;
+    return c;
+}
+
+#define PT_CARRY_BYTES_PER_PARTICLE 80
+
+/* Fortran MIN/MAX with the NaN rule of the oracle (a NaN first operand
+ * propagates), and maxval with NaN propagation. */
+__device__ __forceinline__ double pt_max(double a, double b) { return (b > a) ? b : a; }
+__device__ __forceinline__ double pt_min(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double pt_nanmax(double m, double q) { return (q > m || q != q) ? q : m; }
+
+/* floor(xp) as a 0-based node index; dm (only reachable when x - floor(x)
+ * rounds up to 1 for a tiny negative x, where the reference indexes past the
+ * array) wraps to 0, NaN maps to 0.  Identical rule in the oracle. */
+__device__ __forceinline__ int32_t pt_node_index(double q, int32_t d)
+{
+    return (q >= 0.0 && q < (double)d) ? (int32_t)q : 0;
+}
+
+__device__ __forceinline__ uint64_t pt_globaltimer()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+/* Loop guard shared with the oracle: < 0 stops the particle before an attempt. */
+__device__ __forceinline__ int32_t pt_attempt_guard(double t, double dt, int64_t attempts,
+                                                    int64_t max_steps)
+{
+    if (max_steps > 0 && attempts >= max_steps) return PT_ST_STEP_LIMIT;
+    if (dt != dt) return PT_ST_NONFINITE;
+    if (!(dt > 0.0) || t + dt == t) return PT_ST_DT_UNDERFLOW;
+    return 1;
+}
+
+/* Launchers implemented by the kernel translation units. */
+struct PtLaunch {
+    int grid, block;
+    cudaStream_t stream;
+};
+
+#define PT_DECLARE_FP64_LAUNCHERS(sfx)                                            \
+    cudaError_t pt_launch_rk5_##sfx(const PtRun &P, int nc, cudaStream_t s);     \
+    cudaError_t pt_launch_dp853_##sfx(const PtRun &P, int nc, cudaStream_t s);   \
+    cudaError_t pt_launch_accel_##sfx(const PtRun &P, int nc, int64_t n,         \
+                                      const double *vec, double *acc, cudaStream_t s);
+
+PT_DECLARE_FP64_LAUNCHERS(exact)
+PT_DECLARE_FP64_LAUNCHERS(fma)
+
+cudaError_t pt_launch_debug_pow(int64_t n, const double *x, const double *y, double *out,
+                                cudaStream_t s);
+
+#endif /* PT_COMMON_CUH */

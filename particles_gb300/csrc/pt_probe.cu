@@ -1,0 +1,69 @@
+/*
+ * pt_probe.cu -- arithmetic-throughput probes used as roofline denominators.
+ *
+ * The FP64 kernels are bounded by the FP64 pipe, whose rate the measured-peak
+ * file of this machine does not list, so the benchmark measures it live on
+ * the same GPU: a grid of 8 independent FMA chains per thread, long enough
+ * (~50 ms) to reach steady clocks.  kind 0 = FP64 FMA, kind 1 = FP32 FMA.
+ * Result in flop/s with an FMA counted as 2 flops.
+ */
+#include <cuda_runtime.h>
+
+#include "pt_common.cuh"
+
+namespace {
+
+template <class T>
+__global__ void k_fma_chains(T *out, int iters, T a, T b)
+{
+    T x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = (T)(threadIdx.x + j) * (T)1e-3;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) x[j] = fma(x[j], a, b);
+    }
+    T s = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s += x[j];
+    if (s == (T)12345.678) out[0] = s;   /* keeps the chains alive; practically never true */
+}
+
+template <class T>
+double measure(int iters)
+{
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int block = 256, grid = sms * 8;
+    T *out = nullptr;
+    if (cudaMalloc(&out, sizeof(T)) != cudaSuccess) return -1.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    const T a = (T)0.999999, b = (T)1e-7;
+    k_fma_chains<T><<<grid, block>>>(out, iters / 8, a, b);   /* warm-up */
+    cudaEventRecord(e0);
+    k_fma_chains<T><<<grid, block>>>(out, iters, a, b);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (err != cudaSuccess || ms <= 0.f) return -1.0;
+    const double flops = 2.0 * 8.0 * (double)iters * (double)grid * block;
+    return flops / (ms * 1e-3);
+}
+
+}  // namespace
+
+extern "C" int pt_probe_peak(int32_t kind, int32_t iters, double *flops_per_s)
+{
+    if (!flops_per_s || iters <= 0) return PT_ERR_ARG;
+    double r = (kind == 0) ? measure<double>(iters) : measure<float>(iters);
+    *flops_per_s = r;
+    return r > 0 ? PT_OK : PT_ERR_CUDA;
+}

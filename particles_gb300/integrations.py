@@ -1,0 +1,174 @@
+"""Python face of the integrator, shaped like the reference's interface.
+
+``integrate_rk5`` / ``integrate_dp853`` take the arguments of the Fortran
+subroutines (sources/integrations.F90:57 and :224) -- m, dm, params, time, uu,
+bb, state, cnt -- but for all particles at once, and ``integrate`` is the
+driver's dispatch on the method string (particles.F90:337-356).  Every call
+goes through the C ABI of ``libparticles_gb300.so``; nothing runs on the CPU.
+
+Layouts (numpy C order == Fortran column-major):
+  uu, bb, jj : (3, dm3, dm2, dm1)      state : (np, m, 8)      cnt : (np, 3)
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .params import method_id
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _options(precision, *, eta=0.0, jj=None, open_x=False, max_steps=0, t_stop=0.0,
+             status=None, carry=None, time_budget_s=0.0):
+    o = N.PtOptions()
+    o.struct_size = C.sizeof(N.PtOptions)
+    o.precision = N.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+    o.open_x = int(bool(open_x))
+    o.controller = 0
+    o.max_steps = int(max_steps)
+    o.eta = float(eta)
+    o.jj = _ptr(jj)
+    o.t_stop = float(t_stop)
+    o.time_budget_s = float(time_budget_s)
+    o.status = _ptr(status)
+    o.carry = _ptr(carry)
+    return o
+
+
+def carry_buffer(npart: int) -> np.ndarray:
+    """Zero-filled (fresh) host controller memory for resumable windows."""
+    return np.zeros(int(N.load().pt_carry_bytes(npart)), np.uint8)
+
+
+def integrate(method, params, time, uu, bb, state, cnt=None, *, precision="fp64", eta=0.0,
+              jj=None, open_x=False, max_steps=0, t_stop=0.0, carry=None, status=None,
+              time_budget_s=0.0, check=True):
+    """Integrate every particle of ``state`` in place on the GPU.
+
+    Returns (state, cnt, status).  With ``check`` a negative return code
+    raises ``PtError``; otherwise the code is in ``status``/``pt_last_error``.
+    """
+    L = N.load()
+    mid = method_id(method)
+    assert state.dtype == np.float64 and state.flags.c_contiguous and state.ndim == 3
+    npart, m, eight = state.shape
+    assert eight == 8
+    if cnt is None:
+        cnt = np.zeros((npart, 3), np.int64)
+    if status is None:
+        status = np.zeros(npart, np.int32)
+    uu, bb = _f64(uu), _f64(bb)
+    jj = _f64(jj) if jj is not None else None
+    dm = np.array(uu.shape[:0:-1], np.int32)
+    opt = _options(precision, eta=eta, jj=jj, open_x=open_x, max_steps=max_steps,
+                   t_stop=t_stop, status=status, carry=carry, time_budget_s=time_budget_s)
+    rc = L.pt_integrate(mid, npart, m, _ptr(dm), _ptr(_f64(params)), _ptr(_f64(time)),
+                        _ptr(uu), _ptr(bb), _ptr(state), _ptr(cnt), C.byref(opt))
+    if check:
+        N.check(rc, "pt_integrate")
+    return state, cnt, status
+
+
+def integrate_rk5(m, dm, params, time, uu, bb, state, cnt, **kw):
+    """Batched integrations.F90:57 (`integrate_rk5(m, dm, params, time, uu, bb, state, cnt)`)."""
+    assert state.shape[1] == m and tuple(uu.shape[:0:-1]) == tuple(dm)
+    return integrate("rk5", params, time, uu, bb, state, cnt, **kw)
+
+
+def integrate_dp853(m, dm, params, time, uu, bb, state, cnt, **kw):
+    """Batched integrations.F90:224 (`integrate_dp853(...)`)."""
+    assert state.shape[1] == m and tuple(uu.shape[:0:-1]) == tuple(dm)
+    return integrate("dop853", params, time, uu, bb, state, cnt, **kw)
+
+
+class Fields:
+    """Fields uploaded once and converted to the kernel layout on the device.
+
+    ``uu``, ``bb`` (and ``jj``) are numpy host arrays or CUDA torch tensors in
+    the reference layout.
+    """
+
+    def __init__(self, uu, bb, jj=None, precision="fp64", stream=None):
+        self._L = N.load()
+        self.precision = precision
+        self._h = C.c_void_p()
+        prec = N.PRECISIONS[precision]
+        dm = np.array(tuple(uu.shape[:0:-1]), np.int32)
+        self.dm = tuple(int(x) for x in dm)
+        self.has_j = jj is not None
+        if isinstance(uu, np.ndarray):
+            uu, bb = _f64(uu), _f64(bb)
+            jj = _f64(jj) if jj is not None else None
+            rc = self._L.pt_fields_create(_ptr(dm), _ptr(uu), _ptr(bb), _ptr(jj), prec,
+                                          C.byref(self._h))
+        else:
+            rc = self._L.pt_fields_create_device(
+                _ptr(dm), C.c_void_p(uu.data_ptr()), C.c_void_p(bb.data_ptr()),
+                C.c_void_p(jj.data_ptr()) if jj is not None else None, prec,
+                C.c_void_p(stream) if stream else None, C.byref(self._h))
+        N.check(rc, "pt_fields_create")
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def nbytes(self) -> int:
+        return int(self._L.pt_fields_bytes(self._h))
+
+    def close(self):
+        if self._h:
+            self._L.pt_fields_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def integrate(self, method, params, time, state, cnt=None, *, eta=0.0, open_x=False,
+                  max_steps=0, t_stop=0.0, carry=None, status=None, time_budget_s=0.0,
+                  check=True):
+        """Host-buffer run on these fields (pt_integrate_fields)."""
+        npart, m, _ = state.shape
+        if cnt is None:
+            cnt = np.zeros((npart, 3), np.int64)
+        if status is None:
+            status = np.zeros(npart, np.int32)
+        opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
+                       t_stop=t_stop, status=status, carry=carry, time_budget_s=time_budget_s)
+        rc = self._L.pt_integrate_fields(method_id(method), npart, m, self._h,
+                                         _ptr(_f64(params)), _ptr(_f64(time)), _ptr(state),
+                                         _ptr(cnt), C.byref(opt))
+        if check:
+            N.check(rc, "pt_integrate_fields")
+        return state, cnt, status
+
+    def run_device(self, method, params, d_time, d_state, d_cnt, d_status=None, d_carry=None,
+                   *, eta=0.0, open_x=False, max_steps=0, t_stop=0.0, time_budget_s=0.0,
+                   stream=0):
+        """Launch on device tensors (torch); returns without synchronising."""
+        npart, m, _ = d_state.shape
+        opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
+                       t_stop=t_stop, time_budget_s=time_budget_s)
+        rc = self._L.pt_run_device(
+            method_id(method), npart, m, self._h, _ptr(_f64(params)),
+            C.c_void_p(d_time.data_ptr()), C.c_void_p(d_state.data_ptr()),
+            C.c_void_p(d_cnt.data_ptr()),
+            C.c_void_p(d_status.data_ptr()) if d_status is not None else None,
+            C.c_void_p(d_carry.data_ptr()) if d_carry is not None else None,
+            C.byref(opt), C.c_void_p(stream) if stream else None)
+        N.check(rc, "pt_run_device")
+
+    def run_check(self) -> int:
+        return int(self._L.pt_run_check(self._h))
