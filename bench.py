@@ -1,0 +1,426 @@
+#!/usr/bin/env python
+"""Benchmark: accepted particle-steps/s of the fused GB300 integrator.
+
+Workload (default, `dop853-256`): DOP853 FP64, rtol = atol = 1e-10, periodic
+256^3 grid, B = x^ + Kolmogorov dB (dB_rms = 1, |n| in [1, 32]), V of the same
+spectrum (V_rms = 0.2), E = -V x B + eta J with eta = 1e-3, 2^20 protons with
+uniform positions, isotropic directions and gamma log-uniform in [1.001, 1e3],
+t_end = 100 gyro-periods of B0 at gamma = 1 (qom = 200, c = 20, L = 1), dense
+output at every gyro-period.  Inputs are seeded synthetic data.
+
+A step is one window of that run: every particle advances from t to
+t + window (default 0.05 gyro-periods) with its controller memory carried, so
+successive steps continue the same trajectories the uninterrupted run
+follows (bit for bit).  Warm-up steps run the first windows; the timed steps
+the next ones.
+
+Reported (one JSON line, rank 0):
+  value      accepted particle-steps/s with everything resident in HBM,
+             device time over the K timed steps (CUDA events + barrier)
+  e2e        the same through the host-buffer C ABI (pt_integrate_fields):
+             pinned host state/counters/carry copied in and out every step
+  roofline   algorithmic FP64 flops of the timed kernel launches / their
+             CUDA-event time, against the FP64 FMA peak measured live
+  cpu_baseline  the CPU oracle (OpenMP, all host threads) on a seeded
+             particle subsample of the same windows
+
+`--impl reference` times the reference algorithm on the host cores (the CPU
+oracle, the restatement of sources/integrations.F90) on the same workload,
+each step a bounded particle sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+QOM, VUN = 200.0, 1.0 / 20.0
+T0 = 2.0 * math.pi / QOM
+
+WORKLOADS = {
+    # the benchmark spec's metric's FP64 configuration
+    "dop853-256": dict(method="dop853", n=256, spectrum="kolmogorov", nmax=32, db_rms=1.0,
+                       v_rms=0.2, eta=1e-3, npart=1 << 20, gamma=(1.001, 1e3), speed=None,
+                       tol=1e-10, periods=100, seed=1, window=0.05),
+    # the CPU-runnable configuration (reference RK5, 64^3, 1024 particles)
+    "rk5-64": dict(method="rk5", n=64, spectrum="flat", nmax=4, db_rms=0.5, v_rms=0.1,
+                   eta=0.0, npart=1024, gamma=None, speed=0.5, tol=1e-8, periods=10, seed=0,
+                   window=1.0),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="dop853-256")
+    ap.add_argument("--precision", choices=["fp64", "fp64_fma"], default="fp64")
+    ap.add_argument("--particles", type=int, default=0,
+                    help="override the particle count (profiling of small cases only)")
+    ap.add_argument("--window", type=float, default=0.0,
+                    help="override the window in gyro-periods (profiling only)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def build_inputs(cfg, npart, rank):
+    """Fields (reference layout), params, time grid and this rank's particles."""
+    from particles_gb300 import fields, initial, params
+    tmax = cfg["periods"] * T0
+    prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=tmax, atol=cfg["tol"],
+                             rtol=cfg["tol"], facmin=0.333, facmax=6.0, safe=0.9, beta=0.0)
+    tg = params.time_grid(cfg["periods"], tmax)
+    out = fields.snapshot(cfg["n"], db_rms=cfg["db_rms"], v_rms=cfg["v_rms"], vunit=VUN,
+                          spectrum=cfg["spectrum"], nmin=1.0, nmax=cfg["nmax"],
+                          seed=cfg["seed"], with_j=cfg["eta"] != 0.0)
+    idx = np.arange(rank * npart, (rank + 1) * npart, dtype=np.uint64)
+    s0 = initial.isotropic_state(npart, cfg["seed"], speed=cfg["speed"],
+                                 gamma_range=cfg["gamma"], index=idx)
+    return prm, tg, out, s0
+
+
+class ClockSampler:
+    """nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except (ValueError, IndexError):
+                continue
+            for name, v in zip(names, r[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _oracle_sample(cfg, s0_all, tg, nsub, seed=12345):
+    import oracle
+    idx = np.random.default_rng(seed).choice(s0_all.shape[0], nsub, replace=False)
+    idx.sort()
+    state = np.zeros((nsub, tg.size, 8))
+    state[:, 0, :6] = s0_all[idx]
+    return state, np.zeros((nsub, 3), np.int64), oracle.make_carry(nsub)
+
+
+def _oracle_window(cfg, prm, tg, out, sample, t_stop, nthreads):
+    import oracle
+    uu, bb = out[:2]
+    jj = out[2] if len(out) > 2 else None
+    state, cnt, carry = sample
+    oracle.integrate(cfg["method"], prm, tg, uu, bb, state, cnt, eta=cfg["eta"], jj=jj,
+                     carry=carry, t_stop=t_stop, nthreads=nthreads)
+
+
+def _calibrate(cfg, prm, tg, out, s0_all, window, nthreads, ncal=512):
+    """Seconds per particle of the first window on the host (CPU oracle)."""
+    sample = _oracle_sample(cfg, s0_all, tg, min(ncal, s0_all.shape[0]), seed=777)
+    t = time.perf_counter()
+    _oracle_window(cfg, prm, tg, out, sample, window * T0, nthreads)
+    return (time.perf_counter() - t) / sample[0].shape[0]
+
+
+def cpu_baseline(cfg, prm, tg, out, s0_all, window, warm, steps, seconds):
+    """The CPU oracle (test infrastructure, here only the timed baseline) with
+    all host threads on a seeded particle subsample, over exactly the windows
+    the GPU timed (after the same warm-up windows); the subsample is sized so
+    the timed part takes about ``seconds``."""
+    nthreads = os.cpu_count() or 1
+    per_particle = _calibrate(cfg, prm, tg, out, s0_all, window, nthreads)
+    nsub = int(seconds / max(per_particle * steps, 1e-9))
+    nsub = max(256, min(nsub, s0_all.shape[0]))
+    sample = _oracle_sample(cfg, s0_all, tg, nsub)
+    w = 0
+    for _ in range(warm):
+        w += 1
+        _oracle_window(cfg, prm, tg, out, sample, w * window * T0, nthreads)
+    cnt = sample[1]
+    acc0 = cnt[:, 1].sum()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        w += 1
+        _oracle_window(cfg, prm, tg, out, sample, w * window * T0, nthreads)
+    el = time.perf_counter() - t0
+    acc = float(cnt[:, 1].sum() - acc0)
+    return {"value": acc / el, "unit": "particle-steps/s", "cores": nthreads, "kind": "port",
+            "sample": f"{nsub} of the workload's {s0_all.shape[0]} particles (seeded choice) over "
+                      f"the same {steps} timed windows of {window} gyro-periods after {warm} "
+                      f"warm-up windows; {int(acc)} accepted steps in {el:.1f} s"}
+
+
+def run_reference(args, cfg, rank, world):
+    """--impl reference: the reference algorithm (CPU oracle) on the host cores,
+    each step one window of the workload over a seeded particle sample sized
+    to about 6 s of host time."""
+    if rank != 0:
+        return 0
+    npart = args.particles or cfg["npart"]
+    window = args.window or cfg["window"]
+    prm, tg, out, s0 = build_inputs(cfg, npart, 0)
+    nthreads = os.cpu_count() or 1
+    per_particle = _calibrate(cfg, prm, tg, out, s0, window, nthreads)
+    nsub = max(256, min(int(6.0 / max(per_particle, 1e-9)), npart))
+    sample = _oracle_sample(cfg, s0, tg, nsub)
+    w = 0
+    for _ in range(args.warmup):
+        w += 1
+        _oracle_window(cfg, prm, tg, out, sample, w * window * T0, nthreads)
+    cnt = sample[1]
+    acc0 = cnt[:, 1].sum()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        w += 1
+        _oracle_window(cfg, prm, tg, out, sample, w * window * T0, nthreads)
+    el = time.perf_counter() - t0
+    acc = float(cnt[:, 1].sum() - acc0)
+    v = acc / el
+    line = {
+        "impl": "reference", "metric": "accepted particle-steps/s", "value": v,
+        "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": workload_config(cfg, npart, window, args),
+        "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": nthreads,
+                         "kind": "port",
+                         "sample": f"{nsub} seeded particles of the workload's {npart}, windows "
+                                   f"of {window} gyro-periods ({args.warmup} warm-up, "
+                                   f"{args.steps} timed)"},
+        "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "the reference is Fortran and cannot be built here (no Fortran compiler); its "
+                "algorithm runs as the project's C++ restatement (oracle/), OpenMP over particles",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(cfg, npart, window, args):
+    return {
+        "workload": args.workload, "method": cfg["method"], "grid": f"{cfg['n']}^3",
+        "spectrum": cfg["spectrum"], "particles": npart, "rtol": cfg["tol"],
+        "t_end_gyroperiods": cfg["periods"], "window_gyroperiods": window,
+        "eta": cfg["eta"], "precision": args.precision,
+        "l2": "field records exceed the 129 MB L2 (inputs larger than L2; no flush)",
+    }
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    cfg = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        return run_reference(args, cfg, rank, world)
+
+    import torch
+    from particles_gb300 import Fields, roofline
+    from particles_gb300 import _native as N
+    import ctypes as C
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    npart = args.particles or cfg["npart"]
+    window = args.window or cfg["window"]
+    prm, tg, out, s0 = build_inputs(cfg, npart, rank)
+    uu, bb = out[:2]
+    jj = out[2] if len(out) > 2 else None
+    L = N.load()
+    m = tg.size
+    dev = torch.device("cuda", local)
+    f = Fields(uu, bb, jj, precision=args.precision)
+    rec_bytes = (10 if jj is not None else 6) * 8
+    stream = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(stream):
+        d_time = torch.tensor(tg, device=dev)
+        d_state = torch.zeros((npart, m, 8), dtype=torch.float64, device=dev)
+        d_state[:, 0, :6] = torch.tensor(s0, device=dev)
+        d_cnt = torch.zeros((npart, 3), dtype=torch.int64, device=dev)
+        d_status = torch.zeros(npart, dtype=torch.int32, device=dev)
+        d_carry = torch.zeros(int(L.pt_carry_bytes(npart)), dtype=torch.uint8, device=dev)
+    stream.synchronize()
+
+    def window_run(w):
+        f.run_device(cfg["method"], prm, d_time, d_state, d_cnt, d_status, d_carry,
+                     eta=cfg["eta"], t_stop=w * window * T0, time_budget_s=900.0,
+                     stream=stream.cuda_stream)
+
+    w = 0
+    for _ in range(args.warmup):
+        w += 1
+        window_run(w)
+    stream.synchronize()
+    if f.run_check() not in (N.PT_OK,):
+        raise RuntimeError(f"warm-up failed: {N.last_error()}")
+    acc0 = d_cnt.sum(0).cpu().numpy()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t_start = time.perf_counter()
+        for k in range(args.steps):
+            w += 1
+            ev[k][0].record(stream)
+            window_run(w)
+            ev[k][1].record(stream)
+        stream.synchronize()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t_start
+    if world > 1:
+        torch.distributed.barrier()
+    rc = f.run_check()
+    if rc != N.PT_OK:
+        raise RuntimeError(f"timed run failed: {N.last_error()}")
+    kern_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_s = sum(kern_ms) * 1e-3
+    c_now = d_cnt.cpu().numpy()
+    dcnt_tot = c_now.sum(0) - acc0
+    accepted = float(dcnt_tot[1])
+    elapsed = dev_s
+    if world > 1:
+        t = torch.tensor([elapsed, accepted], dtype=torch.float64, device=dev)
+        mx = t[:1].clone()
+        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+        sm = t[1:].clone()
+        torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
+        elapsed, accepted = float(mx.item()), float(sm.item())
+    value = accepted / elapsed
+
+    # roofline of the dominant (only) kernel: algorithmic FP64 flops / event time
+    flops = roofline.run_flops(cfg["method"], np.array([dcnt_tot]), with_eta=cfg["eta"] != 0.0,
+                               fresh=False, resumed=npart * args.steps)
+    achieved = flops / dev_s
+    pk = C.c_double()
+    L.pt_probe_peak(0, 16384, C.byref(pk))
+    peak = pk.value
+    roof = {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,
+            "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+            "peak_source": "FP64 FMA peak measured live on this GPU (pt_probe_peak); "
+                           "the measured-peaks file lists only HBM and bf16",
+            "flops_per_step": flops / args.steps,
+            "gather_bytes_per_step": roofline.gather_bytes(cfg["method"], np.array([dcnt_tot]),
+                                                           record_bytes=rec_bytes) / args.steps}
+
+    line = {
+        "metric": "accepted particle-steps/s (plain FP64 kernel)",
+        "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded fields and particles)",
+        "config": workload_config(cfg, npart, window, args),
+        "wall_s_timed": wall, "gpu_launches": args.steps,
+        "rejected_fraction": float(dcnt_tot[2] / max(dcnt_tot[0], 1)),
+        "attempts_per_s": float(dcnt_tot[0]) / elapsed,
+        "roofline": roof, "clocks": clocks.summary(),
+    }
+
+    # end to end through the host-buffer C ABI: pinned host copies every step
+    if not args.no_e2e and rank == 0:
+        h_state = torch.empty((npart, m, 8), dtype=torch.float64).pin_memory()
+        h_cnt = torch.empty((npart, 3), dtype=torch.int64).pin_memory()
+        h_carry = torch.empty(int(L.pt_carry_bytes(npart)), dtype=torch.uint8).pin_memory()
+        h_status = torch.empty(npart, dtype=torch.int32).pin_memory()
+        h_state.copy_(d_state.cpu())
+        h_cnt.copy_(d_cnt.cpu())
+        h_carry.copy_(d_carry.cpu())
+        e2e_acc0 = float(h_cnt[:, 1].sum())
+        k_e2e = max(1, min(args.steps, 4))
+        from particles_gb300.integrations import _options
+        from particles_gb300.params import method_id
+        t_e = time.perf_counter()
+        for _ in range(k_e2e):
+            w += 1
+            o = _options(args.precision, eta=cfg["eta"], t_stop=w * window * T0,
+                         status=None, carry=None, time_budget_s=900.0)
+            o.status = C.c_void_p(h_status.data_ptr())
+            o.carry = C.c_void_p(h_carry.data_ptr())
+            rc = L.pt_integrate_fields(method_id(cfg["method"]), npart, m, f.handle, prm.ctypes.data_as(C.c_void_p),
+                                       tg.ctypes.data_as(C.c_void_p),
+                                       C.c_void_p(h_state.data_ptr()), C.c_void_p(h_cnt.data_ptr()),
+                                       C.byref(o))
+            if rc != N.PT_OK:
+                raise RuntimeError(f"e2e step failed: {N.last_error()}")
+        el_e = time.perf_counter() - t_e
+        acc_e = float(h_cnt[:, 1].sum()) - e2e_acc0
+        bytes_in = tg.nbytes + h_state.numel() * 8 + h_cnt.numel() * 8 + h_carry.numel()
+        bytes_out = h_state.numel() * 8 + h_cnt.numel() * 8 + h_carry.numel() + h_status.numel() * 4
+        line["e2e"] = {"value": acc_e / el_e, "unit": "particle-steps/s",
+                       "h2d_bytes_per_step": int(bytes_in), "d2h_bytes_per_step": int(bytes_out),
+                       "steps": k_e2e, "api": "pt_integrate_fields (host pinned buffers)"}
+
+    if not args.no_cpu and rank == 0 and world == 1:
+        line["cpu_baseline"] = cpu_baseline(cfg, prm, tg, out, s0, window, args.warmup,
+                                            args.steps, args.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    f.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -149,6 +149,19 @@ int32_t pt_abi_version(void);
  * or_tableau), so tests can compare coefficients bit for bit without a GPU. */
 int32_t pt_tableau(int32_t which, double *out);
 
+/* The host-side unpacking of a run without launching it (no GPU needed):
+ * out = { tend, tmax, expo, unit_map, budget_s, max_steps, eta, open_x }. */
+int pt_debug_unpack(int32_t method, int64_t np, int32_t m, const int32_t dm[3],
+                    int32_t precision, int32_t has_j, const double params[17],
+                    const pt_options *opt, double out[8]);
+
+/* The same unpacking launched into a one-thread kernel that writes what the
+ * device receives (d_out, 8 doubles) and the host-side struct size and
+ * offset of the window end (host_out, 2 doubles). */
+int pt_debug_echo(int32_t method, int64_t np, int32_t m, const int32_t dm[3],
+                  int32_t precision, int32_t has_j, const double params[17],
+                  const pt_options *opt, double *d_out, double *host_out);
+
 /* Throughput probe for roofline denominators: kind 0 FP64 FMA, 1 FP32 FMA;
  * writes flop/s (FMA = 2 flops) measured on the current device. */
 int pt_probe_peak(int32_t kind, int32_t iters, double *flops_per_s);

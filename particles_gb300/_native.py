@@ -26,7 +26,7 @@ EXPORTS = [
     "pt_integrate", "pt_method_from_name", "pt_fields_create", "pt_fields_create_device",
     "pt_fields_destroy", "pt_fields_bytes", "pt_integrate_fields", "pt_carry_bytes",
     "pt_run_device", "pt_run_check", "pt_last_error", "pt_abi_version", "pt_tableau",
-    "pt_debug_pow", "pt_debug_accel", "pt_probe_peak",
+    "pt_debug_pow", "pt_debug_accel", "pt_probe_peak", "pt_debug_unpack", "pt_debug_echo",
 ]
 
 
@@ -81,6 +81,8 @@ def load():
     L.pt_debug_pow.argtypes = [i64, vp, vp, vp, vp]
     L.pt_debug_accel.argtypes = [vp, i64, vp, vp, vp, vp]
     L.pt_probe_peak.argtypes = [i32, i32, C.POINTER(d)]
+    L.pt_debug_unpack.argtypes = [i32, i64, i32, vp, i32, i32, vp, vp, vp]
+    L.pt_debug_echo.argtypes = [i32, i64, i32, vp, i32, i32, vp, vp, vp, vp]
     _lib = L
     return L
 

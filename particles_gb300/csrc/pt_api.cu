@@ -200,7 +200,13 @@ extern "C" int32_t pt_method_from_name(const char *name)
 /* runs                                                                   */
 /* ---------------------------------------------------------------------- */
 
-static void unpack_params(const double *p, const pt_fields *f, PtRun &R)
+struct RunShape {
+    int32_t dm[3];
+    int32_t precision;
+    int32_t has_j;
+};
+
+static void unpack_params(const double *p, const RunShape &g, PtRun &R)
 {
     memset(&R, 0, sizeof R);
     R.qom = p[0]; R.vun = p[1]; R.tmx = p[2]; R.dtm = p[4];
@@ -211,36 +217,32 @@ static void unpack_params(const double *p, const pt_fields *f, PtRun &R)
     for (int i = 0; i < 3; ++i) {
         R.xl[i] = p[11 + i];
         R.xs[i] = p[14 + i];
-        R.dm[i] = f->dm[i];
-        R.dmr[i] = (double)f->dm[i];
-        R.inv_dm[i] = 1.0 / (double)f->dm[i];
+        R.dm[i] = g.dm[i];
+        R.dmr[i] = (double)g.dm[i];
+        R.inv_dm[i] = 1.0 / (double)g.dm[i];
         unit = unit && (R.xl[i] == 0.0) && !signbit(R.xl[i]) && (R.xs[i] == 1.0);
     }
     R.unit_map = unit ? 1 : 0;
 }
 
-static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
-                    const double *params, const double *d_time, double *d_state, int64_t *d_cnt,
-                    int32_t *d_status, void *d_carry, const pt_options *opt, cudaStream_t s)
+/* Argument checks and the host part of a run: everything but pointers. */
+static int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
+                       const double *params, const pt_options *opt, PtRun &R)
 {
     if (method != PT_METHOD_RK5 && method != PT_METHOD_DOP853)
         return set_err(PT_ERR_ARG, "unknown method%s");
-    if (!f) return set_err(PT_ERR_ARG, "fields handle is NULL%s");
     if (np < 0 || m < 1) return set_err(PT_ERR_ARG, "np < 0 or m < 1%s");
     if (!params) return set_err(PT_ERR_ARG, "params is NULL%s");
-    if (np > 0 && (!d_time || !d_state || !d_cnt)) return set_err(PT_ERR_ARG, "NULL buffer%s");
-    if ((int64_t)m * np * 8 > ((int64_t)1 << 62)) return set_err(PT_ERR_ARG, "state too large%s");
+    if ((int64_t)m * np > ((int64_t)1 << 56)) return set_err(PT_ERR_ARG, "state too large%s");
     for (int i = 0; i < 17; ++i)
         if (i != 3 && !isfinite(params[i])) return set_err(PT_ERR_ARG, "non-finite params%s");
     if (params[14] == 0.0 || params[15] == 0.0 || params[16] == 0.0)
         return set_err(PT_ERR_ARG, "zero domain size%s");
-
-    int32_t precision = f->precision;
     double eta = 0.0, t_stop = 0.0, budget = 0.0;
     int32_t open_x = 0;
     int64_t max_steps = 0;
     if (opt) {
-        if (opt->precision != f->precision)
+        if (opt->precision != g.precision)
             return set_err(PT_ERR_ARG, "options precision differs from the field handle%s");
         if (opt->controller != 0)
             return set_err(PT_ERR_UNSUPPORTED, "learned controller not available for this precision%s");
@@ -250,21 +252,42 @@ static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
         open_x = opt->open_x;
         max_steps = opt->max_steps;
     }
-    if (eta != 0.0 && !f->has_j)
+    if (!isfinite(eta) || !isfinite(t_stop) || !isfinite(budget))
+        return set_err(PT_ERR_ARG, "non-finite option%s");
+    if (eta != 0.0 && !g.has_j)
         return set_err(PT_ERR_ARG, "eta != 0 needs a field handle created with J%s");
-    if (eta == 0.0 && f->has_j)
+    if (eta == 0.0 && g.has_j)
         return set_err(PT_ERR_ARG, "field handle holds J but eta == 0%s");
-
-    PtRun R;
-    unpack_params(params, f, R);
+    unpack_params(params, g, R);
     R.eta = eta;
-    R.has_j = f->has_j;
+    R.has_j = g.has_j;
     R.open_x = open_x ? 1 : 0;
     R.max_steps = max_steps > 0 ? max_steps : 1000000000LL;
     R.tend = (t_stop > 0.0 && t_stop < R.tmx) ? t_stop : R.tmx;
     R.budget_ns = (uint64_t)((budget > 0.0 ? budget : 600.0) * 1e9);
     R.m = m;
     R.np = np;
+    return PT_OK;
+}
+
+static RunShape shape_of(const pt_fields *f)
+{
+    RunShape g;
+    for (int i = 0; i < 3; ++i) g.dm[i] = f->dm[i];
+    g.precision = f->precision;
+    g.has_j = f->has_j;
+    return g;
+}
+
+static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
+                    const double *params, const double *d_time, double *d_state, int64_t *d_cnt,
+                    int32_t *d_status, void *d_carry, const pt_options *opt, cudaStream_t s)
+{
+    if (!f) return set_err(PT_ERR_ARG, "fields handle is NULL%s");
+    if (np > 0 && (!d_time || !d_state || !d_cnt)) return set_err(PT_ERR_ARG, "NULL buffer%s");
+    PtRun R;
+    int rc = prepare_run(method, np, m, shape_of(f), params, opt, R);
+    if (rc != PT_OK) return rc;
     R.fld = f->rec64;
     R.time = d_time;
     R.state = d_state;
@@ -281,11 +304,54 @@ static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
     }
     e = cudaMemsetAsync(f->scratch, 0, 2 * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return cuda_err(e, "scratch reset");
-    if (precision == PT_PREC_FP64)
+    if (f->precision == PT_PREC_FP64)
         e = method == PT_METHOD_RK5 ? pt_launch_rk5_exact(R, f->nc, s) : pt_launch_dp853_exact(R, f->nc, s);
     else
         e = method == PT_METHOD_RK5 ? pt_launch_rk5_fma(R, f->nc, s) : pt_launch_dp853_fma(R, f->nc, s);
     if (e != cudaSuccess) return cuda_err(e, "kernel launch");
+    return PT_OK;
+}
+
+/* Launch-parameter echo: out (device, 8 doubles) = what the kernel receives;
+ * host_out (host, 2 doubles) = host sizeof(PtRun), offsetof(tend). */
+extern "C" int pt_debug_echo(int32_t method, int64_t np, int32_t m, const int32_t dm[3],
+                             int32_t precision, int32_t has_j, const double params[17],
+                             const pt_options *opt, double *d_out, double *host_out)
+{
+    RunShape g;
+    for (int i = 0; i < 3; ++i) g.dm[i] = dm[i];
+    g.precision = precision;
+    g.has_j = has_j;
+    PtRun R;
+    int rc = prepare_run(method, np, m, g, params, opt, R);
+    if (rc != PT_OK) return rc;
+    host_out[0] = (double)sizeof(PtRun);
+    host_out[1] = (double)offsetof(PtRun, tend);
+    cudaError_t e = pt_launch_echo_exact(R, d_out, (cudaStream_t)0);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_echo");
+}
+
+extern "C" int pt_debug_unpack(int32_t method, int64_t np, int32_t m, const int32_t dm[3],
+                               int32_t precision, int32_t has_j, const double params[17],
+                               const pt_options *opt, double out[8])
+{
+    if (!dm || !out) return set_err(PT_ERR_ARG, "NULL argument%s");
+    RunShape g;
+    for (int i = 0; i < 3; ++i) g.dm[i] = dm[i];
+    g.precision = precision;
+    g.has_j = has_j;
+    PtRun R;
+    int rc = prepare_run(method, np, m, g, params, opt, R);
+    if (rc != PT_OK) return rc;
+    out[0] = R.tend;
+    out[1] = R.tmx;
+    out[2] = R.expo;
+    out[3] = (double)R.unit_map;
+    out[4] = (double)R.budget_ns * 1e-9;
+    out[5] = (double)R.max_steps;
+    out[6] = R.eta;
+    out[7] = (double)R.open_x;
     return PT_OK;
 }
 
@@ -441,7 +507,8 @@ extern "C" int pt_debug_accel(const pt_fields *f, int64_t n, const double params
     if (!f || !params) return set_err(PT_ERR_ARG, "NULL argument%s");
     if (n <= 0) return PT_OK;
     PtRun R;
-    unpack_params(params, f, R);
+    RunShape g = shape_of(f);
+    unpack_params(params, g, R);
     R.fld = f->rec64;
     R.has_j = f->has_j;
     R.eta = 0.0;

@@ -13,6 +13,7 @@
 #ifndef PT_COMMON_CUH
 #define PT_COMMON_CUH
 
+#include <stddef.h>
 #include <stdint.h>
 #include <cuda_runtime.h>
 
@@ -94,6 +95,10 @@ __device__ __forceinline__ uint64_t pt_globaltimer()
     return t;
 }
 
+/* Internal "keep integrating" word of the step loops; distinct from every
+ * PT_ST_* status (PT_ST_RUNNING is 1). */
+#define PT_GO 0x7fff
+
 /* Loop guard shared with the oracle: < 0 stops the particle before an attempt. */
 __device__ __forceinline__ int32_t pt_attempt_guard(double t, double dt, int64_t attempts,
                                                     int64_t max_steps)
@@ -101,7 +106,7 @@ __device__ __forceinline__ int32_t pt_attempt_guard(double t, double dt, int64_t
     if (max_steps > 0 && attempts >= max_steps) return PT_ST_STEP_LIMIT;
     if (dt != dt) return PT_ST_NONFINITE;
     if (!(dt > 0.0) || t + dt == t) return PT_ST_DT_UNDERFLOW;
-    return 1;
+    return PT_GO;
 }
 
 /* Launchers implemented by the kernel translation units. */
@@ -114,7 +119,8 @@ struct PtLaunch {
     cudaError_t pt_launch_rk5_##sfx(const PtRun &P, int nc, cudaStream_t s);     \
     cudaError_t pt_launch_dp853_##sfx(const PtRun &P, int nc, cudaStream_t s);   \
     cudaError_t pt_launch_accel_##sfx(const PtRun &P, int nc, int64_t n,         \
-                                      const double *vec, double *acc, cudaStream_t s);
+                                      const double *vec, double *acc, cudaStream_t s); \
+    cudaError_t pt_launch_echo_##sfx(const PtRun &P, double *out, cudaStream_t s);
 
 PT_DECLARE_FP64_LAUNCHERS(exact)
 PT_DECLARE_FP64_LAUNCHERS(fma)

@@ -25,9 +25,10 @@
  * Every multiply/add goes through pt_dmul/pt_dadd, which are __dmul_rn /
  * __dadd_rn on the device (never contracted into FMA, whatever -fmad says)
  * and plain operators on the host (the host side must be compiled with
- * -ffp-contract=off).  Accuracy is a few ulp over the controller's ranges
- * (tests compare against libm); bit-identity between host and device is the
- * property that matters.
+ * -ffp-contract=off).  Error bound: (2 + 2|y ln x|) ulp against libm, since
+ * z = y ln x is rounded once before exp (tests check it); for the
+ * controller's exponents and error ratios that is a few ulp.  Bit-identity
+ * between host and device is the property that matters.
  */
 #ifndef PT_DETMATH_H
 #define PT_DETMATH_H

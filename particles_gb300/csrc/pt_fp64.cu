@@ -238,14 +238,14 @@ __device__ __forceinline__ void lane_close(const PtRun &P, const PtCarry &C, con
     if (st == PT_ST_TIMEOUT) atomicExch(P.flags, 1);
 }
 
-/* Status before an attempt: 1 = go on, else the particle closes with it. */
+/* Status before an attempt: PT_GO = go on, else the particle closes with it. */
 __device__ __forceinline__ int32_t lane_check(const PtRun &P, const Lane &L, uint64_t t_start)
 {
     if (!(L.t < P.tend)) return (L.t >= P.tmx) ? PT_ST_DONE : PT_ST_RUNNING;
     int32_t g = pt_attempt_guard(L.t, L.dt, L.c0, P.max_steps);
-    if (g < 0) return g;
+    if (g != PT_GO) return g;
     if (P.budget_ns && pt_globaltimer() - t_start > P.budget_ns) return PT_ST_TIMEOUT;
-    return 1;
+    return PT_GO;
 }
 
 /* ---------------------------------------------------------------------- */
@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(PT_BLOCK) k_rk5(const PtRun P)
         if (!active) continue;
 
         int32_t st = lane_check(P, L, t_start);
-        if (st == 1) {
+        if (st == PT_GO) {
             const double dt = L.dt;
             double k[6][6], ss[6], ac[6], sf[6];
             if (!have_f1) eval_f<NC>(P, si, F1);               /* stage 1: f(si) */
@@ -355,13 +355,13 @@ __global__ void __launch_bounds__(PT_BLOCK) k_rk5(const PtRun P)
                 have_f1 = true;
                 L.dt = dt * pt_max(P.fcmn, P.safe * pt_det_pow(del, -0.25));
             }
-            if (st == 1) {
+            if (st == PT_GO) {
                 L.c0++;
                 L.dt = pt_min(L.dt, P.dtm);                     /* :195 */
                 if (esc) st = PT_ST_ESCAPED;
             }
         }
-        if (st != 1) {
+        if (st != PT_GO) {
             lane_close(P, C, L, si, st);
             active = false;
         }
@@ -405,7 +405,7 @@ __global__ void __launch_bounds__(PT_BLOCK) k_dp853(const PtRun P)
         if (!active) continue;
 
         int32_t st = lane_check(P, L, t_start);
-        if (st == 1) {
+        if (st == PT_GO) {
             const double dt = L.dt;
             double ss[6], sf[6];
             {                                                   /* :368 */
@@ -483,13 +483,13 @@ __global__ void __launch_bounds__(PT_BLOCK) k_dp853(const PtRun P)
                 L.dt = dt * pt_max(P.fcmn, P.safe * pt_det_pow(err, P.expo));
                 L.rejected = true;
             }
-            if (st == 1) {
+            if (st == PT_GO) {
                 L.c0++;
                 L.dt = pt_min(L.dt, P.dtm);                     /* :500 */
                 if (esc) st = PT_ST_ESCAPED;
             }
         }
-        if (st != 1) {
+        if (st != PT_GO) {
             lane_close(P, C, L, si, st);
             active = false;
         }
@@ -510,6 +510,19 @@ __global__ void k_accel(const PtRun P, int64_t n, const double *vec, double *acc
 #pragma unroll
         for (int c = 0; c < 6; ++c) acc[6 * i + c] = a[c];
     }
+}
+
+/* Echo of the launch parameters as the device sees them (layout check). */
+__global__ void k_echo(const PtRun P, double *out)
+{
+    out[0] = P.tend;
+    out[1] = P.tmx;
+    out[2] = P.expo;
+    out[3] = (double)P.max_steps;
+    out[4] = (double)P.budget_ns;
+    out[5] = (double)sizeof(PtRun);
+    out[6] = (double)offsetof(PtRun, tend);
+    out[7] = (double)P.np;
 }
 
 template <class K>
@@ -544,6 +557,12 @@ cudaError_t PT_NAME(pt_launch_rk5)(const PtRun &P, int nc, cudaStream_t s)
 cudaError_t PT_NAME(pt_launch_dp853)(const PtRun &P, int nc, cudaStream_t s)
 {
     return nc == 10 ? launch_persistent(k_dp853<10>, P, s) : launch_persistent(k_dp853<6>, P, s);
+}
+
+cudaError_t PT_NAME(pt_launch_echo)(const PtRun &P, double *out, cudaStream_t s)
+{
+    k_echo<<<1, 1, 0, s>>>(P, out);
+    return cudaGetLastError();
 }
 
 cudaError_t PT_NAME(pt_launch_accel)(const PtRun &P, int nc, int64_t n, const double *vec,

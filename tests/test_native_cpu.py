@@ -1,0 +1,76 @@
+"""The C-ABI library on a machine without a GPU: it loads, exports every
+symbol the public header declares, carries the same tableau as the oracle,
+and rejects bad arguments before touching CUDA."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _header_functions():
+    text = (ROOT / "include" / "particles_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pt_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_exports_every_header_symbol(native):
+    from particles_gb300 import _native as N
+    declared = _header_functions()
+    assert declared, "no declarations parsed"
+    for name in declared:
+        assert hasattr(native, name), f"{name} missing from the library"
+    assert sorted(N.EXPORTS) == declared
+
+
+def test_abi_version_and_carry_size(native):
+    assert native.pt_abi_version() == 1
+    assert native.pt_carry_bytes(0) == 0
+    assert native.pt_carry_bytes(1000) == 80 * 1000
+
+
+@pytest.mark.parametrize("name,mid", [("rk5", 1), ("dop853", 2), ("dp853", 2), ("rk8", 2),
+                                      ("rk5   ", 1), ("RK5", 0), ("euler", 0), ("", 0)])
+def test_method_names(native, name, mid):
+    assert native.pt_method_from_name(name.encode()) == mid
+
+
+@pytest.mark.parametrize("which", [1, 2])
+def test_tableau_bitwise_equals_oracle(native, oracle_lib, which):
+    n = native.pt_tableau(which, None)
+    got = np.zeros(n)
+    native.pt_tableau(which, got.ctypes.data_as(C.c_void_p))
+    ref = oracle_lib.tableau(which)
+    assert np.array_equal(got.view(np.int64), ref.view(np.int64))
+
+
+def test_argument_errors_need_no_gpu(native):
+    from particles_gb300 import _native as N
+    dm = np.array([4, 4, 4], np.int32)
+    f = np.zeros(3 * 64)
+    p = np.zeros(17)
+    st = np.zeros((2, 3, 8))
+    cnt = np.zeros((2, 3), np.int64)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)
+    assert native.pt_integrate(7, 2, 3, ptr(dm), ptr(p), ptr(np.zeros(3)), ptr(f), ptr(f),
+                               ptr(st), ptr(cnt), None) == N.PT_ERR_ARG
+    assert b"method" in native.pt_last_error()
+    assert native.pt_integrate(1, -1, 3, ptr(dm), ptr(p), ptr(np.zeros(3)), ptr(f), ptr(f),
+                               ptr(st), ptr(cnt), None) == N.PT_ERR_ARG
+    assert native.pt_integrate(1, 0, 3, ptr(dm), ptr(p), ptr(np.zeros(3)), ptr(f), ptr(f),
+                               ptr(st), ptr(cnt), None) == N.PT_OK          # empty batch
+    bad = np.array([0, 4, 4], np.int32)
+    h = C.c_void_p()
+    assert native.pt_fields_create(ptr(bad), ptr(f), ptr(f), None, 0, C.byref(h)) == N.PT_ERR_ARG
+    assert native.pt_fields_create(ptr(dm), ptr(f), ptr(f), None, 9, C.byref(h)) == N.PT_ERR_UNSUPPORTED
+    assert native.pt_run_check(None) == N.PT_ERR_ARG
+    assert native.pt_fields_destroy(None) == N.PT_OK
+
+
+def test_options_struct_layout():
+    from particles_gb300 import _native as N
+    assert C.sizeof(N.PtOptions) == 112
+    assert N.PtOptions.max_steps.offset == 16 and N.PtOptions.carry.offset == 64

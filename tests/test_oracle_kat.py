@@ -1,0 +1,309 @@
+"""Known-answer tests that pin the CPU oracle.
+
+The reference ships no tests, fixtures or golden vectors and cannot be built
+here (Fortran, no compiler), so the oracle is pinned by analytic answers:
+tableau identities of the published methods, exactness of the trilinear
+gather, gyration in a uniform field, E x B drift, convergence order, the
+agreement of the two methods, and internal identities (counters, windowed
+resume, redundant-evaluation elimination).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from particles_gb300 import fields, initial, params
+
+QOM, VUN = 200.0, 1.0 / 20.0
+T0 = 2.0 * math.pi / QOM
+
+
+# ---------------------------------------------------------------- tableaux --
+
+def test_rk5_tableau_identities():
+    t = oracle.tableau(1)
+    B = t[:25].reshape(5, 5)
+    c, d = t[25:31], t[31:37]
+    nodes = np.array([0.2, 0.3, 0.6, 1.0, 7.0 / 8.0])      # Cash & Karp 1990
+    assert np.allclose(B.sum(1), nodes, atol=1e-15, rtol=0)
+    assert abs(c.sum() - 1.0) < 1e-15
+    assert abs(d.sum()) < 1e-15
+    # 4th-order embedded weights c* = c - d also sum to one
+    assert abs((c - d).sum() - 1.0) < 1e-15
+    assert B[0, 0] == 0.2 and B[1, 0] == 0.075 and B[1, 1] == 0.225
+
+
+def test_dop853_tableau_identities():
+    v = oracle.tableau(2)
+    a = v[:50]
+    b = v[50:58]
+    rows = [1, 2, 2, 3, 3, 4, 5, 6, 7, 8, 9]          # non-zero a-coefficients per stage 2..12
+    sums, k = [], 0
+    for r in rows:
+        sums.append(a[k:k + r].sum())
+        k += r
+    nodes = [0.0526001519587677318785587544488, 0.0789002279381515978178381316732,
+             0.118350341907227396726757197510, 0.281649658092772603273242802490,
+             1.0 / 3.0, 0.25, 4.0 / 13.0, 127.0 / 195.0, 0.6, 6.0 / 7.0, 1.0]
+    # cancellation among coefficients up to |a| = 43 leaves a few ulp of 43
+    assert np.allclose(sums, nodes, atol=2e-14, rtol=0)
+    assert abs(b.sum() - 1.0) < 1e-14
+
+
+# ---------------------------------------------------------------- gather --
+
+def _trilinear_fields(n, coef):
+    """U = B = c0 + c1 x + c2 y + c3 z + c4 xy + c5 yz + c6 zx + c7 xyz on nodes i/n."""
+    z, y, x = np.meshgrid(np.arange(n) / n, np.arange(n) / n, np.arange(n) / n, indexing="ij")
+    f = (coef[0] + coef[1] * x + coef[2] * y + coef[3] * z + coef[4] * x * y
+         + coef[5] * y * z + coef[6] * z * x + coef[7] * x * y * z)
+    return np.stack([f, 2 * f, -f]), f
+
+
+def test_interpolation_exact_for_trilinear_fields():
+    n = 8
+    rng = np.random.default_rng(0)
+    coef = rng.normal(size=8)
+    uu, f = _trilinear_fields(n, coef)
+    bb = uu.copy()
+    for _ in range(200):
+        pos = rng.uniform(0, (n - 1) / n, 3)          # stay inside non-wrapping cells
+        u, b = oracle.interpolate_lin(uu, bb, pos)
+        x, y, z = pos
+        ex = (coef[0] + coef[1] * x + coef[2] * y + coef[3] * z + coef[4] * x * y
+              + coef[5] * y * z + coef[6] * z * x + coef[7] * x * y * z)
+        assert np.allclose(u, [ex, 2 * ex, -ex], rtol=1e-12, atol=1e-12)
+        assert np.array_equal(u, b)
+
+
+def test_interpolation_reproduces_nodes_and_is_periodic():
+    n = 6
+    rng = np.random.default_rng(1)
+    uu = rng.normal(size=(3, n, n, n))
+    bb = rng.normal(size=(3, n, n, n))
+    for i, j, k in [(0, 0, 0), (5, 2, 3), (1, 4, 5)]:
+        u, b = oracle.interpolate_lin(uu, bb, np.array([i, j, k]) / n)
+        assert np.allclose(u, uu[:, k, j, i], rtol=0, atol=1e-14)
+        assert np.allclose(b, bb[:, k, j, i], rtol=0, atol=1e-14)
+    for _ in range(50):
+        p = rng.uniform(0, 1, 3)
+        u0, b0 = oracle.interpolate_lin(uu, bb, p)
+        for shift in ([1, 0, 0], [0, -2, 0], [3, 1, -1]):
+            u1, b1 = oracle.interpolate_lin(uu, bb, p + np.array(shift))
+            assert np.allclose(u0, u1, atol=1e-12) and np.allclose(b0, b1, atol=1e-12)
+    # a non-unit domain [xl, xl+xs) maps onto the same nodes
+    u2, _ = oracle.interpolate_lin(uu, bb, np.array([2.5, -1.0, 4.0]) + 0.5 * p,
+                                   xl=(2.5, -1.0, 4.0), xs=(0.5, 0.5, 0.5))
+    u3, _ = oracle.interpolate_lin(uu, bb, p)
+    assert np.allclose(u2, u3, atol=1e-12)
+
+
+def test_interpolation_tiny_negative_wraps_to_node_zero():
+    # x - floor(x) rounds to 1.0 for x = -1e-18; the reference would index past
+    # the array there, the oracle wraps to the periodic image (node 0).
+    n = 4
+    uu = np.arange(3 * n ** 3, dtype=float).reshape(3, n, n, n)
+    u, _ = oracle.interpolate_lin(uu, uu, np.array([-1e-18, 0.0, 0.0]))
+    assert np.allclose(u, uu[:, 0, 0, 0])
+
+
+def test_interpolate_near():
+    n = 5
+    rng = np.random.default_rng(2)
+    uu = rng.normal(size=(3, n, n, n))
+    bb = rng.normal(size=(3, n, n, n))
+    u, b = oracle.interpolate_near(uu, bb, np.array([0.41, 0.79, 0.05]))
+    assert np.array_equal(u, uu[:, 0, 3, 2]) and np.array_equal(b, bb[:, 0, 3, 2])
+
+
+# ---------------------------------------------------------------- force --
+
+def test_lorentz_force_uniform_field():
+    uu, bb = fields.uniform_field(4, b=(0.0, 0.0, 2.0), u=(0.01, 0.0, 0.0))
+    vec = np.array([0.3, 0.3, 0.3, 0.6, -0.2, 0.1])
+    acc = oracle.acceleration(QOM, VUN, uu, bb, vec)
+    g = math.sqrt(1 + (vec[3:] ** 2).sum())
+    v = vec[3:] / g
+    w = v - np.array([0.01, 0.0, 0.0])
+    assert np.allclose(acc[:3], v / VUN, rtol=1e-15)
+    assert np.allclose(acc[3:], QOM * np.cross(w, [0, 0, 2.0]), rtol=1e-14)
+
+
+# ---------------------------------------------------------------- motion --
+
+def _gyration_case(method, nper_step, periods=1.0, speed=0.5):
+    """Uniform B = x^: helical motion with gamma constant and period 2 pi gamma / qom."""
+    u = speed / math.sqrt(1.0 - speed ** 2)           # perpendicular momentum
+    gam = math.sqrt(1.0 + 0.1 ** 2 + u ** 2)          # u_par = 0.1
+    tg_period = 2 * math.pi * gam / QOM
+    tmax = periods * tg_period
+    dt = tg_period / nper_step
+    # huge tolerances: the controller wants large steps, dtmax pins dt
+    prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=dt, atol=1.0, rtol=1.0,
+                             facmax=6.0)
+    tg = params.time_grid(4, tmax)
+    uu, bb = fields.uniform_field(4, b=(1.0, 0.0, 0.0))
+    st = np.zeros((1, tg.size, 8))
+    st[0, 0, :6] = [0.3, 0.4, 0.5, 0.1, u * 0.6, u * 0.8]
+    s, c, status = oracle.integrate(method, prm, tg, uu, bb, st)
+    assert status[0] == oracle.ST_DONE
+    # the last step ends within rounding of tmax, so the last sample is ~sf
+    up = u  # perpendicular momentum magnitude (y,z plane)
+    r = up / (VUN * QOM)
+    ph0 = math.atan2(0.8, 0.6)
+    tt = tg[-1]
+    om = QOM / gam
+    # u_perp rotates clockwise about +x for a positive charge
+    uy = up * math.cos(ph0 - om * tt)
+    uz = up * math.sin(ph0 - om * tt)
+    # position: centre of the gyro-orbit + radius vector
+    cy = 0.4 + r * math.sin(ph0) * 1.0
+    cz = 0.5 - r * math.cos(ph0) * 1.0
+    y = cy - r * math.sin(ph0 - om * tt)
+    z = cz + r * math.cos(ph0 - om * tt)
+    x = 0.3 + (0.1 / gam) / VUN * tt
+    exact = np.array([x, y, z, 0.1, uy, uz])
+    return s[0, -1, :6], exact, c[0]
+
+
+@pytest.mark.parametrize("method,order", [("rk5", 5), ("dop853", 8)])
+def test_gyration_convergence_order(method, order):
+    errs = []
+    for nps in (24, 48):
+        got, exact, c = _gyration_case(method, nps)
+        errs.append(np.abs(got - exact).max())
+    # halving dt divides the global error by ~2^order
+    ratio = errs[0] / errs[1]
+    assert ratio > 2 ** (order - 1.2), (errs, ratio)
+
+
+@pytest.mark.parametrize("method", ["rk5", "dop853"])
+def test_gyration_accuracy_and_gamma(method):
+    got, exact, c = _gyration_case(method, 200 if method == "rk5" else 40, periods=3.0)
+    assert np.abs(got - exact).max() < 1e-9
+    assert c[0] == c[1] + c[2]
+
+
+def test_exb_drift():
+    """Uniform B = z^, U = 0.05 c x^ (E = -U x B): a particle at rest drifts
+    on average with U (code velocity U/vun)."""
+    u0 = 0.05
+    uu, bb = fields.uniform_field(4, b=(0.0, 0.0, 1.0), u=(u0, 0.0, 0.0))
+    tmax = 40 * T0
+    prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=tmax, atol=1e-10, rtol=1e-10)
+    tg = params.time_grid(400, tmax)
+    st = np.zeros((1, tg.size, 8))
+    st[0, 0, :6] = [0.5, 0.5, 0.5, 0.0, 0.0, 0.0]
+    s, c, status = oracle.integrate("dop853", prm, tg, uu, bb, st)
+    x = s[0, :, 0]
+    vx = np.polyfit(tg, x, 1)[0]
+    assert abs(vx * VUN / u0 - 1.0) < 0.01
+    assert abs(np.polyfit(tg, s[0, :, 1], 1)[0]) * VUN < 1e-3 * u0
+    # energy oscillates with the cycloid but stays bounded by the drift frame
+    assert s[0, :, 6].max() < 1.0 + 4 * u0 ** 2
+
+
+def _turbulent_case(method, tol, npart=8, periods=1.0, seed=3):
+    uu, bb = fields.snapshot(16, seed=seed)
+    tmax = periods * T0
+    prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=tmax, atol=tol, rtol=tol)
+    tg = params.time_grid(4, tmax)
+    st = np.zeros((npart, tg.size, 8))
+    st[:, 0, :6] = initial.isotropic_state(npart, seed, speed=0.5)
+    return prm, tg, uu, bb, st
+
+
+def test_rk5_and_dop853_agree_at_tight_tolerance():
+    prm, tg, uu, bb, st = _turbulent_case("rk5", 1e-12)
+    s5, _, _ = oracle.integrate("rk5", prm, tg, uu, bb, st.copy())
+    prm8 = prm.copy()
+    prm8[5] = prm8[6] = 1e-13
+    s8, _, _ = oracle.integrate("dop853", prm8, tg, uu, bb, st.copy())
+    assert np.abs(s5[:, -1, :6] - s8[:, -1, :6]).max() < 5e-6
+
+
+# ------------------------------------------------------ internal identities --
+
+@pytest.mark.parametrize("method", ["rk5", "dop853"])
+def test_faithful_and_minimal_evaluations_identical(method):
+    prm, tg, uu, bb, st = _turbulent_case(method, 1e-8)
+    a = oracle.integrate(method, prm, tg, uu, bb, st.copy(), faithful=True)
+    b = oracle.integrate(method, prm, tg, uu, bb, st.copy(), faithful=False)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert (a[1][:, 0] == a[1][:, 1] + a[1][:, 2]).all()
+
+
+@pytest.mark.parametrize("method", ["rk5", "dop853"])
+def test_windowed_resume_is_bit_identical(method):
+    prm, tg, uu, bb, st = _turbulent_case(method, 1e-9, periods=2.0)
+    full = oracle.integrate(method, prm, tg, uu, bb, st.copy())
+    s2 = st.copy()
+    cnt = np.zeros((st.shape[0], 3), np.int64)
+    carry = oracle.make_carry(st.shape[0])
+    for w in (0.3, 0.9, 1.7):
+        _, _, status = oracle.integrate(method, prm, tg, uu, bb, s2, cnt, carry=carry, t_stop=w * T0)
+        assert (status == oracle.ST_RUNNING).all()
+    _, _, status = oracle.integrate(method, prm, tg, uu, bb, s2, cnt, carry=carry)
+    assert (status == oracle.ST_DONE).all()
+    assert np.array_equal(full[0], s2) and np.array_equal(full[1], cnt)
+
+
+# ------------------------------------------------------------ edge cases --
+
+def test_empty_and_single_sample():
+    prm, tg, uu, bb, st = _turbulent_case("rk5", 1e-8)
+    oracle.integrate("rk5", prm, tg, uu, bb, np.zeros((0, tg.size, 8)))
+    st1 = st[:, :1].copy()
+    s, c, status = oracle.integrate("rk5", prm, tg[:1], uu, bb, st1)
+    assert (status == 0).all() and (c[:, 1] > 0).all()
+    assert np.array_equal(s[:, 0, :6], st[:, 0, :6])
+
+
+def test_step_limit_nonfinite_underflow_escape():
+    prm, tg, uu, bb, st = _turbulent_case("dop853", 1e-8)
+    _, c, status = oracle.integrate("dop853", prm, tg, uu, bb, st.copy(), max_steps=3)
+    assert (status == oracle.ST_STEP_LIMIT).all() and (c[:, 0] == 3).all()
+    bad = bb.copy()
+    bad[1] = np.nan
+    _, _, status = oracle.integrate("rk5", prm, tg, uu, bad, st.copy())
+    assert (status == oracle.ST_NONFINITE).all()
+    p0 = prm.copy()
+    p0[4] = 0.0                                       # dtmax = 0 -> dt = 0
+    _, _, status = oracle.integrate("rk5", p0, tg, uu, bb, st.copy())
+    assert (status == oracle.ST_DT_UNDERFLOW).all()
+    s = st.copy()
+    s[:, 0, 0] = 0.999
+    s[:, 0, 3] = 2.0                                  # moving +x fast, leaves at x = 1
+    out, c, status = oracle.integrate("rk5", prm, tg, uu, bb, s, open_x=True)
+    assert (status == oracle.ST_ESCAPED).all()
+    assert (c[:, 0] == c[:, 1] + c[:, 2]).all()
+
+
+# ------------------------------------------------------------------- pow --
+
+def test_det_pow_against_libm():
+    rng = np.random.default_rng(5)
+    xs = 10.0 ** rng.uniform(-15, 15, 3000)
+    for y in (-0.2, -0.25, -0.125, 0.2, 0.125, 1.0 / 3.0, -0.075):
+        for x in xs:
+            got, ref = oracle.det_pow(x, y), x ** y
+            # stated bound of the method: the rounding of z = y ln x carries
+            # |z| ulp of relative error into exp(z)
+            bound = (2.0 + 2.0 * abs(y * math.log(x))) * np.spacing(ref)
+            assert abs(got - ref) <= bound, (x, y, got, ref)
+    assert oracle.det_pow(0.0, -0.2) == math.inf
+    assert oracle.det_pow(0.0, 0.2) == 0.0
+    assert oracle.det_pow(3.0, 0.0) == 1.0
+    assert oracle.det_pow(1.0, 123.0) == 1.0
+    assert math.isnan(oracle.det_pow(math.nan, 0.5))
+    assert math.isnan(oracle.det_pow(-1.0, 0.5))
+    assert abs(oracle.det_pow(5e-324, -0.25) / (5e-324) ** -0.25 - 1) < 400 * 2.2e-16
+
+
+# ---------------------------------------------------------- flop constants --
+
+def test_flop_counts_are_the_benchmark_constants():
+    from particles_gb300 import roofline
+    for key, (method, what, eta) in roofline.COUNT_KEYS.items():
+        assert sum(oracle.count_ops(method, what, eta)) == roofline.FLOPS[key], key
