@@ -141,6 +141,27 @@ int pt_run_device(int32_t method, int64_t np, int32_t m, const pt_fields *f,
  * PT_ERR_TIMEOUT or PT_ERR_CUDA. */
 int pt_run_check(const pt_fields *f);
 
+/* ---- no device allocation ------------------------------------------------ */
+
+/* For callers that cannot call cudaMalloc (code where the device allocator is
+ * off limits: host callbacks, foreign allocators that forbid allocations of
+ * their own, real-time loops that must not block).  No counterpart in the
+ * reference.  The same exact FP64 integration as pt_run_device with the
+ * reference's behaviour (no options), but the fields come as DEVICE pointers
+ * in the reference layout and every byte of scratch -- the converted field
+ * records, the work-queue head, the flags -- lives in a static device array
+ * that each GPU loading this library holds until exit.  Nothing is allocated.
+ * Capacity: grids of at most 64^3 nodes (ideal MHD); larger ones return
+ * PT_ERR_ARG.  The first call on a device looks up the array's address, so
+ * make it before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race, so serialise them.  Launches on `stream` and
+ * returns without synchronising; d_status (np int32, may be NULL) holds the
+ * per-particle outcome once the stream is synchronised. */
+int pt_integrate_device_noalloc(int32_t method, int64_t np, int32_t m, const int32_t dm[3],
+                                const double params[17], const double *d_time,
+                                const double *d_uu, const double *d_bb, double *d_state,
+                                int64_t *d_cnt, int32_t *d_status, void *stream);
+
 /* ---- diagnostics --------------------------------------------------------- */
 
 const char *pt_last_error(void);

@@ -27,6 +27,7 @@ EXPORTS = [
     "pt_fields_destroy", "pt_fields_bytes", "pt_integrate_fields", "pt_carry_bytes",
     "pt_run_device", "pt_run_check", "pt_last_error", "pt_abi_version", "pt_tableau",
     "pt_debug_pow", "pt_debug_accel", "pt_probe_peak", "pt_debug_unpack", "pt_debug_echo",
+    "pt_integrate_device_noalloc",
 ]
 
 
@@ -83,6 +84,7 @@ def load():
     L.pt_probe_peak.argtypes = [i32, i32, C.POINTER(d)]
     L.pt_debug_unpack.argtypes = [i32, i64, i32, vp, i32, i32, vp, vp, vp]
     L.pt_debug_echo.argtypes = [i32, i64, i32, vp, i32, i32, vp, vp, vp, vp]
+    L.pt_integrate_device_noalloc.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
 

@@ -312,6 +312,20 @@ static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
     return PT_OK;
 }
 
+/* Access for the no-allocation entry point (pt_noalloc.cu). */
+int pt_prepare_run_public(int32_t method, int64_t np, int32_t m, const int32_t dm[3],
+                          int32_t precision, int32_t has_j, const double *params,
+                          const pt_options *opt, PtRun &R)
+{
+    RunShape g;
+    for (int i = 0; i < 3; ++i) g.dm[i] = dm[i];
+    g.precision = precision;
+    g.has_j = has_j;
+    return prepare_run(method, np, m, g, params, opt, R);
+}
+
+void pt_set_last_error(const char *msg) { snprintf(g_err, sizeof g_err, "%s", msg); }
+
 /* Launch-parameter echo: out (device, 8 doubles) = what the kernel receives;
  * host_out (host, 2 doubles) = host sizeof(PtRun), offsetof(tend). */
 extern "C" int pt_debug_echo(int32_t method, int64_t np, int32_t m, const int32_t dm[3],
