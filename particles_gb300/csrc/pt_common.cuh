@@ -46,15 +46,17 @@ struct PtRun {
     int64_t *cnt;
     int32_t *status;
     unsigned char *carry;  /* SoA carry or NULL */
+    const int32_t *order;  /* queue order (particle index per queue slot) or NULL */
     unsigned long long *queue;  /* work-queue head */
     int32_t *flags;        /* [0] time budget hit, [1] particles with negative status */
 };
 
-/* Carry (controller memory) SoA layout inside one buffer of 80*np bytes:
- *   double t[np], dt[np], errold[np], si[6][np]; int32 n[np], flags[np]
- * flags bit0 = started, bit1 = the previous DOP853 attempt was rejected. */
+/* Carry (controller memory) SoA layout inside one buffer of 128*np bytes:
+ *   double t[np], dt[np], errold[np], si[6][np], k1[6][np]; int32 n[np], flags[np]
+ * flags bit0 = started, bit1 = the previous DOP853 attempt was rejected,
+ * bit2 = k1 holds f(si), so a resumed particle needs no evaluation. */
 struct PtCarry {
-    double *t, *dt, *errold, *si;
+    double *t, *dt, *errold, *si, *k1;
     int32_t *n, *flags;
 };
 
@@ -66,13 +68,14 @@ __host__ __device__ inline PtCarry pt_carry_view(unsigned char *base, int64_t np
     c.dt = d + np;
     c.errold = d + 2 * np;
     c.si = d + 3 * np;
-    int32_t *i = reinterpret_cast<int32_t *>(d + 9 * np);
+    c.k1 = d + 9 * np;
+    int32_t *i = reinterpret_cast<int32_t *>(d + 15 * np);
     c.n = i;
     c.flags = i + np;
     return c;
 }
 
-#define PT_CARRY_BYTES_PER_PARTICLE 80
+#define PT_CARRY_BYTES_PER_PARTICLE 128
 
 /* Fortran MIN/MAX with the NaN rule of the oracle (a NaN first operand
  * propagates), and maxval with NaN propagation. */

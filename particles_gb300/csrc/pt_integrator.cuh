@@ -1,0 +1,485 @@
+/*
+ * pt_integrator.cuh -- the step machine shared by the fused integrators.
+ *
+ * One lane owns one particle at a time and pulls the next particle from a
+ * device work queue when its particle finishes.  All lanes of a warp walk the
+ * same sequence of evaluation slots in lock-step:
+ *
+ *   slot 0 (tail): finish the attempt (final combination, error norm,
+ *                  accept/reject), and let idle lanes take a new particle;
+ *                  ONE evaluation serves both -- f(sf) for accepted lanes
+ *                  (the next attempt's stage 1 and the Hermite end slope) and
+ *                  f(si) for particles that start fresh;
+ *   slots 1..S-1:  the stages of the next attempt, each one evaluation.
+ *
+ * So the gather + force code exists once in the kernel (small code, no
+ * instruction-fetch stalls), every evaluation runs converged across the warp,
+ * and the stage coefficients come from a per-stage table.  The k rows live in
+ * shared memory (row-major by stage and component, lane fastest), which keeps
+ * the register count low enough for 12+ warps per SM.
+ *
+ * The arithmetic of every stage sum, error norm, controller and dense-output
+ * row keeps the operand order of the reference (sources/integrations.F90), so
+ * a translation unit compiled with --fmad=false reproduces the CPU oracle bit
+ * for bit; the same code compiled with contraction is the FMA variant.
+ *
+ * The evaluation f(s) is a policy type EV with
+ *     static __device__ void f(const PtRun &P, const double s[6], double a[6]);
+ * (FP64 records, or FP32 records for mixed precision).
+ */
+#ifndef PT_INTEGRATOR_CUH
+#define PT_INTEGRATOR_CUH
+
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "pt_common.cuh"
+#include "pt_detmath.h"
+#include "pt_tableau.h"
+
+namespace pt_sm {
+
+using namespace pt_tab;
+
+/* One stage of a tableau: the stage state is built from k rows r[0..n-1]
+ * with coefficients a[], and f(stage) is stored into row dst. */
+struct Stage {
+    int n, dst;
+    double a[9];
+    int r[9];
+};
+
+/* DOP853 (integrations.F90:365-416): k rows 0..9 as in the reference's
+ * k(1:10,:), stages 11 and 12 overwrite rows 1 and 2 (k(2), k(3)). */
+static __constant__ Stage kDop[12] = {
+    { 0, 0, { 0 }, { 0 } },
+    { 1, 1, { A0201 }, { 0 } },
+    { 2, 2, { A0301, A0302 }, { 0, 1 } },
+    { 2, 3, { A0401, A0403 }, { 0, 2 } },
+    { 3, 4, { A0501, A0503, A0504 }, { 0, 2, 3 } },
+    { 3, 5, { A0601, A0604, A0605 }, { 0, 3, 4 } },
+    { 4, 6, { A0701, A0704, A0705, A0706 }, { 0, 3, 4, 5 } },
+    { 5, 7, { A0801, A0804, A0805, A0806, A0807 }, { 0, 3, 4, 5, 6 } },
+    { 6, 8, { A0901, A0904, A0905, A0906, A0907, A0908 }, { 0, 3, 4, 5, 6, 7 } },
+    { 7, 9, { A1001, A1004, A1005, A1006, A1007, A1008, A1009 }, { 0, 3, 4, 5, 6, 7, 8 } },
+    { 8, 1, { A1101, A1104, A1105, A1106, A1107, A1108, A1109, A1110 },
+      { 0, 3, 4, 5, 6, 7, 8, 9 } },
+    { 9, 2, { A1201, A1204, A1205, A1206, A1207, A1208, A1209, A1210, A1211 },
+      { 0, 3, 4, 5, 6, 7, 8, 9, 1 } },
+};
+
+/* Cash-Karp (integrations.F90:131-138): k_j = dt f(s_j) in rows 0..5;
+ * stage j sums B(j-1, i) k_i for i < j in order. */
+static __constant__ Stage kCk[6] = {
+    { 0, 0, { 0 }, { 0 } },
+    { 1, 1, { CK_B2_1 }, { 0 } },
+    { 2, 2, { CK_B3_1, CK_B3_2 }, { 0, 1 } },
+    { 3, 3, { CK_B4_1, CK_B4_2, CK_B4_3 }, { 0, 1, 2 } },
+    { 4, 4, { CK_B5_1, CK_B5_2, CK_B5_3, CK_B5_4 }, { 0, 1, 2, 3 } },
+    { 5, 5, { CK_B6_1, CK_B6_2, CK_B6_3, CK_B6_4, CK_B6_5 }, { 0, 1, 2, 3, 4 } },
+};
+
+template <int METHOD> struct Traits;
+template <> struct Traits<PT_METHOD_DOP853> {
+    static constexpr int ROWS = 10;    /* k(1:10,:) */
+    static constexpr int SLOTS = 12;   /* tail + 11 stages */
+    static constexpr int F1 = 0;       /* row holding f(si) */
+    static constexpr int IORD = 8;
+};
+template <> struct Traits<PT_METHOD_RK5> {
+    static constexpr int ROWS = 7;     /* k_0..k_5 (with dt) + f(si) */
+    static constexpr int SLOTS = 6;    /* tail + 5 stages */
+    static constexpr int F1 = 6;
+    static constexpr int IORD = 5;
+};
+
+/* Per-lane k rows in shared memory: element (row, c) of lane l at
+ * base[(row * 6 + c) * stride], base = smem + l, stride = blockDim.x. */
+struct KRows {
+    double *base;
+    int stride;
+    __device__ __forceinline__ double &operator()(int row, int c) const
+    {
+        return base[(row * 6 + c) * stride];
+    }
+};
+
+__device__ __forceinline__ double inf64() { return __longlong_as_double(0x7ff0000000000000LL); }
+
+/* ---- per-particle bookkeeping ------------------------------------------ */
+
+struct Lane {
+    int64_t p;
+    double t, dt, errold, tnext;
+    int32_t n;
+    bool rejected;
+    int64_t c0, c1, c2;
+};
+
+enum Mode { M_IDLE = 0, M_ACCEPT, M_REJECT, M_INIT, M_READY };
+
+__device__ __forceinline__ void next_time(const PtRun &P, Lane &L)
+{
+    L.tnext = (L.n < P.m) ? P.time[L.n] : inf64();
+}
+
+/* Loads particle L.p: state(:,1,p) for a fresh start, else the carry (with
+ * f(si) if it was saved).  Returns 0 fresh, 1 resumed without f(si),
+ * 2 resumed with f(si) loaded into row F1. */
+template <int METHOD>
+__device__ __forceinline__ int lane_open(const PtRun &P, const PtCarry &C, const KRows &K,
+                                         Lane &L, double si[6])
+{
+    const bool fresh = (P.carry == nullptr) || !(C.flags[L.p] & 1);
+    if (fresh) {
+        const double2 *s = reinterpret_cast<const double2 *>(P.state + (int64_t)8 * P.m * L.p);
+        const double2 a = s[0], b = s[1], c = s[2];
+        si[0] = a.x; si[1] = a.y; si[2] = b.x; si[3] = b.y; si[4] = c.x; si[5] = c.y;
+        L.t = 0.0; L.n = 1; L.errold = 1.0e-04; L.rejected = false;
+        L.c0 = L.c1 = L.c2 = 0;
+        return 0;
+    }
+    const int32_t fl = C.flags[L.p];
+    L.t = C.t[L.p]; L.dt = C.dt[L.p]; L.errold = C.errold[L.p]; L.n = C.n[L.p];
+    L.rejected = (fl & 2) != 0;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) si[c] = C.si[(int64_t)c * P.np + L.p];
+    L.c0 = P.cnt[3 * L.p]; L.c1 = P.cnt[3 * L.p + 1]; L.c2 = P.cnt[3 * L.p + 2];
+    if (fl & 4) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) K(Traits<METHOD>::F1, c) = C.k1[(int64_t)c * P.np + L.p];
+        return 2;
+    }
+    return 1;
+}
+
+template <int METHOD>
+__device__ __forceinline__ void lane_close(const PtRun &P, const PtCarry &C, const KRows &K,
+                                           const Lane &L, const double si[6], int32_t st,
+                                           bool have_f1)
+{
+    P.cnt[3 * L.p] = L.c0;
+    P.cnt[3 * L.p + 1] = L.c1;
+    P.cnt[3 * L.p + 2] = L.c2;
+    if (P.status) P.status[L.p] = st;
+    if (P.carry) {
+        C.t[L.p] = L.t; C.dt[L.p] = L.dt; C.errold[L.p] = L.errold; C.n[L.p] = L.n;
+        C.flags[L.p] = 1 | (L.rejected ? 2 : 0) | (have_f1 ? 4 : 0);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            C.si[(int64_t)c * P.np + L.p] = si[c];
+            if (have_f1) C.k1[(int64_t)c * P.np + L.p] = K(Traits<METHOD>::F1, c);
+        }
+    }
+    if (st < 0) atomicAdd(P.flags + 1, 1);
+    if (st == PT_ST_TIMEOUT) atomicExch(P.flags, 1);
+}
+
+/* Status before an attempt: PT_GO = go on, else the particle closes. */
+__device__ __forceinline__ int32_t lane_check(const PtRun &P, const Lane &L, uint64_t t_start)
+{
+    if (!(L.t < P.tend)) return (L.t >= P.tmx) ? PT_ST_DONE : PT_ST_RUNNING;
+    const int32_t g = pt_attempt_guard(L.t, L.dt, L.c0, P.max_steps);
+    if (g != PT_GO) return g;
+    if (P.budget_ns && pt_globaltimer() - t_start > P.budget_ns) return PT_ST_TIMEOUT;
+    return PT_GO;
+}
+
+/* dti_guess (integrations.F90:524-589) after its first evaluation ki = f(si);
+ * the second evaluation (:576) does not influence the result. */
+__device__ __forceinline__ double dti_finish(const PtRun &P, int iord, const double si[6],
+                                             const double ki[6])
+{
+    double sr[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) sr[i] = P.atol + P.rtol * fabs(si[i]);
+    double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) { const double q = si[i] / sr[i]; s0 = s0 + q * q; }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) { const double q = ki[i] / sr[i]; s1 = s1 + q * q; }
+    const double d0 = sqrt(s0 / 6.0);
+    const double d1 = sqrt(s1 / 6.0);
+    double dti;
+    if (pt_min(d0, d1) < 1.0e-10) dti = 1.0e-06;
+    else dti = 1.0e-01 * (d0 / d1);
+    double s2 = 0.0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        const double sf = si[i] + dti * ki[i];
+        const double q = (sf - si[i]) / sr[i];
+        s2 = s2 + q * q;
+    }
+    const double d2 = pt_max(d1, sqrt(s2 / 6.0) / dti);
+    double dtf;
+    if (d2 <= 1.0e-15) dtf = pt_max(1.0e-06, 1.0e-03 * dti);
+    else dtf = pt_det_pow(1.0e-02 / d2, 1.0 / (double)iord);
+    return pt_min(pt_min(1.0e+02 * dti, dtf), P.dtm);
+}
+
+/* One cubic-Hermite output row (integrations.F90:159-166 / :448-455).
+ * scale: the slopes are derivatives to be multiplied by dt (DOP853). */
+__device__ __forceinline__ void dense_row(double t, double dt, double tn, const double si[6],
+                                          const double sf[6], const KRows &K, int rowa,
+                                          const double *kb_reg, int rowb, bool scale,
+                                          double *row)
+{
+    const double fr = (t - tn) / dt;
+    const double fl = 1.0 - fr;
+    double st[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const double ds = sf[c] - si[c];
+        const double ka = K(rowa, c);
+        const double kb = kb_reg ? kb_reg[c] : K(rowb, c);
+        const double a = scale ? dt * ka : ka;
+        const double b = scale ? dt * kb : kb;
+        st[c] = fr * si[c] + fl * sf[c] + fl * fr * ((a - ds) * fr + (ds - b) * fl);
+    }
+    const double gam = sqrt(st[3] * st[3] + st[4] * st[4] + st[5] * st[5] + 1.0);
+    double2 *o = reinterpret_cast<double2 *>(row);
+    o[0] = make_double2(st[0], st[1]);
+    o[1] = make_double2(st[2], st[3]);
+    o[2] = make_double2(st[4], st[5]);
+    o[3] = make_double2(gam, dt);
+}
+
+__device__ __forceinline__ bool escaped_x(const PtRun &P, double x)
+{
+    return P.open_x && (x < P.xl[0] || x >= P.xl[0] + P.xs[0]);
+}
+
+/* Stage state of slot j (1..SLOTS-1) in the reference's operand order. */
+template <int METHOD>
+__device__ __forceinline__ void stage_state(int j, const KRows &K, const double si[6], double dt,
+                                            double ss[6])
+{
+    if (METHOD == PT_METHOD_DOP853) {
+        const Stage &S = kDop[j];
+        if (j == 1) {                                           /* :368 */
+            const double h = dt * S.a[0];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) ss[c] = si[c] + h * K(0, c);
+        } else {                                                /* :371-415 */
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                double acc = S.a[0] * K(S.r[0], c);
+                for (int i = 1; i < S.n; ++i) acc = acc + S.a[i] * K(S.r[i], c);
+                ss[c] = si[c] + dt * acc;
+            }
+        }
+    } else {                                                    /* :132-135 */
+        const Stage &S = kCk[j];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            double acc = si[c];
+            for (int i = 0; i < S.n; ++i) acc = acc + S.a[i] * K(S.r[i], c);
+            ss[c] = acc;
+        }
+    }
+}
+
+/* Final combination and error norm: sf and the scaled error (DOP853 err,
+ * RK5 del).  Row 3 receives the 8th-order increment as in :418. */
+template <int METHOD>
+__device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
+                                                 const double si[6], double dt, double sf[6])
+{
+    if (METHOD == PT_METHOD_DOP853) {
+        double sr[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {                           /* :418-421, :425 */
+            const double k4 = B01 * K(0, c) + B06 * K(5, c) + B07 * K(6, c) + B08 * K(7, c)
+                            + B09 * K(8, c) + B10 * K(9, c) + B11 * K(1, c) + B12 * K(2, c);
+            K(3, c) = k4;
+            sf[c] = si[c] + dt * k4;
+            sr[c] = P.atol + P.rtol * pt_max(fabs(si[c]), fabs(sf[c]));
+        }
+        double err3 = 0.0, err5 = 0.0;                          /* :426-437 */
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const double e = K(3, c) - BH1 * K(0, c) - BH2 * K(8, c) - BH3 * K(2, c);
+            const double q = e / sr[c];
+            err3 = err3 + q * q;
+        }
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const double e = ER01 * K(0, c) + ER06 * K(5, c) + ER07 * K(6, c) + ER08 * K(7, c)
+                           + ER09 * K(8, c) + ER10 * K(9, c) + ER11 * K(1, c) + ER12 * K(2, c);
+            const double q = e / sr[c];
+            err5 = err5 + q * q;
+        }
+        const double deno = err5 + 1.0e-02 * err3;
+        return (deno <= 0.0) ? fabs(dt) * err5 / sqrt(6.0) : fabs(dt) * err5 / sqrt(6.0 * deno);
+    } else {                                                    /* :140-148 */
+        double del = 0.0;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            double a = 0.0, e = 0.0;
+            a = a + CK_C1 * K(0, c); a = a + CK_C2 * K(1, c); a = a + CK_C3 * K(2, c);
+            a = a + CK_C4 * K(3, c); a = a + CK_C5 * K(4, c); a = a + CK_C6 * K(5, c);
+            e = e + CK_D1 * K(0, c); e = e + CK_D2 * K(1, c); e = e + CK_D3 * K(2, c);
+            e = e + CK_D4 * K(3, c); e = e + CK_D5 * K(4, c); e = e + CK_D6 * K(5, c);
+            sf[c] = si[c] + a;
+            const double sr = fabs(si[c]) + fabs(K(0, c)) + 2.2250738585072014e-308;
+            const double q = fabs(e / sr);
+            del = (c == 0) ? q : pt_nanmax(del, q);
+        }
+        return del / P.atol;
+    }
+}
+
+/* ---- the kernel ---------------------------------------------------------- */
+
+template <int METHOD, class EV>
+__device__ __forceinline__ void run_machine(const PtRun &P)
+{
+    using T = Traits<METHOD>;
+    extern __shared__ double pt_ksm[];
+    const KRows K{ pt_ksm + threadIdx.x, (int)blockDim.x };
+    const uint64_t t_start = pt_globaltimer();
+    const PtCarry C = P.carry ? pt_carry_view(P.carry, P.np) : PtCarry{};
+    Lane L;
+    L.p = 0; L.t = 0.0; L.dt = 0.0; L.errold = 0.0; L.tnext = 0.0; L.n = 0;
+    L.rejected = false; L.c0 = L.c1 = L.c2 = 0;
+    double si[6] = { 0, 0, 0, 0, 0, 0 };
+    bool active = false, drained = false;
+    int j = 0;
+    for (;;) {
+        double pt[6], a[6], sf[6];
+        bool need = false;
+        int mode = M_IDLE;
+        double q = 0.0;
+        if (j == 0) {
+            /* ---- tail: finish the attempt that just ran ---- */
+            if (active) {
+                q = finish_attempt<METHOD>(P, K, si, L.dt, sf);
+                if (q != q) {
+                    lane_close<METHOD>(P, C, K, L, si, PT_ST_NONFINITE, true);
+                    active = false;
+                } else if (q <= 1.0) {
+                    mode = M_ACCEPT;
+                    need = true;
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) pt[c] = sf[c];
+                } else {
+                    mode = M_REJECT;
+                }
+            }
+            /* ---- idle lanes take the next particle ---- */
+            if (!active && !drained) {
+                const unsigned long long qi = atomicAdd(P.queue, 1ULL);
+                if ((int64_t)qi < P.np) {
+                    L.p = P.order ? (int64_t)P.order[qi] : (int64_t)qi;
+                    const int how = lane_open<METHOD>(P, C, K, L, si);
+                    if (how == 2) {
+                        mode = M_READY;
+                    } else {
+                        mode = M_INIT;
+                        need = true;
+#pragma unroll
+                        for (int c = 0; c < 6; ++c) pt[c] = si[c];
+                    }
+                    active = true;
+                    if (how == 0) L.dt = 0.0;   /* set by dti_finish below */
+                    q = (how == 0) ? 1.0 : 0.0; /* 1 marks a fresh start */
+                } else {
+                    drained = true;
+                }
+            }
+        } else if (active) {
+            stage_state<METHOD>(j, K, si, L.dt, pt);
+            need = true;
+        }
+
+        if (need) EV::f(P, pt, a);                           /* the one evaluation site */
+
+        if (j != 0) {
+            if (active) {
+                const int dst = (METHOD == PT_METHOD_DOP853) ? kDop[j].dst : kCk[j].dst;
+                if (METHOD == PT_METHOD_DOP853) {
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) K(dst, c) = a[c];
+                } else {
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) K(dst, c) = L.dt * a[c];    /* :137 */
+                }
+            }
+        } else {
+            const double dt = L.dt;
+            if (mode == M_ACCEPT) {                                    /* :150-177, :439-476 */
+                L.t = L.t + dt;
+                while (L.n < P.m && L.t >= L.tnext) {
+                    double *row = P.state + (int64_t)8 * ((int64_t)L.n + (int64_t)P.m * L.p);
+                    if (METHOD == PT_METHOD_DOP853)
+                        dense_row(L.t, dt, L.tnext, si, sf, K, 0, a, 0, true, row);
+                    else
+                        dense_row(L.t, dt, L.tnext, si, sf, K, 0, nullptr, 5, false, row);
+                    L.n++;
+                    next_time(P, L);
+                }
+#pragma unroll
+                for (int c = 0; c < 6; ++c) { si[c] = sf[c]; K(T::F1, c) = a[c]; }
+                L.c1++;
+                if (METHOD == PT_METHOD_DOP853) {
+                    double dtn = pt_max(P.fcmn, P.safe * pt_det_pow(q, P.expo)
+                                                       * pt_det_pow(L.errold, P.beta));
+                    dtn = L.rejected ? dt * pt_min(dtn, 1.0) : dt * pt_min(dtn, P.fcmx);
+                    L.errold = pt_max(q, 1.0e-04);
+                    L.rejected = false;
+                    L.dt = dtn;
+                } else {
+                    L.dt = dt * pt_min(P.fcmx, P.safe * pt_det_pow(q, -0.20));
+                }
+                L.c0++;
+                L.dt = pt_min(L.dt, P.dtm);                             /* :195, :500 */
+                if (escaped_x(P, si[0])) {
+                    lane_close<METHOD>(P, C, K, L, si, PT_ST_ESCAPED, true);
+                    active = false;
+                }
+            } else if (mode == M_REJECT) {                            /* :178-187, :480-490 */
+                L.c2++;
+                if (METHOD == PT_METHOD_DOP853) {
+                    L.dt = dt * pt_max(P.fcmn, P.safe * pt_det_pow(q, P.expo));
+                    L.rejected = true;
+                } else {
+                    L.dt = dt * pt_max(P.fcmn, P.safe * pt_det_pow(q, -0.25));
+                }
+                L.c0++;
+                L.dt = pt_min(L.dt, P.dtm);
+            } else if (mode == M_INIT) {
+#pragma unroll
+                for (int c = 0; c < 6; ++c) K(T::F1, c) = a[c];
+                if (q == 1.0) {                                        /* fresh: :120-127 */
+                    L.dt = dti_finish(P, T::IORD, si, a);
+                    double *row = P.state + (int64_t)8 * P.m * L.p;
+                    row[6] = sqrt(si[3] * si[3] + si[4] * si[4] + si[5] * si[5] + 1.0);
+                    row[7] = L.dt;
+                }
+                next_time(P, L);
+            } else if (mode == M_READY) {
+                next_time(P, L);
+            }
+            /* ---- start of the next attempt ---- */
+            if (active) {
+                const int32_t st = lane_check(P, L, t_start);
+                if (st != PT_GO) {
+                    lane_close<METHOD>(P, C, K, L, si, st, true);
+                    active = false;
+                } else if (METHOD == PT_METHOD_RK5) {
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) K(0, c) = L.dt * K(T::F1, c);   /* :137, j = 1 */
+                }
+            }
+            if (!__any_sync(0xffffffffu, active)) {
+                if (!__any_sync(0xffffffffu, !drained)) break;
+                continue;                                               /* j stays 0 */
+            }
+        }
+        j = (j + 1 < T::SLOTS) ? j + 1 : 0;
+    }
+}
+
+}  // namespace pt_sm
+
+#endif /* PT_INTEGRATOR_CUH */

@@ -29,7 +29,7 @@ def test_exports_every_header_symbol(native):
 def test_abi_version_and_carry_size(native):
     assert native.pt_abi_version() == 1
     assert native.pt_carry_bytes(0) == 0
-    assert native.pt_carry_bytes(1000) == 80 * 1000
+    assert native.pt_carry_bytes(1000) == 128 * 1000
 
 
 @pytest.mark.parametrize("name,mid", [("rk5", 1), ("dop853", 2), ("dp853", 2), ("rk8", 2),
