@@ -54,6 +54,10 @@ WORKLOADS = {
     "dop853-256": dict(method="dop853", n=256, spectrum="kolmogorov", nmax=32, db_rms=1.0,
                        v_rms=0.2, eta=1e-3, npart=1 << 20, gamma=(1.001, 1e3), speed=None,
                        tol=1e-10, periods=100, seed=1, window=0.05),
+    # the mixed-precision configuration (configuration 3)
+    "rk5-512": dict(method="rk5", n=512, spectrum="kolmogorov", nmax=32, db_rms=1.0, v_rms=0.2,
+                    eta=0.0, npart=1 << 22, gamma=(1.001, 1e2), speed=None, tol=1e-8,
+                    periods=50, seed=2, window=0.02),
     # the CPU-runnable configuration (reference RK5, 64^3, 1024 particles)
     "rk5-64": dict(method="rk5", n=64, spectrum="flat", nmax=4, db_rms=0.5, v_rms=0.1,
                    eta=0.0, npart=1024, gamma=None, speed=0.5, tol=1e-8, periods=10, seed=0,
@@ -68,7 +72,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="dop853-256")
-    ap.add_argument("--precision", choices=["fp64", "fp64_fma"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "fp64_fma", "fp32"], default="fp64")
     ap.add_argument("--particles", type=int, default=0,
                     help="override the particle count (profiling of small cases only)")
     ap.add_argument("--window", type=float, default=0.0,
@@ -76,6 +80,10 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
+    ap.add_argument("--mixed-steps", type=int, default=5)
+    ap.add_argument("--accuracy-particles", type=int, default=32768)
+    ap.add_argument("--accuracy-seconds", type=float, default=40.0)
     return ap.parse_args()
 
 
@@ -86,8 +94,9 @@ def dist_env():
     return rank, world, local
 
 
-def build_inputs(cfg, npart, rank):
-    """Fields (reference layout), params, time grid and this rank's particles."""
+def build_inputs(cfg, npart, rank, backend="numpy"):
+    """Fields (reference layout), params, time grid and this rank's particles.
+    backend "torch" synthesises the fields on the GPU (CUDA tensors)."""
     from particles_gb300 import fields, initial, params
     tmax = cfg["periods"] * T0
     prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=tmax, atol=cfg["tol"],
@@ -95,7 +104,7 @@ def build_inputs(cfg, npart, rank):
     tg = params.time_grid(cfg["periods"], tmax)
     out = fields.snapshot(cfg["n"], db_rms=cfg["db_rms"], v_rms=cfg["v_rms"], vunit=VUN,
                           spectrum=cfg["spectrum"], nmin=1.0, nmax=cfg["nmax"],
-                          seed=cfg["seed"], with_j=cfg["eta"] != 0.0)
+                          seed=cfg["seed"], with_j=cfg["eta"] != 0.0, backend=backend)
     idx = np.arange(rank * npart, (rank + 1) * npart, dtype=np.uint64)
     s0 = initial.isotropic_state(npart, cfg["seed"], speed=cfg["speed"],
                                  gamma_range=cfg["gamma"], index=idx)
@@ -265,6 +274,119 @@ def workload_config(cfg, npart, window, args):
     }
 
 
+def ks_distance(a, b):
+    """Two-sample Kolmogorov-Smirnov statistic."""
+    a, b = np.sort(np.asarray(a)), np.sort(np.asarray(b))
+    grid = np.concatenate([a, b])
+    fa = np.searchsorted(a, grid, side="right") / a.size
+    fb = np.searchsorted(b, grid, side="right") / b.size
+    return float(np.abs(fa - fb).max())
+
+
+def mixed_leg(args, dev, stream):
+    """Configuration 3 (RK5, rtol 1e-8, 512^3, 2^22 particles): accepted
+    particle-steps/s of the exact FP64, FMA FP64 and mixed FP32 kernels on the
+    same windows, and the mixed kernel's per-particle energy / position error
+    against the exact kernel (bit-identical to the CPU oracle) at a common
+    output time."""
+    import torch
+    from particles_gb300 import Fields, fields, initial, params
+    cfg = WORKLOADS["rk5-512"]
+    npart, window = cfg["npart"], cfg["window"]
+    tmax = cfg["periods"] * T0
+    prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=tmax, atol=cfg["tol"],
+                             rtol=cfg["tol"], facmin=0.333, facmax=6.0, safe=0.9, beta=0.0)
+    tg = params.time_grid(cfg["periods"], tmax)
+    m = tg.size
+    uu, bb = fields.snapshot(cfg["n"], db_rms=cfg["db_rms"], v_rms=cfg["v_rms"], vunit=VUN,
+                             spectrum=cfg["spectrum"], nmin=1.0, nmax=cfg["nmax"],
+                             seed=cfg["seed"], backend="torch")
+    s0 = initial.isotropic_state(npart, cfg["seed"], gamma_range=cfg["gamma"])
+    d_time = torch.tensor(tg, device=dev)
+    out = {"workload": "rk5-512", "grid": "512^3", "particles": npart, "rtol": cfg["tol"],
+           "window_gyroperiods": window, "steps": args.mixed_steps, "warmup": args.warmup}
+    handles = {}
+    for prec in ("fp64", "fp64_fma", "fp32"):
+        handles[prec] = Fields(uu, bb, precision=prec, stream=stream.cuda_stream)
+    del uu, bb
+    torch.cuda.empty_cache()
+
+    def fresh(n):
+        st = torch.zeros((n, m, 8), dtype=torch.float64, device=dev)
+        st[:, 0, :6] = torch.tensor(s0[:n], device=dev)
+        return (st, torch.zeros((n, 3), dtype=torch.int64, device=dev),
+                torch.zeros(n, dtype=torch.int32, device=dev),
+                torch.zeros(int(handles["fp64"]._L.pt_carry_bytes(n)), dtype=torch.uint8,
+                            device=dev))
+
+    rates = {}
+    for prec, f in handles.items():
+        st, cnt, status, carry = fresh(npart)
+        w = 0
+        for _ in range(args.warmup):
+            w += 1
+            f.run_device("rk5", prm, d_time, st, cnt, status, carry, t_stop=w * window * T0,
+                         time_budget_s=900.0, stream=stream.cuda_stream)
+        stream.synchronize()
+        c0 = cnt.sum(0).cpu().numpy()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.mixed_steps):
+            w += 1
+            f.run_device("rk5", prm, d_time, st, cnt, status, carry, t_stop=w * window * T0,
+                         time_budget_s=900.0, stream=stream.cuda_stream)
+        e1.record(stream)
+        stream.synchronize()
+        if f.run_check() != 0:
+            raise RuntimeError(f"mixed leg {prec} failed")
+        d = cnt.sum(0).cpu().numpy() - c0
+        sec = e0.elapsed_time(e1) * 1e-3
+        rates[prec] = {"value": float(d[1]) / sec, "attempts_per_s": float(d[0]) / sec,
+                       "rejected_fraction": float(d[2] / max(d[0], 1)),
+                       "ms_per_step": 1e3 * sec / args.mixed_steps}
+        del st, cnt, status, carry
+        torch.cuda.empty_cache()
+    out["accepted_steps_per_s"] = {k: v["value"] for k, v in rates.items()}
+    out["detail"] = rates
+    out["mixed_over_plain_exact"] = rates["fp32"]["value"] / rates["fp64"]["value"]
+    out["mixed_over_plain_fma"] = rates["fp32"]["value"] / rates["fp64_fma"]["value"]
+
+    # accuracy: a seeded subsample integrated as far as the time budget allows
+    na = min(args.accuracy_particles, npart)
+    res = {}
+    for prec in ("fp64", "fp32"):
+        st, cnt, status, carry = fresh(na)
+        t_start = time.perf_counter()
+        w = 0
+        while True:
+            w += 1
+            handles[prec].run_device("rk5", prm, d_time, st, cnt, status, carry,
+                                     t_stop=min(w * T0, tmax), time_budget_s=900.0,
+                                     stream=stream.cuda_stream)
+            stream.synchronize()
+            if w >= cfg["periods"] or time.perf_counter() - t_start > args.accuracy_seconds / 2:
+                break
+        res[prec] = (st.cpu().numpy(), w)
+    nrow = min(res["fp64"][1], res["fp32"][1])        # sample index reached by both
+    se, sm = res["fp64"][0][:, nrow], res["fp32"][0][:, nrow]
+    g_rel = np.abs(sm[:, 6] - se[:, 6]) / se[:, 6]
+    dpos = np.linalg.norm(sm[:, :3] - se[:, :3], axis=1)
+    out["accuracy"] = {
+        "particles": na, "t_gyroperiods": float(tg[nrow] / T0),
+        "reference": "exact FP64 kernel (bit-identical to the CPU oracle)",
+        "energy_rel_err_median": float(np.median(g_rel)),
+        "energy_rel_err_p90": float(np.percentile(g_rel, 90)),
+        "energy_rel_err_max": float(g_rel.max()),
+        "mean_energy_rel_err": float(abs(sm[:, 6].mean() / se[:, 6].mean() - 1.0)),
+        "position_err_median": float(np.median(dpos)),
+        "position_err_p90": float(np.percentile(dpos, 90)),
+        "ks_gamma": ks_distance(se[:, 6], sm[:, 6]),
+    }
+    for f in handles.values():
+        f.close()
+    return out
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -283,14 +405,17 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     npart = args.particles or cfg["npart"]
     window = args.window or cfg["window"]
-    prm, tg, out, s0 = build_inputs(cfg, npart, rank)
-    uu, bb = out[:2]
-    jj = out[2] if len(out) > 2 else None
+    big = cfg["n"] >= 512
+    prm, tg, out, s0 = build_inputs(cfg, npart, rank, backend="torch" if big else "numpy")
     L = N.load()
     m = tg.size
     dev = torch.device("cuda", local)
-    f = Fields(uu, bb, jj, precision=args.precision)
-    rec_bytes = (10 if jj is not None else 6) * 8
+    f = Fields(out[0], out[1], out[2] if len(out) > 2 else None, precision=args.precision)
+    if big:                                   # host copies only for the CPU baseline
+        out = tuple(a.cpu().numpy() for a in out) if not args.no_cpu else None
+        torch.cuda.empty_cache()
+    rec_bytes = ((10 if cfg["eta"] != 0.0 else 6) * 8 if args.precision != "fp32"
+                 else (12 if cfg["eta"] != 0.0 else 8) * 4)
     stream = torch.cuda.Stream(device=dev)
     with torch.cuda.stream(stream):
         d_time = torch.tensor(tg, device=dev)
@@ -351,7 +476,7 @@ def main():
 
     # roofline of the dominant (only) kernel: algorithmic FP64 flops / event time
     flops = roofline.run_flops(cfg["method"], np.array([dcnt_tot]), with_eta=cfg["eta"] != 0.0,
-                               fresh=False, resumed=npart * args.steps)
+                               fresh=False)
     achieved = flops / dev_s
     pk = C.c_double()
     L.pt_probe_peak(0, 16384, C.byref(pk))
@@ -414,6 +539,11 @@ def main():
     if not args.no_cpu and rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline(cfg, prm, tg, out, s0, window, args.warmup,
                                             args.steps, args.cpu_seconds)
+    if not args.no_mixed and rank == 0 and args.workload == "dop853-256":
+        f.close()
+        del d_state, d_cnt, d_status, d_carry
+        torch.cuda.empty_cache()
+        line["mixed"] = mixed_leg(args, dev, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

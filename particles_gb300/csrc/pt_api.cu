@@ -58,7 +58,9 @@ struct pt_fields {
     int32_t has_j;
     int32_t device;
     int64_t nodes;
-    double *rec64;              /* FP64 records */
+    double *rec64;              /* FP64 records (PT_PREC_FP64, PT_PREC_FP64_FMA) */
+    float *rec32;               /* FP32 records (PT_PREC_FP32) */
+    int32_t nc32;               /* FP32 record width: 8 or 12 */
     int64_t bytes;
     unsigned long long *scratch;   /* [0] queue head, [1] flags (2 x int32) */
 };
@@ -81,6 +83,24 @@ __global__ void k_pack_records64(int64_t nn, const double *__restrict__ uu,
     }
 }
 
+/* Planar reference layout -> FP32 node records { U, B, 0, 0 } or { U, B, J, 0, 0, 0 }. */
+__global__ void k_pack_records32(int64_t nn, const double *__restrict__ uu,
+                                 const double *__restrict__ bb, const double *__restrict__ jj,
+                                 int nc, float *__restrict__ rec)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float4 *o = reinterpret_cast<float4 *>(rec + i * nc);
+        o[0] = make_float4((float)uu[i], (float)uu[i + nn], (float)uu[i + 2 * nn], (float)bb[i]);
+        if (nc == 12) {
+            o[1] = make_float4((float)bb[i + nn], (float)bb[i + 2 * nn], (float)jj[i], (float)jj[i + nn]);
+            o[2] = make_float4((float)jj[i + 2 * nn], 0.f, 0.f, 0.f);
+        } else {
+            o[1] = make_float4((float)bb[i + nn], (float)bb[i + 2 * nn], 0.f, 0.f);
+        }
+    }
+}
+
 static bool dims_ok(const int32_t dm[3])
 {
     if (!dm) return false;
@@ -98,7 +118,7 @@ static int fields_create_impl(const int32_t dm[3], const double *uu, const doubl
     *out = nullptr;
     if (!dims_ok(dm)) return set_err(PT_ERR_ARG, "pt_fields_create: bad dm%s");
     if (!uu || !bb) return set_err(PT_ERR_ARG, "pt_fields_create: uu/bb is NULL%s");
-    if (precision != PT_PREC_FP64 && precision != PT_PREC_FP64_FMA)
+    if (precision != PT_PREC_FP64 && precision != PT_PREC_FP64_FMA && precision != PT_PREC_FP32)
         return set_err(PT_ERR_UNSUPPORTED, "pt_fields_create: precision not built%s");
 
     int rc = PT_OK;
@@ -110,11 +130,17 @@ static int fields_create_impl(const int32_t dm[3], const double *uu, const doubl
     f->precision = precision;
     f->has_j = jj != nullptr;
     f->nc = f->has_j ? 10 : 6;
+    f->nc32 = f->has_j ? 12 : 8;
     f->nodes = nn;
     PT_CU(cudaGetDevice(&f->device));
     PT_CU(cudaMalloc(&f->scratch, 256));
-    PT_CU(cudaMalloc(&f->rec64, (size_t)nn * f->nc * sizeof(double)));
-    f->bytes = (int64_t)nn * f->nc * sizeof(double) + 256;
+    if (precision == PT_PREC_FP32) {
+        PT_CU(cudaMalloc(&f->rec32, (size_t)nn * f->nc32 * sizeof(float)));
+        f->bytes = (int64_t)nn * f->nc32 * sizeof(float) + 256;
+    } else {
+        PT_CU(cudaMalloc(&f->rec64, (size_t)nn * f->nc * sizeof(double)));
+        f->bytes = (int64_t)nn * f->nc * sizeof(double) + 256;
+    }
     if (on_device) {
         d_uu = const_cast<double *>(uu);
         d_bb = const_cast<double *>(bb);
@@ -132,7 +158,10 @@ static int fields_create_impl(const int32_t dm[3], const double *uu, const doubl
     {
         int64_t blocks = (nn + 255) / 256;
         if (blocks > 65536) blocks = 65536;
-        k_pack_records64<<<(int)blocks, 256, 0, stream>>>(nn, d_uu, d_bb, d_jj, f->nc, f->rec64);
+        if (precision == PT_PREC_FP32)
+            k_pack_records32<<<(int)blocks, 256, 0, stream>>>(nn, d_uu, d_bb, d_jj, f->nc32, f->rec32);
+        else
+            k_pack_records64<<<(int)blocks, 256, 0, stream>>>(nn, d_uu, d_bb, d_jj, f->nc, f->rec64);
         PT_CU(cudaGetLastError());
     }
     PT_CU(cudaStreamSynchronize(stream));
@@ -144,6 +173,7 @@ done:
     }
     if (rc != PT_OK) {
         cudaFree(f->rec64);
+        cudaFree(f->rec32);
         cudaFree(f->scratch);
         delete f;
         return rc;
@@ -169,6 +199,7 @@ extern "C" int pt_fields_destroy(pt_fields *f)
 {
     if (!f) return PT_OK;
     cudaFree(f->rec64);
+    cudaFree(f->rec32);
     cudaFree(f->scratch);
     delete f;
     return PT_OK;
@@ -220,9 +251,16 @@ static void unpack_params(const double *p, const RunShape &g, PtRun &R)
         R.dm[i] = g.dm[i];
         R.dmr[i] = (double)g.dm[i];
         R.inv_dm[i] = 1.0 / (double)g.dm[i];
+        R.dm_mask[i] = ((g.dm[i] & (g.dm[i] - 1)) == 0) ? g.dm[i] - 1 : 0;
+        R.gsx[i] = (double)g.dm[i] / R.xs[i];
+        R.gox[i] = -R.xl[i] * R.gsx[i];
+        R.gsxf[i] = (float)R.gsx[i];
         unit = unit && (R.xl[i] == 0.0) && !signbit(R.xl[i]) && (R.xs[i] == 1.0);
     }
     R.unit_map = unit ? 1 : 0;
+    R.inv_vun = 1.0 / R.vun;
+    R.ivunf = (float)R.inv_vun;
+    R.qomf = (float)R.qom;
 }
 
 /* Argument checks and the host part of a run: everything but pointers. */
@@ -260,6 +298,7 @@ static int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
         return set_err(PT_ERR_ARG, "field handle holds J but eta == 0%s");
     unpack_params(params, g, R);
     R.eta = eta;
+    R.etaf = (float)eta;
     R.has_j = g.has_j;
     R.open_x = open_x ? 1 : 0;
     R.max_steps = max_steps > 0 ? max_steps : 1000000000LL;
@@ -289,6 +328,7 @@ static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
     int rc = prepare_run(method, np, m, shape_of(f), params, opt, R);
     if (rc != PT_OK) return rc;
     R.fld = f->rec64;
+    R.fld32 = f->rec32;
     R.time = d_time;
     R.state = d_state;
     R.cnt = d_cnt;
@@ -306,8 +346,11 @@ static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
     if (e != cudaSuccess) return cuda_err(e, "scratch reset");
     if (f->precision == PT_PREC_FP64)
         e = method == PT_METHOD_RK5 ? pt_launch_rk5_exact(R, f->nc, s) : pt_launch_dp853_exact(R, f->nc, s);
-    else
+    else if (f->precision == PT_PREC_FP64_FMA)
         e = method == PT_METHOD_RK5 ? pt_launch_rk5_fma(R, f->nc, s) : pt_launch_dp853_fma(R, f->nc, s);
+    else
+        e = method == PT_METHOD_RK5 ? pt_launch_rk5_mixed(R, f->nc32, s)
+                                    : pt_launch_dp853_mixed(R, f->nc32, s);
     if (e != cudaSuccess) return cuda_err(e, "kernel launch");
     return PT_OK;
 }
@@ -524,10 +567,15 @@ extern "C" int pt_debug_accel(const pt_fields *f, int64_t n, const double params
     RunShape g = shape_of(f);
     unpack_params(params, g, R);
     R.fld = f->rec64;
+    R.fld32 = f->rec32;
     R.has_j = f->has_j;
     R.eta = 0.0;
-    cudaError_t e = (f->precision == PT_PREC_FP64)
-        ? pt_launch_accel_exact(R, f->nc, n, d_vec, d_acc, (cudaStream_t)stream)
-        : pt_launch_accel_fma(R, f->nc, n, d_vec, d_acc, (cudaStream_t)stream);
+    cudaError_t e;
+    if (f->precision == PT_PREC_FP64)
+        e = pt_launch_accel_exact(R, f->nc, n, d_vec, d_acc, (cudaStream_t)stream);
+    else if (f->precision == PT_PREC_FP64_FMA)
+        e = pt_launch_accel_fma(R, f->nc, n, d_vec, d_acc, (cudaStream_t)stream);
+    else
+        e = pt_launch_accel_mixed(R, f->nc32, n, d_vec, d_acc, (cudaStream_t)stream);
     return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_accel");
 }

@@ -26,7 +26,12 @@ struct PtRun {
     double xl[3], xs[3];
     /* grid */
     double inv_dm[3], dmr[3];
+    double gsx[3], gox[3];  /* node coordinate = x * gsx + gox = (x - xl) / xs * dm */
+    double inv_vun;         /* 1 / vun, correctly rounded */
+    float gsxf[3];          /* gsx rounded to FP32 (mixed precision) */
+    float ivunf, qomf, etaf;
     int32_t dm[3];
+    int32_t dm_mask[3];     /* dm - 1 when dm is a power of two, else 0 */
     int32_t unit_map;      /* xl == +0 and xs == 1: (pos - xl) / xs == pos exactly */
     /* extensions */
     double eta;
@@ -127,6 +132,11 @@ struct PtLaunch {
 
 PT_DECLARE_FP64_LAUNCHERS(exact)
 PT_DECLARE_FP64_LAUNCHERS(fma)
+
+cudaError_t pt_launch_rk5_mixed(const PtRun &P, int nc, cudaStream_t s);
+cudaError_t pt_launch_dp853_mixed(const PtRun &P, int nc, cudaStream_t s);
+cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int64_t n, const double *vec,
+                                  double *acc, cudaStream_t s);
 
 cudaError_t pt_launch_debug_pow(int64_t n, const double *x, const double *y, double *out,
                                 cudaStream_t s);

@@ -61,7 +61,11 @@ __device__ __forceinline__ void load_rec(const double *__restrict__ fld, int64_t
  * (accelerations.F90:84-92). */
 template <int NC>
 struct EvalF64 {
-    static __device__ __forceinline__ void f(const PtRun &P, const double s[6], double a[6])
+    static constexpr bool kDelta = false;
+    struct Origin {};
+    static __device__ __forceinline__ void begin(const PtRun &, const double *, Origin &) {}
+    static __device__ __forceinline__ void f(const PtRun &P, const double s[6], const double *,
+                                             const Origin &, double a[6])
     {
         constexpr int NV = (NC == 10) ? 9 : 6;
         int32_t l[3], r[3];
@@ -128,7 +132,8 @@ __global__ void k_accel(const PtRun P, int64_t n, const double *vec, double *acc
         double s[6], a[6];
 #pragma unroll
         for (int c = 0; c < 6; ++c) s[c] = vec[6 * i + c];
-        EvalF64<NC>::f(P, s, a);
+        typename EvalF64<NC>::Origin o;
+        EvalF64<NC>::f(P, s, nullptr, o, a);
 #pragma unroll
         for (int c = 0; c < 6; ++c) acc[6 * i + c] = a[c];
     }

@@ -24,8 +24,14 @@
  * for bit; the same code compiled with contraction is the FMA variant.
  *
  * The evaluation f(s) is a policy type EV with
- *     static __device__ void f(const PtRun &P, const double s[6], double a[6]);
- * (FP64 records, or FP32 records for mixed precision).
+ *     static constexpr bool kDelta;     evaluates from an origin + increment
+ *     struct Origin;                     per-lane data made by begin()
+ *     static void begin(const PtRun&, const double si[6], Origin&);
+ *     static void f(const PtRun&, const double s[6], const double d[6],
+ *                   const Origin&, double a[6]);
+ * where s is the stage state and d = s - si its increment from the
+ * attempt's start (FP64 records use s; mixed precision places the stage
+ * relative to the cell origin of si and uses d for the position).
  */
 #ifndef PT_INTEGRATOR_CUH
 #define PT_INTEGRATOR_CUH
@@ -249,32 +255,43 @@ __device__ __forceinline__ bool escaped_x(const PtRun &P, double x)
     return P.open_x && (x < P.xl[0] || x >= P.xl[0] + P.xs[0]);
 }
 
-/* Stage state of slot j (1..SLOTS-1) in the reference's operand order. */
-template <int METHOD>
+/* Stage state of slot j (1..SLOTS-1) in the reference's operand order, and
+ * its increment d = s - si.  DOP853 forms s = si + (dt * sum) (:368-415), so
+ * the increment is exact and free; RK5 sums from si (:132-135), so with
+ * DELTA the increment is summed first (mixed precision only). */
+template <int METHOD, bool DELTA>
 __device__ __forceinline__ void stage_state(int j, const KRows &K, const double si[6], double dt,
-                                            double ss[6])
+                                            double ss[6], double dl[6])
 {
     if (METHOD == PT_METHOD_DOP853) {
         const Stage &S = kDop[j];
         if (j == 1) {                                           /* :368 */
             const double h = dt * S.a[0];
 #pragma unroll
-            for (int c = 0; c < 6; ++c) ss[c] = si[c] + h * K(0, c);
+            for (int c = 0; c < 6; ++c) { dl[c] = h * K(0, c); ss[c] = si[c] + dl[c]; }
         } else {                                                /* :371-415 */
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
                 double acc = S.a[0] * K(S.r[0], c);
                 for (int i = 1; i < S.n; ++i) acc = acc + S.a[i] * K(S.r[i], c);
-                ss[c] = si[c] + dt * acc;
+                dl[c] = dt * acc;
+                ss[c] = si[c] + dl[c];
             }
         }
     } else {                                                    /* :132-135 */
         const Stage &S = kCk[j];
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-            double acc = si[c];
-            for (int i = 0; i < S.n; ++i) acc = acc + S.a[i] * K(S.r[i], c);
-            ss[c] = acc;
+            if (DELTA) {
+                double acc = S.a[0] * K(S.r[0], c);
+                for (int i = 1; i < S.n; ++i) acc = acc + S.a[i] * K(S.r[i], c);
+                dl[c] = acc;
+                ss[c] = si[c] + acc;
+            } else {
+                double acc = si[c];
+                for (int i = 0; i < S.n; ++i) acc = acc + S.a[i] * K(S.r[i], c);
+                ss[c] = acc;
+            }
         }
     }
 }
@@ -283,7 +300,8 @@ __device__ __forceinline__ void stage_state(int j, const KRows &K, const double 
  * RK5 del).  Row 3 receives the 8th-order increment as in :418. */
 template <int METHOD>
 __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
-                                                 const double si[6], double dt, double sf[6])
+                                                 const double si[6], double dt, double sf[6],
+                                                 double dsf[6])
 {
     if (METHOD == PT_METHOD_DOP853) {
         double sr[6];
@@ -292,7 +310,8 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
             const double k4 = B01 * K(0, c) + B06 * K(5, c) + B07 * K(6, c) + B08 * K(7, c)
                             + B09 * K(8, c) + B10 * K(9, c) + B11 * K(1, c) + B12 * K(2, c);
             K(3, c) = k4;
-            sf[c] = si[c] + dt * k4;
+            dsf[c] = dt * k4;
+            sf[c] = si[c] + dsf[c];
             sr[c] = P.atol + P.rtol * pt_max(fabs(si[c]), fabs(sf[c]));
         }
         double err3 = 0.0, err5 = 0.0;                          /* :426-437 */
@@ -320,6 +339,7 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
             a = a + CK_C4 * K(3, c); a = a + CK_C5 * K(4, c); a = a + CK_C6 * K(5, c);
             e = e + CK_D1 * K(0, c); e = e + CK_D2 * K(1, c); e = e + CK_D3 * K(2, c);
             e = e + CK_D4 * K(3, c); e = e + CK_D5 * K(4, c); e = e + CK_D6 * K(5, c);
+            dsf[c] = a;
             sf[c] = si[c] + a;
             const double sr = fabs(si[c]) + fabs(K(0, c)) + 2.2250738585072014e-308;
             const double q = fabs(e / sr);
@@ -343,25 +363,26 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
     L.p = 0; L.t = 0.0; L.dt = 0.0; L.errold = 0.0; L.tnext = 0.0; L.n = 0;
     L.rejected = false; L.c0 = L.c1 = L.c2 = 0;
     double si[6] = { 0, 0, 0, 0, 0, 0 };
+    typename EV::Origin O;
     bool active = false, drained = false;
     int j = 0;
     for (;;) {
-        double pt[6], a[6], sf[6];
-        bool need = false;
+        /* pt: the evaluation point; in the tail it holds sf (accepted lanes)
+         * or si (particles that start), and f(pt) lands in a; dl = pt - si. */
+        double pt[6], dl[6], a[6];
+        bool need = false, fresh = false;
         int mode = M_IDLE;
         double q = 0.0;
         if (j == 0) {
             /* ---- tail: finish the attempt that just ran ---- */
             if (active) {
-                q = finish_attempt<METHOD>(P, K, si, L.dt, sf);
+                q = finish_attempt<METHOD>(P, K, si, L.dt, pt, dl);
                 if (q != q) {
                     lane_close<METHOD>(P, C, K, L, si, PT_ST_NONFINITE, true);
                     active = false;
                 } else if (q <= 1.0) {
                     mode = M_ACCEPT;
                     need = true;
-#pragma unroll
-                    for (int c = 0; c < 6; ++c) pt[c] = sf[c];
                 } else {
                     mode = M_REJECT;
                 }
@@ -378,21 +399,21 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
                         mode = M_INIT;
                         need = true;
 #pragma unroll
-                        for (int c = 0; c < 6; ++c) pt[c] = si[c];
+                        for (int c = 0; c < 6; ++c) { pt[c] = si[c]; dl[c] = 0.0; }
+                        EV::begin(P, si, O);
                     }
                     active = true;
-                    if (how == 0) L.dt = 0.0;   /* set by dti_finish below */
-                    q = (how == 0) ? 1.0 : 0.0; /* 1 marks a fresh start */
+                    fresh = (how == 0);
                 } else {
                     drained = true;
                 }
             }
         } else if (active) {
-            stage_state<METHOD>(j, K, si, L.dt, pt);
+            stage_state<METHOD, EV::kDelta>(j, K, si, L.dt, pt, dl);
             need = true;
         }
 
-        if (need) EV::f(P, pt, a);                           /* the one evaluation site */
+        if (need) EV::f(P, pt, dl, O, a);                    /* the one evaluation site */
 
         if (j != 0) {
             if (active) {
@@ -407,29 +428,38 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
             }
         } else {
             const double dt = L.dt;
+            /* The controller's power of the error ratio, evaluated once for
+             * accepted and rejected lanes together (converged): safe * q^y
+             * with y = expo (DOP853, :466, :486) or -0.20 / -0.25 (RK5, :177,
+             * :186).  The products below keep the reference's order. */
+            double fpow = 0.0;
+            if (mode == M_ACCEPT || mode == M_REJECT) {
+                const double y = (METHOD == PT_METHOD_DOP853) ? P.expo
+                               : (mode == M_ACCEPT ? -0.20 : -0.25);
+                fpow = P.safe * pt_det_pow(q, y);
+            }
             if (mode == M_ACCEPT) {                                    /* :150-177, :439-476 */
                 L.t = L.t + dt;
                 while (L.n < P.m && L.t >= L.tnext) {
                     double *row = P.state + (int64_t)8 * ((int64_t)L.n + (int64_t)P.m * L.p);
                     if (METHOD == PT_METHOD_DOP853)
-                        dense_row(L.t, dt, L.tnext, si, sf, K, 0, a, 0, true, row);
+                        dense_row(L.t, dt, L.tnext, si, pt, K, 0, a, 0, true, row);
                     else
-                        dense_row(L.t, dt, L.tnext, si, sf, K, 0, nullptr, 5, false, row);
+                        dense_row(L.t, dt, L.tnext, si, pt, K, 0, nullptr, 5, false, row);
                     L.n++;
                     next_time(P, L);
                 }
 #pragma unroll
-                for (int c = 0; c < 6; ++c) { si[c] = sf[c]; K(T::F1, c) = a[c]; }
+                for (int c = 0; c < 6; ++c) { si[c] = pt[c]; K(T::F1, c) = a[c]; }
                 L.c1++;
                 if (METHOD == PT_METHOD_DOP853) {
-                    double dtn = pt_max(P.fcmn, P.safe * pt_det_pow(q, P.expo)
-                                                       * pt_det_pow(L.errold, P.beta));
+                    double dtn = pt_max(P.fcmn, fpow * pt_det_pow(L.errold, P.beta));
                     dtn = L.rejected ? dt * pt_min(dtn, 1.0) : dt * pt_min(dtn, P.fcmx);
                     L.errold = pt_max(q, 1.0e-04);
                     L.rejected = false;
                     L.dt = dtn;
                 } else {
-                    L.dt = dt * pt_min(P.fcmx, P.safe * pt_det_pow(q, -0.20));
+                    L.dt = dt * pt_min(P.fcmx, fpow);
                 }
                 L.c0++;
                 L.dt = pt_min(L.dt, P.dtm);                             /* :195, :500 */
@@ -439,18 +469,14 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
                 }
             } else if (mode == M_REJECT) {                            /* :178-187, :480-490 */
                 L.c2++;
-                if (METHOD == PT_METHOD_DOP853) {
-                    L.dt = dt * pt_max(P.fcmn, P.safe * pt_det_pow(q, P.expo));
-                    L.rejected = true;
-                } else {
-                    L.dt = dt * pt_max(P.fcmn, P.safe * pt_det_pow(q, -0.25));
-                }
+                L.dt = dt * pt_max(P.fcmn, fpow);
+                if (METHOD == PT_METHOD_DOP853) L.rejected = true;
                 L.c0++;
                 L.dt = pt_min(L.dt, P.dtm);
             } else if (mode == M_INIT) {
 #pragma unroll
                 for (int c = 0; c < 6; ++c) K(T::F1, c) = a[c];
-                if (q == 1.0) {                                        /* fresh: :120-127 */
+                if (fresh) {                                           /* :120-127 */
                     L.dt = dti_finish(P, T::IORD, si, a);
                     double *row = P.state + (int64_t)8 * P.m * L.p;
                     row[6] = sqrt(si[3] * si[3] + si[4] * si[4] + si[5] * si[5] + 1.0);
@@ -466,9 +492,12 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
                 if (st != PT_GO) {
                     lane_close<METHOD>(P, C, K, L, si, st, true);
                     active = false;
-                } else if (METHOD == PT_METHOD_RK5) {
+                } else {
+                    if (METHOD == PT_METHOD_RK5) {
 #pragma unroll
-                    for (int c = 0; c < 6; ++c) K(0, c) = L.dt * K(T::F1, c);   /* :137, j = 1 */
+                        for (int c = 0; c < 6; ++c) K(0, c) = L.dt * K(T::F1, c);   /* :137, j = 1 */
+                    }
+                    EV::begin(P, si, O);
                 }
             }
             if (!__any_sync(0xffffffffu, active)) {

@@ -1,0 +1,204 @@
+/*
+ * pt_mixed.cu -- mixed-precision fused integrators (PT_PREC_FP32).
+ *
+ * The step machine of pt_integrator.cuh keeps everything that accumulates in
+ * FP64: the particle state si/sf, every stage sum, the embedded error norm,
+ * the step-size controller and the dense output.  Only the evaluation f(s)
+ * changes: the field records are FP32 and the trilinear gather and the
+ * Lorentz force run in FP32 (128 FMA/clk/SM on GB300 against 2 DP ops/clk/SM).
+ *
+ * f(s) in FP32 (same physics as accelerations.F90:59-96 with
+ * interpolations.F90:104-226):
+ *   - once per attempt, the cell of si and the offset of si in it are found
+ *     in FP64 ((x - xl) / xs * dm, periodic floor), so they stay exact far
+ *     from the origin;
+ *   - a stage at si + d sits at offset + d * dm / xs cells from that cell,
+ *     computed in FP32 (d spans a few cells at most);
+ *   - the right-hand neighbour is (left + 1) mod dm, the periodic neighbour
+ *     the reference computes through x + 1/dm;
+ *   - weights, gather and force in FP32; FP64 <-> FP32 conversions use the
+ *     integer pipe (pt_convert.cuh), so an evaluation issues no FP64-pipe
+ *     instruction at all (the exact FP64 evaluation issues ~290).
+ *
+ * Field records (HBM): 8 floats {Ux,Uy,Uz,Bx,By,Bz,0,0} = one 32-B sector per
+ * node, or 12 floats {U,B,J,0,0,0} = 48 B with eta J; x-fastest node order.
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "pt_common.cuh"
+#include "pt_convert.cuh"
+#include "pt_integrator.cuh"
+
+#define PT_BLOCK 128
+
+namespace {
+
+template <int NC>
+__device__ __forceinline__ void load_rec32(const float *__restrict__ fld, int64_t node, float v[NC])
+{
+    const float4 *q = reinterpret_cast<const float4 *>(fld + node * NC);
+#pragma unroll
+    for (int i = 0; i < NC / 4; ++i) {
+        const float4 x = __ldg(q + i);
+        v[4 * i] = x.x;
+        v[4 * i + 1] = x.y;
+        v[4 * i + 2] = x.z;
+        v[4 * i + 3] = x.w;
+    }
+}
+
+template <int NC>
+struct EvalF32 {
+    static constexpr bool kDelta = true;
+    /* Cell of si and the offset of si inside it (FP32), fixed for one attempt. */
+    struct Origin {
+        int32_t cell[3];
+        float off[3];
+    };
+
+    /* Once per attempt, in FP64: node coordinate (x - xl) / xs * dm of si. */
+    static __device__ __forceinline__ void begin(const PtRun &P, const double si[6], Origin &O)
+    {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const double xn = fma(si[i], P.gsx[i], P.gox[i]);
+            const double fl = floor(xn);
+            O.off[i] = pt_d2f(xn - fl);
+            O.cell[i] = (int32_t)fl;          /* beyond 2^31 cells it saturates */
+        }
+    }
+
+    /* f(s) with s = si + d: the stage position relative to the origin cell is
+     * off + d * dm / xs in FP32 (d is at most a few cells); momenta, gather and
+     * force in FP32; every FP64 <-> FP32 conversion on the integer pipe. */
+    static __device__ __forceinline__ void f(const PtRun &P, const double s[6], const double d[6],
+                                             const Origin &O, double a[6])
+    {
+        constexpr int NV = (NC == 12) ? 9 : 6;
+        int32_t l[3], r[3];
+        float xd[3], xu[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const float rel = fmaf(pt_d2f(d[i]), P.gsxf[i], O.off[i]);
+            const float cf = floorf(rel);
+            xd[i] = rel - cf;
+            const int32_t ci = O.cell[i] + (int32_t)cf;
+            int32_t li;
+            if (P.dm_mask[i]) {
+                li = ci & P.dm_mask[i];
+            } else {
+                li = ci % P.dm[i];
+                if (li < 0) li += P.dm[i];
+            }
+            l[i] = li;
+            r[i] = (li + 1 == P.dm[i]) ? 0 : li + 1;
+            xu[i] = 1.0f - xd[i];
+        }
+        const float puu = xu[0] * xu[1], pud = xu[0] * xd[1];
+        const float pdu = xd[0] * xu[1], pdd = xd[0] * xd[1];
+        const float w8[8] = { puu * xu[2], puu * xd[2], pud * xu[2], pud * xd[2],
+                              pdu * xu[2], pdu * xd[2], pdd * xu[2], pdd * xd[2] };
+        const int64_t d1 = P.dm[0], d12 = (int64_t)P.dm[0] * P.dm[1];
+        const int64_t yl = d1 * l[1], yr = d1 * r[1], zl = d12 * l[2], zr = d12 * r[2];
+        const int64_t node[8] = { l[0] + yl + zl, l[0] + yl + zr, l[0] + yr + zl, l[0] + yr + zr,
+                                  r[0] + yl + zl, r[0] + yl + zr, r[0] + yr + zl, r[0] + yr + zr };
+        float acc[NV];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            float v[NC];
+            load_rec32<NC>(P.fld32, node[q], v);
+#pragma unroll
+            for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * v[cc] : fmaf(w8[q], v[cc], acc[cc]);
+        }
+        const float ux = pt_d2f(s[3]), uy = pt_d2f(s[4]), uz = pt_d2f(s[5]);
+        const float g = sqrtf(fmaf(ux, ux, fmaf(uy, uy, fmaf(uz, uz, 1.0f))));
+        const float ig = 1.0f / g;
+        const float v0 = ux * ig, v1 = uy * ig, v2 = uz * ig;
+        const float w0 = v0 - acc[0], w1 = v1 - acc[1], w2 = v2 - acc[2];
+        a[0] = pt_f2d(v0 * P.ivunf);
+        a[1] = pt_f2d(v1 * P.ivunf);
+        a[2] = pt_f2d(v2 * P.ivunf);
+        float f3 = w1 * acc[5] - w2 * acc[4];
+        float f4 = w2 * acc[3] - w0 * acc[5];
+        float f5 = w0 * acc[4] - w1 * acc[3];
+        if (NC == 12) {
+            f3 = fmaf(P.etaf, acc[6 % NV], f3);
+            f4 = fmaf(P.etaf, acc[7 % NV], f4);
+            f5 = fmaf(P.etaf, acc[8 % NV], f5);
+        }
+        a[3] = pt_f2d(P.qomf * f3);
+        a[4] = pt_f2d(P.qomf * f4);
+        a[5] = pt_f2d(P.qomf * f5);
+    }
+};
+
+template <int METHOD, int NC>
+__global__ void __launch_bounds__(PT_BLOCK, 3) k_integrate_mixed(const PtRun P)
+{
+    pt_sm::run_machine<METHOD, EvalF32<NC>>(P);
+}
+
+template <int NC>
+__global__ void k_accel_mixed(const PtRun P, int64_t n, const double *vec, double *acc)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double s[6], a[6];
+        const double d[6] = { 0, 0, 0, 0, 0, 0 };
+#pragma unroll
+        for (int c = 0; c < 6; ++c) s[c] = vec[6 * i + c];
+        typename EvalF32<NC>::Origin o;
+        EvalF32<NC>::begin(P, s, o);
+        EvalF32<NC>::f(P, s, d, o, a);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc[6 * i + c] = a[c];
+    }
+}
+
+template <int METHOD, int NC>
+cudaError_t launch(const PtRun &P, cudaStream_t s)
+{
+    if (P.np <= 0) return cudaSuccess;
+    auto kern = k_integrate_mixed<METHOD, NC>;
+    const int smem = pt_sm::Traits<METHOD>::ROWS * 6 * (int)sizeof(double) * PT_BLOCK;
+    static bool configured = false;
+    static int per_sm = 1, sms = 1;
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PT_BLOCK, smem);
+        if (per_sm < 1) per_sm = 1;
+        configured = true;
+    }
+    int64_t grid = (int64_t)sms * per_sm;
+    const int64_t need = (P.np + PT_BLOCK - 1) / PT_BLOCK;
+    if (need < grid) grid = need;
+    kern<<<(int)(grid < 1 ? 1 : grid), PT_BLOCK, smem, s>>>(P);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t pt_launch_rk5_mixed(const PtRun &P, int nc, cudaStream_t s)
+{
+    return nc == 12 ? launch<PT_METHOD_RK5, 12>(P, s) : launch<PT_METHOD_RK5, 8>(P, s);
+}
+
+cudaError_t pt_launch_dp853_mixed(const PtRun &P, int nc, cudaStream_t s)
+{
+    return nc == 12 ? launch<PT_METHOD_DOP853, 12>(P, s) : launch<PT_METHOD_DOP853, 8>(P, s);
+}
+
+cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int64_t n, const double *vec,
+                                  double *acc, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const int grid = (int)((n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096);
+    if (nc == 12) k_accel_mixed<12><<<grid, 128, 0, s>>>(P, n, vec, acc);
+    else k_accel_mixed<8><<<grid, 128, 0, s>>>(P, n, vec, acc);
+    return cudaGetLastError();
+}

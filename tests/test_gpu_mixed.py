@@ -1,0 +1,130 @@
+"""Mixed precision (PT_PREC_FP32): FP32 field records, gather and force; FP64
+stage sums, error norm, controller and state.  Checked against the FP64
+oracle with stated tolerances."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import small_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def _accel_on_device(torch, f, prm, vec):
+    from particles_gb300 import _native as N
+    dv = torch.tensor(vec.ravel(), device="cuda")
+    da = torch.empty_like(dv)
+    N.check(N.load().pt_debug_accel(f.handle, vec.shape[0], prm.ctypes.data_as(C.c_void_p),
+                                    C.c_void_p(dv.data_ptr()), C.c_void_p(da.data_ptr()), None),
+            "pt_debug_accel")
+    torch.cuda.synchronize()
+    return da.cpu().numpy().reshape(-1, 6)
+
+
+def test_fp32_force_within_single_precision(cuda, oracle_lib):
+    """The FP32 gather + force agrees with the FP64 oracle to a few FP32 ulp of
+    the force scale, including far from the origin and across the periodic seam."""
+    torch = cuda
+    import oracle
+    from particles_gb300 import Fields, fields, params
+    uu, bb = fields.snapshot(24, db_rms=0.8, v_rms=0.2, seed=7)
+    prm = params.pack_params(qom=200.0, vunit=0.05, tmax=1.0)
+    rng = np.random.default_rng(3)
+    pos = np.concatenate([rng.uniform(0, 1, (400, 3)), rng.uniform(-50, 80, (200, 3)),
+                          np.array([[1 - 1e-12, 0.5, 0.5], [-1e-18, 0.25, 0.75]])])
+    mom = rng.normal(0, 2, (pos.shape[0], 3)) * 10.0 ** rng.uniform(-2, 2.5, (pos.shape[0], 1))
+    vec = np.concatenate([pos, mom], 1)
+    f = Fields(uu, bb, precision="fp32")
+    got = _accel_on_device(torch, f, prm, vec)
+    ref = np.stack([oracle.acceleration(200.0, 0.05, uu, bb, v) for v in vec])
+    # dx/dt: |v|/vun <= 20; du/dt: qom |w x B| ~ 200 * 2 * 2
+    assert np.abs(got[:, :3] - ref[:, :3]).max() < 20.0 * 4e-7
+    scale = np.abs(ref[:, 3:]).max(axis=1, keepdims=True) + 1.0
+    assert (np.abs(got[:, 3:] - ref[:, 3:]) / scale).max() < 4e-6
+
+
+def _fixed_step_case(uu, bb, method, nsteps_per_period, periods, npart=64, seed=9):
+    """dt pinned by dtmax and a tolerance of 1 accepts every step, so the FP64
+    oracle and the mixed kernel take the same steps at the same times and
+    differ by rounding alone."""
+    from particles_gb300 import initial, params
+    T0 = 2.0 * np.pi / 200.0
+    tmax = periods * T0
+    prm = params.pack_params(qom=200.0, vunit=0.05, tmax=tmax, dtmax=T0 / nsteps_per_period,
+                             atol=1.0, rtol=1.0)
+    tg = params.time_grid(int(round(periods)) * 4, tmax)
+    st = np.zeros((npart, tg.size, 8))
+    st[:, 0, :6] = initial.isotropic_state(npart, seed, speed=0.5)
+    return prm, tg, st
+
+
+@pytest.mark.parametrize("method", ["rk5", "dop853"])
+def test_mixed_fixed_steps_uniform_field(cuda, oracle_lib, method):
+    """Gyration + E x B drift with identical steps: the mixed kernel follows
+    the FP64 oracle to FP32 accuracy (energy and position) over 10 periods."""
+    import oracle
+    from particles_gb300 import fields, integrate
+    uu, bb = fields.uniform_field(8, b=(0.3, 0.2, 1.0), u=(0.004, -0.002, 0.001))
+    prm, tg, st = _fixed_step_case(uu, bb, method, 100, 10.0)
+    so, co, _ = oracle.integrate(method, prm, tg, uu, bb, st.copy())
+    sg, cg, stg = integrate(method, prm, tg, uu, bb, st.copy(), precision="fp32")
+    assert (stg == 0).all() and np.array_equal(co, cg)
+    gam_rel = np.abs(sg[:, :, 6] - so[:, :, 6]) / so[:, :, 6]
+    assert gam_rel.max() < 1e-6
+    assert np.abs(sg[:, :, :3] - so[:, :, :3]).max() < 1e-5
+
+
+def test_mixed_fixed_steps_turbulent_field(cuda, oracle_lib):
+    """Turbulent trilinear field, identical steps, one gyro-period: energy
+    and position stay within FP32-level error of the FP64 oracle."""
+    import oracle
+    from particles_gb300 import fields, integrate
+    uu, bb = fields.snapshot(24, db_rms=0.5, v_rms=0.1, seed=13)
+    prm, tg, st = _fixed_step_case(uu, bb, "rk5", 200, 1.0, npart=128, seed=13)
+    so, co, _ = oracle.integrate("rk5", prm, tg, uu, bb, st.copy())
+    sg, cg, stg = integrate("rk5", prm, tg, uu, bb, st.copy(), precision="fp32")
+    assert (stg == 0).all() and np.array_equal(co, cg)
+    gam_rel = np.abs(sg[:, -1, 6] - so[:, -1, 6]) / so[:, -1, 6]
+    assert np.median(gam_rel) < 1e-6 and gam_rel.max() < 1e-5
+    assert np.median(np.abs(sg[:, -1, :3] - so[:, -1, :3])) < 1e-5
+
+
+@pytest.mark.parametrize("method", ["rk5", "dop853"])
+def test_mixed_turbulent_statistics(cuda, oracle_lib, method):
+    """Adaptive steps in a turbulent trilinear field: FP32 rounding picks
+    another valid step sequence (about half of all attempts sit near the
+    accept/reject threshold at cell faces), so trajectories separate like any
+    two roundings do.  Ensemble energy and step statistics must still agree.
+    DOP853 runs at rtol = 1e-7: FP32 noise in the stages floors its error
+    estimate, so tighter tolerances only shrink the steps."""
+    prob = small_problem(method, n=24, npart=128, periods=2.0, seed=13,
+                         tol=1e-8 if method == "rk5" else 1e-7)
+    import oracle
+    from particles_gb300 import integrate
+    uu, bb = prob["fields"]
+    so, co, _ = oracle.integrate(method, prob["params"], prob["time"], uu, bb, prob["state"].copy())
+    sg, cg, stg = integrate(method, prob["params"], prob["time"], uu, bb, prob["state"].copy(),
+                            precision="fp32")
+    assert (stg == 0).all()
+    g_o, g_g = so[:, -1, 6], sg[:, -1, 6]
+    rel = np.abs(g_g - g_o) / g_o
+    assert np.median(rel) < 1e-4 and rel.max() < 2e-3
+    assert abs(g_g.mean() / g_o.mean() - 1.0) < 2e-5
+    assert 0.9 < cg[:, 1].sum() / co[:, 1].sum() < 1.3
+
+
+def test_mixed_windowed_resume_matches_single_run(cuda):
+    """Windows with the carry reproduce the uninterrupted mixed run bit for bit."""
+    from particles_gb300 import Fields, carry_buffer
+    prob = small_problem("rk5", n=16, npart=64, periods=1.5, seed=17)
+    uu, bb = prob["fields"]
+    T0 = 2.0 * np.pi / 200.0
+    f = Fields(uu, bb, precision="fp32")
+    full = f.integrate("rk5", prob["params"], prob["time"], prob["state"].copy())
+    s = prob["state"].copy()
+    c = np.zeros((s.shape[0], 3), np.int64)
+    carry = carry_buffer(s.shape[0])
+    for w in (0.3, 0.8, 0.0):
+        f.integrate("rk5", prob["params"], prob["time"], s, c, carry=carry, t_stop=w * T0)
+    assert np.array_equal(full[0], s) and np.array_equal(full[1], c)
