@@ -81,6 +81,12 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision leg")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-controller leg")
+    ap.add_argument("--no-order", action="store_true",
+                    help="keep the natural queue order (default: longest first)")
+    ap.add_argument("--records", type=int, default=10_000_000)
+    ap.add_argument("--legs", default="headline,mixed,learned",
+                    help="comma list of legs to run (headline always prints the line)")
     ap.add_argument("--mixed-steps", type=int, default=5)
     ap.add_argument("--accuracy-particles", type=int, default=32768)
     ap.add_argument("--accuracy-seconds", type=float, default=40.0)
@@ -274,6 +280,51 @@ def workload_config(cfg, npart, window, args):
     }
 
 
+def stopped_particles(f, d_status, where):
+    """Particles that ended with a negative status (reported, not fatal).
+
+    The reference's trilinear gather computes the right-hand node from
+    x + 1/dm separately from the left one (interpolations.F90:141-146); one
+    ulp below some cell faces the two skip a node, so the interpolated field
+    jumps there, adaptive steps shrink without bound and the reference loops
+    forever (integrations.F90:361).  The exact kernel reproduces that
+    arithmetic and stops such a particle with DT_UNDERFLOW."""
+    from particles_gb300 import _native as N
+    rc = f.run_check()
+    if rc not in (N.PT_OK, N.PT_ERR_PARTICLE):
+        raise RuntimeError(f"{where} failed: {N.last_error()}")
+    st = d_status.cpu().numpy()
+    names = {-2: "STEP_LIMIT", -3: "DT_UNDERFLOW", -4: "NONFINITE", -5: "TIMEOUT"}
+    out = {}
+    for code, name in names.items():
+        k = int((st == code).sum())
+        if k:
+            out[name] = k
+    return out
+
+
+class QueueOrder:
+    """Longest-first queue order for the persistent kernel: particles sorted
+    by the attempts they needed in the previous window, so the slowest ones
+    start first and the end-of-window tail stays short.  The order changes
+    which lane takes which particle, never a particle's result."""
+
+    def __init__(self, torch, d_cnt, enabled=True):
+        self.torch, self.cnt, self.enabled = torch, d_cnt, enabled
+        self.prev = None
+        self.order = None
+
+    def before(self):
+        if self.enabled:
+            self.prev = self.cnt[:, 0].clone()
+        return self.order
+
+    def after(self):
+        if self.enabled:
+            work = self.cnt[:, 0] - self.prev
+            self.order = self.torch.argsort(work, descending=True).to(self.torch.int32)
+
+
 def ks_distance(a, b):
     """Two-sample Kolmogorov-Smirnov statistic."""
     a, b = np.sort(np.asarray(a)), np.sort(np.asarray(b))
@@ -319,37 +370,67 @@ def mixed_leg(args, dev, stream):
                 torch.zeros(int(handles["fp64"]._L.pt_carry_bytes(n)), dtype=torch.uint8,
                             device=dev))
 
+    from particles_gb300 import learned as LRN
     rates = {}
-    for prec, f in handles.items():
+    model = None
+    for name, prec in (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"),
+                       ("fp32_learned", "fp32")):
+        f = handles[prec]
+        mdl = model if name == "fp32_learned" else None
         st, cnt, status, carry = fresh(npart)
+        ordq = QueueOrder(torch, cnt, enabled=not args.no_order)
         w = 0
         for _ in range(args.warmup):
             w += 1
+            o = ordq.before()
             f.run_device("rk5", prm, d_time, st, cnt, status, carry, t_stop=w * window * T0,
-                         time_budget_s=900.0, stream=stream.cuda_stream)
+                         time_budget_s=900.0, stream=stream.cuda_stream, order=o, model=mdl)
+            ordq.after()
         stream.synchronize()
         c0 = cnt.sum(0).cpu().numpy()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(args.mixed_steps):
             w += 1
+            o = ordq.before()
             f.run_device("rk5", prm, d_time, st, cnt, status, carry, t_stop=w * window * T0,
-                         time_budget_s=900.0, stream=stream.cuda_stream)
+                         time_budget_s=900.0, stream=stream.cuda_stream, order=o, model=mdl)
+            ordq.after()
         e1.record(stream)
         stream.synchronize()
-        if f.run_check() != 0:
-            raise RuntimeError(f"mixed leg {prec} failed")
+        stopped = stopped_particles(f, status, f"mixed leg {name}")
         d = cnt.sum(0).cpu().numpy() - c0
         sec = e0.elapsed_time(e1) * 1e-3
-        rates[prec] = {"value": float(d[1]) / sec, "attempts_per_s": float(d[0]) / sec,
+        rates[name] = {"value": float(d[1]) / sec, "attempts_per_s": float(d[0]) / sec,
                        "rejected_fraction": float(d[2] / max(d[0], 1)),
-                       "ms_per_step": 1e3 * sec / args.mixed_steps}
+                       "ms_per_step": 1e3 * sec / args.mixed_steps,
+                       "particle_gyroperiods_per_s": npart * window * args.mixed_steps / sec,
+                       "stopped_particles": stopped}
+        if name == "fp64":
+            # the plain integrator writes the learned controller's training records
+            rec = LRN.record_buffer(torch, min(args.records, 4_000_000))
+            w += 1
+            f.run_device("rk5", prm, d_time, st, cnt, status, carry, t_stop=w * window * T0,
+                         time_budget_s=900.0, stream=stream.cuda_stream, records=rec)
+            stream.synchronize()
+            X, T = LRN.dataset(LRN.records_from_buffer(rec), "rk5")
+            norm = LRN.normalisation(X, T)
+            params_mlp, hist = LRN.train(torch, X, T, norm, epochs=2, batch=16384, lr=2e-3)
+            model = LRN.Model(params_mlp, norm, safety=0.9)
+            out["learned_training"] = {"records": int(X.shape[0]), "mse_per_epoch": hist}
+            del rec
         del st, cnt, status, carry
         torch.cuda.empty_cache()
+    if model is not None:
+        model.close()
     out["accepted_steps_per_s"] = {k: v["value"] for k, v in rates.items()}
     out["detail"] = rates
     out["mixed_over_plain_exact"] = rates["fp32"]["value"] / rates["fp64"]["value"]
     out["mixed_over_plain_fma"] = rates["fp32"]["value"] / rates["fp64_fma"]["value"]
+    out["mixed_learned_over_plain_exact"] = rates["fp32_learned"]["value"] / rates["fp64"]["value"]
+    out["physics_rate_mixed_learned_over_plain_exact"] = (
+        rates["fp32_learned"]["particle_gyroperiods_per_s"]
+        / rates["fp64"]["particle_gyroperiods_per_s"])
 
     # accuracy: a seeded subsample integrated as far as the time budget allows
     na = min(args.accuracy_particles, npart)
@@ -368,6 +449,9 @@ def mixed_leg(args, dev, stream):
                 break
         res[prec] = (st.cpu().numpy(), w)
     nrow = min(res["fp64"][1], res["fp32"][1])        # sample index reached by both
+    e1 = res["fp64"][0][:, 1, 6]
+    m1 = res["fp32"][0][:, 1, 6]
+    g1 = np.abs(m1 - e1) / e1
     se, sm = res["fp64"][0][:, nrow], res["fp32"][0][:, nrow]
     g_rel = np.abs(sm[:, 6] - se[:, 6]) / se[:, 6]
     dpos = np.linalg.norm(sm[:, :3] - se[:, :3], axis=1)
@@ -381,9 +465,119 @@ def mixed_leg(args, dev, stream):
         "position_err_median": float(np.median(dpos)),
         "position_err_p90": float(np.percentile(dpos, 90)),
         "ks_gamma": ks_distance(se[:, 6], sm[:, 6]),
+        "energy_rel_err_at_1_gyroperiod_median": float(np.median(g1)),
+        "energy_rel_err_at_1_gyroperiod_p90": float(np.percentile(g1, 90)),
+        "note": "adaptive steps in a trilinear field: trajectories of two roundings separate "
+                "chaotically, so per-particle errors at late times measure chaos; the ensemble "
+                "(mean energy, KS distance) measures precision",
     }
     for f in handles.values():
         f.close()
+    return out
+
+
+def learned_leg(args, dev, stream):
+    """Configuration 5: a controller trained on accepted-step records of the
+    plain integrator on the configuration-2 shape with field seed 10, then
+    evaluated with field seed 11, 2^20 particles, DOP853 rtol 1e-10 (exact
+    FP64): rejected fraction, attempts/s, accepted steps/s and simulated
+    particle-time per second against the classical controller."""
+    import torch
+    from particles_gb300 import Fields, fields, initial, learned, params
+    cfg = WORKLOADS["dop853-256"]
+    npart, window = cfg["npart"], cfg["window"]
+    tmax = cfg["periods"] * T0
+    prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=tmax, atol=cfg["tol"],
+                             rtol=cfg["tol"], facmin=0.333, facmax=6.0, safe=0.9, beta=0.0)
+    tg = params.time_grid(cfg["periods"], tmax)
+    d_time = torch.tensor(tg, device=dev)
+    L = None
+
+    def setup(seed):
+        uu, bb, jj = fields.snapshot(cfg["n"], db_rms=cfg["db_rms"], v_rms=cfg["v_rms"],
+                                     vunit=VUN, spectrum=cfg["spectrum"], nmin=1.0,
+                                     nmax=cfg["nmax"], seed=seed, with_j=True, backend="torch")
+        f = Fields(uu, bb, jj, stream=stream.cuda_stream)
+        del uu, bb, jj
+        torch.cuda.empty_cache()
+        s0 = initial.isotropic_state(npart, seed, gamma_range=cfg["gamma"])
+        st = torch.zeros((npart, tg.size, 8), dtype=torch.float64, device=dev)
+        st[:, 0, :6] = torch.tensor(s0, device=dev)
+        cnt = torch.zeros((npart, 3), dtype=torch.int64, device=dev)
+        status = torch.zeros(npart, dtype=torch.int32, device=dev)
+        carry = torch.zeros(int(f._L.pt_carry_bytes(npart)), dtype=torch.uint8, device=dev)
+        return f, st, cnt, status, carry
+
+    # records from the classical run, field seed 10
+    f, st, cnt, status, carry = setup(10)
+    rec = learned.record_buffer(torch, args.records)
+    t_rec = time.perf_counter()
+    w = 0
+    while True:
+        w += 1
+        f.run_device("dop853", prm, d_time, st, cnt, status, carry, eta=cfg["eta"],
+                     t_stop=w * 0.01 * T0, time_budget_s=900.0, stream=stream.cuda_stream,
+                     records=rec)
+        stream.synchronize()
+        n_rec = int(rec[:2].cpu().numpy().view(np.uint64)[0])
+        if n_rec >= args.records or w >= 40:
+            break
+    records = learned.records_from_buffer(rec)
+    t_rec = time.perf_counter() - t_rec
+    del rec, st, cnt, status, carry
+    f.close()
+    torch.cuda.empty_cache()
+    X, T = learned.dataset(records, "dop853")
+    norm = learned.normalisation(X, T)
+    t_tr = time.perf_counter()
+    p, hist = learned.train(torch, X, T, norm, epochs=2, batch=16384, lr=2e-3)
+    t_tr = time.perf_counter() - t_tr
+    model = learned.Model(p, norm, safety=0.9)
+    out = {"workload": "dop853-256, field seed 11 (trained on seed 10)",
+           "records": int(X.shape[0]), "record_seconds": t_rec, "train_seconds": t_tr,
+           "mse_per_epoch": hist, "target": "accepted log dt + at most log 2 of error headroom",
+           "safety": 0.9}
+    f, st, cnt, status, carry = setup(11)
+    snap = (st.clone(), cnt.clone(), carry.clone())
+    for name, mdl in (("classical", None), ("learned", model)):
+        st.copy_(snap[0]); cnt.copy_(snap[1]); carry.copy_(snap[2])
+        ordq = QueueOrder(torch, cnt, enabled=not args.no_order)
+        w = 0
+        for _ in range(args.warmup):
+            w += 1
+            o = ordq.before()
+            f.run_device("dop853", prm, d_time, st, cnt, status, carry, eta=cfg["eta"],
+                         t_stop=w * window * T0, time_budget_s=900.0,
+                         stream=stream.cuda_stream, order=o, model=mdl)
+            ordq.after()
+        stream.synchronize()
+        c0 = cnt.sum(0).cpu().numpy()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            w += 1
+            o = ordq.before()
+            f.run_device("dop853", prm, d_time, st, cnt, status, carry, eta=cfg["eta"],
+                         t_stop=w * window * T0, time_budget_s=900.0,
+                         stream=stream.cuda_stream, order=o, model=mdl)
+            ordq.after()
+        e1.record(stream)
+        stream.synchronize()
+        stopped = stopped_particles(f, status, f"learned leg {name}")
+        d = cnt.sum(0).cpu().numpy() - c0
+        sec = e0.elapsed_time(e1) * 1e-3
+        out[name] = {"accepted_steps_per_s": float(d[1]) / sec,
+                     "attempts_per_s": float(d[0]) / sec,
+                     "rejected_fraction": float(d[2] / max(d[0], 1)),
+                     "attempts": int(d[0]), "accepted": int(d[1]),
+                     "particle_gyroperiods_per_s": npart * window * args.steps / sec,
+                     "stopped_particles": stopped}
+    model.close()
+    f.close()
+    c, l = out["classical"], out["learned"]
+    out["accepted_steps_per_s_ratio"] = l["accepted_steps_per_s"] / c["accepted_steps_per_s"]
+    out["physics_rate_ratio"] = l["particle_gyroperiods_per_s"] / c["particle_gyroperiods_per_s"]
+    out["attempts_ratio"] = l["attempts"] / c["attempts"]
     return out
 
 
@@ -426,18 +620,21 @@ def main():
         d_carry = torch.zeros(int(L.pt_carry_bytes(npart)), dtype=torch.uint8, device=dev)
     stream.synchronize()
 
+    ordq = QueueOrder(torch, d_cnt, enabled=not args.no_order)
+
     def window_run(w):
+        order = ordq.before()
         f.run_device(cfg["method"], prm, d_time, d_state, d_cnt, d_status, d_carry,
                      eta=cfg["eta"], t_stop=w * window * T0, time_budget_s=900.0,
-                     stream=stream.cuda_stream)
+                     stream=stream.cuda_stream, order=order)
+        ordq.after()
 
     w = 0
     for _ in range(args.warmup):
         w += 1
         window_run(w)
     stream.synchronize()
-    if f.run_check() not in (N.PT_OK,):
-        raise RuntimeError(f"warm-up failed: {N.last_error()}")
+    stopped_particles(f, d_status, "warm-up")
     acc0 = d_cnt.sum(0).cpu().numpy()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
@@ -456,9 +653,7 @@ def main():
         wall = time.perf_counter() - t_start
     if world > 1:
         torch.distributed.barrier()
-    rc = f.run_check()
-    if rc != N.PT_OK:
-        raise RuntimeError(f"timed run failed: {N.last_error()}")
+    stopped = stopped_particles(f, d_status, "timed run")
     kern_ms = [a.elapsed_time(b) for a, b in ev]
     dev_s = sum(kern_ms) * 1e-3
     c_now = d_cnt.cpu().numpy()
@@ -496,7 +691,7 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded fields and particles)",
         "config": workload_config(cfg, npart, window, args),
-        "wall_s_timed": wall, "gpu_launches": args.steps,
+        "wall_s_timed": wall, "gpu_launches": args.steps, "stopped_particles": stopped,
         "rejected_fraction": float(dcnt_tot[2] / max(dcnt_tot[0], 1)),
         "attempts_per_s": float(dcnt_tot[0]) / elapsed,
         "roofline": roof, "clocks": clocks.summary(),
@@ -539,11 +734,15 @@ def main():
     if not args.no_cpu and rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline(cfg, prm, tg, out, s0, window, args.warmup,
                                             args.steps, args.cpu_seconds)
-    if not args.no_mixed and rank == 0 and args.workload == "dop853-256":
+    legs = set(args.legs.split(","))
+    if not args.no_mixed and "mixed" in legs and rank == 0 and args.workload == "dop853-256":
         f.close()
         del d_state, d_cnt, d_status, d_carry
         torch.cuda.empty_cache()
         line["mixed"] = mixed_leg(args, dev, stream)
+    if not args.no_learned and "learned" in legs and rank == 0 and args.workload == "dop853-256":
+        torch.cuda.empty_cache()
+        line["learned"] = learned_leg(args, dev, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -83,8 +83,15 @@ typedef struct pt_options {
     int32_t      *status;         /* host: np per-particle PT_ST_* words, or NULL */
     void         *carry;          /* host: pt_carry_bytes(np) bytes of controller memory
                                      for resumable windows (zero-filled = fresh), or NULL */
-    const void   *model;          /* learned-controller weights (pt_mlp_*), or NULL */
-    int64_t       reserved[4];
+    const void   *model;          /* learned controller (a pt_mlp from pt_mlp_create) used
+                                     when controller == 1 */
+    void         *records;        /* device buffer for accepted-step records (pt_run_device
+                                     only): a 16-byte header whose first 8 bytes count the
+                                     records, then records of 10 floats each */
+    int64_t       record_capacity;/* records that fit after the header */
+    const int32_t *order;         /* device: particle index per queue slot, e.g. longest
+                                     first (pt_run_device only), or NULL */
+    int64_t       reserved[1];
 } pt_options;
 
 /* ---- one-shot, reference-shaped call ----------------------------------- */
@@ -140,6 +147,30 @@ int pt_run_device(int32_t method, int64_t np, int32_t m, const pt_fields *f,
 /* After synchronising the stream of the last pt_run_device on f: PT_OK,
  * PT_ERR_TIMEOUT or PT_ERR_CUDA. */
 int pt_run_check(const pt_fields *f);
+
+/* ---- learned step-size controller (no counterpart in the reference) ----- */
+
+/* MLP 8 -> 64 -> 64 -> 1 (SiLU) from eight local invariants at the start of
+ * an attempt (log|B|, log|E|, log gamma, pitch cosine, log(|grad B|/|B|),
+ * log(Omega dt_prev), log(err_prev), log dt_prev) to log(trial dt); inference
+ * on FP16 tensor cores inside the integrator.  The embedded error estimate
+ * still accepts or rejects every step and a rejection falls back to the
+ * classical controller.  params: PT_MLP_NPARAM floats (W1[8][64], b1[64],
+ * W2[64][64], b2[64], W3[64], b3); norm: feature means[8], standard
+ * deviations[8], target mean and standard deviation; safety multiplies the
+ * proposed step. */
+typedef struct pt_mlp pt_mlp;
+int32_t pt_mlp_nparam(void);
+int pt_mlp_create(const float *params, const float norm[18], float safety, pt_mlp **out);
+int pt_mlp_destroy(pt_mlp *m);
+/* Tensor-core inference on n feature rows (device pointers), as in the integrator. */
+int pt_mlp_infer(const pt_mlp *m, const float *d_X, int64_t n, float *d_out, void *stream);
+/* Training: mean-squared-error loss and its gradient over n standardised rows
+ * (X n x 8, T n), and one Adam update (device pointers). */
+int pt_mlp_loss_grad(const float *d_params, const float *d_X, const float *d_T, int64_t n,
+                     float *d_grad, float *d_loss, void *stream);
+int pt_mlp_adam(float *d_params, const float *d_grad, float *d_m, float *d_v, int64_t step,
+                float lr, float beta1, float beta2, float eps, void *stream);
 
 /* ---- no device allocation ------------------------------------------------ */
 

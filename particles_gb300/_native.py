@@ -27,7 +27,8 @@ EXPORTS = [
     "pt_fields_destroy", "pt_fields_bytes", "pt_integrate_fields", "pt_carry_bytes",
     "pt_run_device", "pt_run_check", "pt_last_error", "pt_abi_version", "pt_tableau",
     "pt_debug_pow", "pt_debug_accel", "pt_probe_peak", "pt_debug_unpack", "pt_debug_echo",
-    "pt_integrate_device_noalloc",
+    "pt_integrate_device_noalloc", "pt_mlp_nparam", "pt_mlp_create", "pt_mlp_destroy",
+    "pt_mlp_infer", "pt_mlp_loss_grad", "pt_mlp_adam",
 ]
 
 
@@ -37,7 +38,8 @@ class PtOptions(C.Structure):
         ("controller", C.c_int32), ("max_steps", C.c_int64), ("eta", C.c_double),
         ("jj", C.c_void_p), ("t_stop", C.c_double), ("time_budget_s", C.c_double),
         ("status", C.c_void_p), ("carry", C.c_void_p), ("model", C.c_void_p),
-        ("reserved", C.c_int64 * 4),
+        ("records", C.c_void_p), ("record_capacity", C.c_int64), ("order", C.c_void_p),
+        ("reserved", C.c_int64 * 1),
     ]
 
 
@@ -85,6 +87,12 @@ def load():
     L.pt_debug_unpack.argtypes = [i32, i64, i32, vp, i32, i32, vp, vp, vp]
     L.pt_debug_echo.argtypes = [i32, i64, i32, vp, i32, i32, vp, vp, vp, vp]
     L.pt_integrate_device_noalloc.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.pt_mlp_nparam.restype = i32
+    L.pt_mlp_create.argtypes = [vp, vp, C.c_float, C.POINTER(vp)]
+    L.pt_mlp_destroy.argtypes = [vp]
+    L.pt_mlp_infer.argtypes = [vp, vp, i64, vp, vp]
+    L.pt_mlp_loss_grad.argtypes = [vp, vp, vp, i64, vp, vp, vp]
+    L.pt_mlp_adam.argtypes = [vp, vp, vp, vp, i64, C.c_float, C.c_float, C.c_float, C.c_float, vp]
     _lib = L
     return L
 

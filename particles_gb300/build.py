@@ -31,11 +31,12 @@ COMMON = [
 # (output object, source, extra flags)
 UNITS = [
     ("pt_api.o", "pt_api.cu", ["--fmad=false"]),
-    ("pt_fp64_exact.o", "pt_fp64.cu", ["--fmad=false", "-DPT_SFX=exact"]),
+    ("pt_fp64_exact.o", "pt_fp64.cu", ["--fmad=false", "-DPT_SFX=exact", "-DPT_EXACT"]),
     ("pt_fp64_fma.o", "pt_fp64.cu", ["--fmad=true", "-DPT_SFX=fma"]),
     ("pt_mixed.o", "pt_mixed.cu", ["--fmad=true"]),
     ("pt_probe.o", "pt_probe.cu", ["--fmad=true"]),
     ("pt_noalloc.o", "pt_noalloc.cu", ["--fmad=false"]),
+    ("pt_mlp_train.o", "pt_mlp_train.cu", ["--fmad=true"]),
 ]
 
 

@@ -20,6 +20,9 @@
 #include "pt_detmath.h"
 #include "pt_tableau.h"
 
+/* Device blob of a learned-controller model (pt_mlp_train.cu). */
+const unsigned char *pt_mlp_blob(const pt_mlp *m);
+
 /* ---------------------------------------------------------------------- */
 /* errors                                                                 */
 /* ---------------------------------------------------------------------- */
@@ -282,8 +285,12 @@ static int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
     if (opt) {
         if (opt->precision != g.precision)
             return set_err(PT_ERR_ARG, "options precision differs from the field handle%s");
-        if (opt->controller != 0)
-            return set_err(PT_ERR_UNSUPPORTED, "learned controller not available for this precision%s");
+        if (opt->controller != 0 && opt->controller != 1)
+            return set_err(PT_ERR_ARG, "unknown controller%s");
+        if (opt->controller == 1 && !opt->model)
+            return set_err(PT_ERR_ARG, "controller 1 needs opt->model%s");
+        if (opt->records && opt->record_capacity < 0)
+            return set_err(PT_ERR_ARG, "negative record capacity%s");
         eta = opt->eta;
         t_stop = opt->t_stop;
         budget = opt->time_budget_s;
@@ -306,6 +313,12 @@ static int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
     R.budget_ns = (uint64_t)((budget > 0.0 ? budget : 600.0) * 1e9);
     R.m = m;
     R.np = np;
+    if (opt) {
+        R.mlp = (opt->controller == 1) ? pt_mlp_blob(static_cast<const pt_mlp *>(opt->model)) : nullptr;
+        R.rec = static_cast<float *>(opt->records);
+        R.rec_cap = opt->record_capacity;
+        R.order = opt->order;
+    }
     return PT_OK;
 }
 
@@ -451,6 +464,8 @@ extern "C" int pt_integrate_fields(int32_t method, int64_t np, int32_t m, const 
     const size_t cbytes = (size_t)3 * np * sizeof(int64_t);
     int32_t *h_status = opt ? opt->status : nullptr;
     void *h_carry = opt ? opt->carry : nullptr;
+    if (opt && (opt->records || opt->order))
+        return set_err(PT_ERR_UNSUPPORTED, "records and order are device-API options (pt_run_device)%s");
     cudaStream_t s = nullptr;
     PT_CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     PT_CU(cudaMalloc(&d_time, (size_t)m * sizeof(double)));

@@ -52,6 +52,9 @@ struct PtRun {
     int32_t *status;
     unsigned char *carry;  /* SoA carry or NULL */
     const int32_t *order;  /* queue order (particle index per queue slot) or NULL */
+    const unsigned char *mlp;  /* learned-controller weight blob or NULL */
+    float *rec;            /* accepted-step records (see PT_REC_*) or NULL */
+    int64_t rec_cap;       /* record capacity */
     unsigned long long *queue;  /* work-queue head */
     int32_t *flags;        /* [0] time budget hit, [1] particles with negative status */
 };
@@ -81,6 +84,13 @@ __host__ __device__ inline PtCarry pt_carry_view(unsigned char *base, int64_t np
 }
 
 #define PT_CARRY_BYTES_PER_PARTICLE 128
+
+/* Accepted-step record buffer: a 16-byte header whose first 8 bytes count
+ * the records written, then records of PT_REC_FLOATS floats: the eight
+ * controller features at the start of an accepted step, log(dt) and
+ * log(error ratio) of that step. */
+#define PT_REC_FLOATS 10
+#define PT_REC_HEADER_FLOATS 4
 
 /* Fortran MIN/MAX with the NaN rule of the oracle (a NaN first operand
  * propagates), and maxval with NaN propagation. */

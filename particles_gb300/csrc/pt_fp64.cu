@@ -62,6 +62,9 @@ __device__ __forceinline__ void load_rec(const double *__restrict__ fld, int64_t
 template <int NC>
 struct EvalF64 {
     static constexpr bool kDelta = false;
+    using Rec = double;
+    static constexpr int NCR = NC;
+    static __device__ __forceinline__ const double *records(const PtRun &P) { return P.fld; }
     struct Origin {};
     static __device__ __forceinline__ void begin(const PtRun &, const double *, Origin &) {}
     static __device__ __forceinline__ void f(const PtRun &P, const double s[6], const double *,
@@ -117,10 +120,10 @@ struct EvalF64 {
     }
 };
 
-template <int METHOD, int NC>
+template <int METHOD, int NC, bool LEARN>
 __global__ void __launch_bounds__(PT_BLOCK, 3) k_integrate(const PtRun P)
 {
-    pt_sm::run_machine<METHOD, EvalF64<NC>>(P);
+    pt_sm::run_machine<METHOD, EvalF64<NC>, LEARN>(P);
 }
 
 /* Standalone f(vec) for parity tests of the gather and force. */
@@ -152,29 +155,39 @@ __global__ void k_echo(const PtRun P, double *out)
     out[7] = (double)P.np;
 }
 
-template <int METHOD, int NC>
-cudaError_t launch(const PtRun &P, cudaStream_t s)
+template <int METHOD, int NC, bool LEARN>
+cudaError_t launch1(const PtRun &P, cudaStream_t s)
 {
-    if (P.np <= 0) return cudaSuccess;
-    auto kern = k_integrate<METHOD, NC>;
-    const int smem = pt_sm::Traits<METHOD>::ROWS * 6 * (int)sizeof(double) * PT_BLOCK;
-    static bool configured = false;
-    static int per_sm = 1, sms = 1;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    auto kern = k_integrate<METHOD, NC, LEARN>;
+    const int smem = pt_sm::smem_bytes<METHOD>(PT_BLOCK, LEARN && P.rec != nullptr);
+    /* occupancy per shared-memory size (recording runs add 4 KB per block) */
+    static int conf_smem[2] = { -1, -1 }, conf_per_sm[2] = { 1, 1 };
+    static int sms = 0;
+    const int slot = (LEARN && P.rec != nullptr) ? 1 : 0;
+    if (conf_smem[slot] != smem) {
+        const int full = pt_sm::smem_bytes<METHOD>(PT_BLOCK, true);
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, full);
         if (e != cudaSuccess) return e;
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PT_BLOCK, smem);
-        if (per_sm < 1) per_sm = 1;
-        configured = true;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&conf_per_sm[slot], kern, PT_BLOCK, smem);
+        if (conf_per_sm[slot] < 1) conf_per_sm[slot] = 1;
+        conf_smem[slot] = smem;
     }
+    const int per_sm = conf_per_sm[slot];
     int64_t grid = (int64_t)sms * per_sm;
     const int64_t need = (P.np + PT_BLOCK - 1) / PT_BLOCK;
     if (need < grid) grid = need;
     kern<<<(int)(grid < 1 ? 1 : grid), PT_BLOCK, smem, s>>>(P);
     return cudaGetLastError();
+}
+
+template <int METHOD, int NC>
+cudaError_t launch(const PtRun &P, cudaStream_t s)
+{
+    if (P.np <= 0) return cudaSuccess;
+    return (P.mlp || P.rec) ? launch1<METHOD, NC, true>(P, s) : launch1<METHOD, NC, false>(P, s);
 }
 
 }  // namespace

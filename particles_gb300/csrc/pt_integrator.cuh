@@ -41,6 +41,7 @@
 
 #include "pt_common.cuh"
 #include "pt_detmath.h"
+#include "pt_mlp.cuh"
 #include "pt_tableau.h"
 
 namespace pt_sm {
@@ -296,6 +297,24 @@ __device__ __forceinline__ void stage_state(int j, const KRows &K, const double 
     }
 }
 
+/* 1/x for the error norms of the non-exact variants: the hardware
+ * approximation (about 2^-23 relative) refined by one Newton step (about
+ * 2^-46), against ~8 FP64-pipe operations for an IEEE division.  The exact
+ * variant (PT_EXACT) keeps the reference's divisions. */
+__device__ __forceinline__ double pt_rcp(double x)
+{
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+}
+
+#ifdef PT_EXACT
+#define PT_DIV(a, b) ((a) / (b))
+#else
+#define PT_DIV(a, b) ((a) * pt_rcp(b))
+#endif
+
 /* Final combination and error norm: sf and the scaled error (DOP853 err,
  * RK5 del).  Row 3 receives the 8th-order increment as in :418. */
 template <int METHOD>
@@ -315,19 +334,27 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
             sr[c] = P.atol + P.rtol * pt_max(fabs(si[c]), fabs(sf[c]));
         }
         double err3 = 0.0, err5 = 0.0;                          /* :426-437 */
+#ifndef PT_EXACT
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sr[c] = pt_rcp(sr[c]);     /* now 1/sr */
+#define PT_OVER_SR(e, c) ((e) * sr[c])
+#else
+#define PT_OVER_SR(e, c) ((e) / sr[c])
+#endif
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
             const double e = K(3, c) - BH1 * K(0, c) - BH2 * K(8, c) - BH3 * K(2, c);
-            const double q = e / sr[c];
+            const double q = PT_OVER_SR(e, c);
             err3 = err3 + q * q;
         }
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
             const double e = ER01 * K(0, c) + ER06 * K(5, c) + ER07 * K(6, c) + ER08 * K(7, c)
                            + ER09 * K(8, c) + ER10 * K(9, c) + ER11 * K(1, c) + ER12 * K(2, c);
-            const double q = e / sr[c];
+            const double q = PT_OVER_SR(e, c);
             err5 = err5 + q * q;
         }
+#undef PT_OVER_SR
         const double deno = err5 + 1.0e-02 * err3;
         return (deno <= 0.0) ? fabs(dt) * err5 / sqrt(6.0) : fabs(dt) * err5 / sqrt(6.0 * deno);
     } else {                                                    /* :140-148 */
@@ -342,21 +369,38 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
             dsf[c] = a;
             sf[c] = si[c] + a;
             const double sr = fabs(si[c]) + fabs(K(0, c)) + 2.2250738585072014e-308;
-            const double q = fabs(e / sr);
+            const double q = fabs(PT_DIV(e, sr));
             del = (c == 0) ? q : pt_nanmax(del, q);
         }
-        return del / P.atol;
+        return PT_DIV(del, P.atol);
     }
 }
 
 /* ---- the kernel ---------------------------------------------------------- */
 
-template <int METHOD, class EV>
+/* Dynamic shared memory of one block: the k rows, then (when recording
+ * accepted steps) eight pending feature floats per lane. */
+template <int METHOD>
+__host__ __device__ constexpr int smem_bytes(int block, bool record)
+{
+    return Traits<METHOD>::ROWS * 6 * 8 * block + (record ? 8 * 4 * block : 0);
+}
+
+template <int METHOD, class EV, bool LEARN>
 __device__ __forceinline__ void run_machine(const PtRun &P)
 {
     using T = Traits<METHOD>;
     extern __shared__ double pt_ksm[];
     const KRows K{ pt_ksm + threadIdx.x, (int)blockDim.x };
+    unsigned char *const smem_tail =
+        reinterpret_cast<unsigned char *>(pt_ksm) + T::ROWS * 6 * 8 * blockDim.x;
+    PtMlpSmem M{};
+    float *pend = nullptr;                 /* pending features, [8][blockDim] */
+    bool have_pend = false;
+    if (LEARN) {
+        if (P.mlp) M = pt_mlp_view(P.mlp);
+        if (P.rec) pend = reinterpret_cast<float *>(smem_tail) + threadIdx.x;
+    }
     const uint64_t t_start = pt_globaltimer();
     const PtCarry C = P.carry ? pt_carry_view(P.carry, P.np) : PtCarry{};
     Lane L;
@@ -393,6 +437,7 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
                 if ((int64_t)qi < P.np) {
                     L.p = P.order ? (int64_t)P.order[qi] : (int64_t)qi;
                     const int how = lane_open<METHOD>(P, C, K, L, si);
+                    have_pend = false;
                     if (how == 2) {
                         mode = M_READY;
                     } else {
@@ -428,6 +473,7 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
             }
         } else {
             const double dt = L.dt;
+            const bool was_rejected = L.rejected;
             /* The controller's power of the error ratio, evaluated once for
              * accepted and rejected lanes together (converged): safe * q^y
              * with y = expo (DOP853, :466, :486) or -0.20 / -0.25 (RK5, :177,
@@ -485,6 +531,49 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
                 next_time(P, L);
             } else if (mode == M_READY) {
                 next_time(P, L);
+            }
+            if (LEARN) {
+                /* Features at the new si of an accepted step: the record of
+                 * the step that just completed pairs the features at its
+                 * start with its outcome; the MLP proposes the next trial
+                 * step (the error estimate still accepts or rejects it, and
+                 * a rejection falls back to the classical controller). */
+                const bool want = (mode == M_ACCEPT) && active;
+                float feat[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+                if (want) {
+                    pt_field_features<typename EV::Rec, EV::NCR>(P, EV::records(P), si, feat);
+                    const float om = P.qomf * __expf(feat[0] - feat[2]);     /* qom |B| / gamma */
+                    const float dtf = pt_d2f(dt);
+                    feat[5] = __logf(om * dtf + 1e-30f);
+                    feat[6] = __logf(pt_d2f(q) + 1e-30f);
+                    feat[7] = __logf(dtf);
+                    if (P.rec) {
+                        if (have_pend) {
+                            const unsigned long long i =
+                                atomicAdd(reinterpret_cast<unsigned long long *>(P.rec), 1ULL);
+                            if ((int64_t)i < P.rec_cap) {
+                                float *r = P.rec + PT_REC_HEADER_FLOATS + i * PT_REC_FLOATS;
+#pragma unroll
+                                for (int c = 0; c < 8; ++c) r[c] = pend[c * blockDim.x];
+                                r[8] = feat[7];
+                                r[9] = feat[6];
+                            }
+                        }
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) pend[c * blockDim.x] = feat[c];
+                        have_pend = true;
+                    }
+                }
+                if (P.mlp && __any_sync(0xffffffffu, want)) {
+                    const float y = pt_mlp_warp(M, feat);
+                    if (want) {
+                        const double lo = P.fcmn * dt;
+                        const double hi = (METHOD == PT_METHOD_DOP853 && was_rejected) ? dt : P.fcmx * dt;
+                        const double h = pt_f2d(__expf(y));
+                        L.dt = pt_min(pt_max(h, lo), hi);
+                        L.dt = pt_min(L.dt, P.dtm);
+                    }
+                }
             }
             /* ---- start of the next attempt ---- */
             if (active) {

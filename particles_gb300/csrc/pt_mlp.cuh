@@ -1,0 +1,245 @@
+/*
+ * pt_mlp.cuh -- the learned step-size controller inside the step machine.
+ *
+ * An MLP 8 -> 64 -> 64 -> 1 (SiLU) maps eight local invariants of a particle
+ * at the start of an attempt to log(trial step).  Inference runs on the
+ * tensor cores with warp-level mma.sync m16n8k16 (FP16 operands, FP32
+ * accumulate): the 32 lanes of a warp are the 32 rows of the activation
+ * matrix (two m16 tiles).  The layer-1 input K of 8 is zero-padded to 16, the
+ * layer-3 output N of 1 to 8.  A layer's FP32 accumulators convert in place
+ * into the next layer's FP16 A fragments (the C layout of two adjacent n8
+ * tiles is the A layout of one k16 tile), so only the input and the output
+ * cross lanes.
+ *
+ * Fragment layouts (PTX ISA, mma.m16n8k16 .f16): g = lane >> 2, q = lane & 3;
+ *   A (16x16): a0a1 = A[g][2q..2q+1], a2a3 = A[g+8][2q..], a4a5 = A[g][2q+8..],
+ *              a6a7 = A[g+8][2q+8..]
+ *   B (16x8):  b0b1 = B[2q..2q+1][g], b2b3 = B[2q+8..2q+9][g]
+ *   C (16x8):  c0c1 = C[g][2q..2q+1], c2c3 = C[g+8][2q..2q+1]
+ *
+ * Weight blob (pt_mlp_create, global memory, copied to shared memory by
+ * each block): B fragments pre-arranged per (k-tile, n-tile, lane) as uint2,
+ * then FP32 b1[64], b2[64], b3[4], the feature means mu[8] and inverse
+ * standard deviations isd[8].  Features are standardised in FP32 before the
+ * FP16 conversion; the target scaling and the safety factor are folded into
+ * W3 and b3 when the blob is built.
+ */
+#ifndef PT_MLP_CUH
+#define PT_MLP_CUH
+
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#define PT_MLP_NIN 8
+#define PT_MLP_NH 64
+/* uint2 fragments: W1 8 n-tiles, W2 4 k-tiles x 8 n-tiles, W3 4 k-tiles */
+#define PT_MLP_FRAG_W1 0
+#define PT_MLP_FRAG_W2 (8 * 32)
+#define PT_MLP_FRAG_W3 (PT_MLP_FRAG_W2 + 32 * 32)
+#define PT_MLP_NFRAG (PT_MLP_FRAG_W3 + 4 * 32)
+/* FP32 tail after the fragments: b1[64], b2[64], b3[4], mu[8], isd[8] */
+#define PT_MLP_BLOB_FLOATS (64 + 64 + 4 + 8 + 8)
+#define PT_MLP_BLOB_BYTES (PT_MLP_NFRAG * 8 + PT_MLP_BLOB_FLOATS * 4)
+
+struct PtMlpSmem {
+    const uint2 *frag;
+    const float *b1, *b2, *b3, *mu, *isd;
+};
+
+__device__ __forceinline__ uint32_t pt_pack_h2(float lo, float hi)
+{
+    const __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+__device__ __forceinline__ void pt_mma16816(float c[4], const uint32_t a[4], uint2 b)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
+        "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
+}
+
+__device__ __forceinline__ float pt_silu(float z) { return z / (1.0f + __expf(-z)); }
+
+/* Views of a blob; blob may be shared memory or global memory (the
+ * integrator reads it through L1, 11.9 KB, so the k rows keep all of the
+ * shared memory and the occupancy of the classical kernel). */
+__device__ __forceinline__ PtMlpSmem pt_mlp_view(const unsigned char *blob)
+{
+    PtMlpSmem m;
+    m.frag = reinterpret_cast<const uint2 *>(blob);
+    m.b1 = reinterpret_cast<const float *>(blob + PT_MLP_NFRAG * 8);
+    m.b2 = m.b1 + 64;
+    m.b3 = m.b2 + 64;
+    m.mu = m.b3 + 4;
+    m.isd = m.mu + 8;
+    return m;
+}
+
+/* Copies the blob into shared memory (whole block, before the main loop). */
+__device__ __forceinline__ PtMlpSmem pt_mlp_load(const unsigned char *blob, unsigned char *smem)
+{
+    const uint4 *src = reinterpret_cast<const uint4 *>(blob);
+    uint4 *dst = reinterpret_cast<uint4 *>(smem);
+    for (int i = threadIdx.x; i < PT_MLP_BLOB_BYTES / 16; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    PtMlpSmem m;
+    m.frag = reinterpret_cast<const uint2 *>(smem);
+    m.b1 = reinterpret_cast<const float *>(smem + PT_MLP_NFRAG * 8);
+    m.b2 = m.b1 + 64;
+    m.b3 = m.b2 + 64;
+    m.mu = m.b3 + 4;
+    m.isd = m.mu + 8;
+    return m;
+}
+
+/* y = MLP(x) for the 32 lanes of a converged warp; every lane passes its own
+ * eight raw features and receives its own output (log trial step). */
+__device__ __forceinline__ float pt_mlp_warp(const PtMlpSmem &M, const float x[8])
+{
+    const int lane = threadIdx.x & 31;
+    const int g = lane >> 2, q = lane & 3;
+    uint32_t xp[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        xp[i] = pt_pack_h2((x[2 * i] - M.mu[2 * i]) * M.isd[2 * i],
+                           (x[2 * i + 1] - M.mu[2 * i + 1]) * M.isd[2 * i + 1]);
+    float out = 0.0f;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
+        /* layer-1 A fragment: rows g and g + 8 of this m tile, columns 2q, 2q+1 */
+        uint32_t a1[4];
+        const int r0 = 16 * mt + g, r1 = r0 + 8;
+        uint32_t v0 = 0, v1 = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const uint32_t s0 = __shfl_sync(0xffffffffu, xp[i], r0);
+            const uint32_t s1 = __shfl_sync(0xffffffffu, xp[i], r1);
+            if (q == i) { v0 = s0; v1 = s1; }
+        }
+        a1[0] = v0; a1[1] = v1; a1[2] = 0u; a1[3] = 0u;
+        /* layer 1 -> SiLU -> layer-2 A fragments */
+        uint32_t a2[4][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            float c[4];
+            c[0] = c[2] = M.b1[8 * nt + 2 * q];
+            c[1] = c[3] = M.b1[8 * nt + 2 * q + 1];
+            pt_mma16816(c, a1, M.frag[PT_MLP_FRAG_W1 + nt * 32 + lane]);
+            const int kt = nt >> 1, hiw = (nt & 1) * 2;
+            a2[kt][hiw] = pt_pack_h2(pt_silu(c[0]), pt_silu(c[1]));
+            a2[kt][hiw + 1] = pt_pack_h2(pt_silu(c[2]), pt_silu(c[3]));
+        }
+        /* layer 2 -> SiLU -> layer-3 A fragments */
+        uint32_t a3[4][4];
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) {
+            float c[4];
+            c[0] = c[2] = M.b2[8 * nt + 2 * q];
+            c[1] = c[3] = M.b2[8 * nt + 2 * q + 1];
+#pragma unroll
+            for (int kt = 0; kt < 4; ++kt)
+                pt_mma16816(c, a2[kt], M.frag[PT_MLP_FRAG_W2 + (kt * 8 + nt) * 32 + lane]);
+            const int kt3 = nt >> 1, hiw = (nt & 1) * 2;
+            a3[kt3][hiw] = pt_pack_h2(pt_silu(c[0]), pt_silu(c[1]));
+            a3[kt3][hiw + 1] = pt_pack_h2(pt_silu(c[2]), pt_silu(c[3]));
+        }
+        /* layer 3: column 0 of the n8 tile is the output */
+        float c[4] = { M.b3[0], 0.0f, M.b3[0], 0.0f };
+#pragma unroll
+        for (int kt = 0; kt < 4; ++kt) pt_mma16816(c, a3[kt], M.frag[PT_MLP_FRAG_W3 + kt * 32 + lane]);
+        /* row r0 sits in c0 of lane 4g, row r1 in c2 of lane 4g (q == 0) */
+        const int r = lane - 16 * mt;
+        const int src = 4 * (r & 7);
+        const float y0 = __shfl_sync(0xffffffffu, c[0], src);
+        const float y1 = __shfl_sync(0xffffffffu, c[2], src);
+        if (r >= 0 && r < 16) out = (r < 8) ? y0 : y1;
+    }
+    return out;
+}
+
+/* ---- features ----------------------------------------------------------- */
+
+#include "pt_common.cuh"
+#include "pt_convert.cuh"
+
+__device__ __forceinline__ float pt_to_f(float v) { return v; }
+__device__ __forceinline__ float pt_to_f(double v) { return pt_d2f(v); }   /* integer pipe */
+
+/* The five field invariants of the learned controller at the particle state
+ * s, in FP32: log|B|, log|E|, log gamma, pitch cosine u.B/(|u||B|) and
+ * log(|grad B|/|B|), with E = -U x B + eta J and grad B the analytic
+ * derivative of the trilinear interpolant (the derivatives of the same eight
+ * corner weights).  REC/NCR: record type and width of the field records. */
+template <class REC, int NCR>
+__device__ __forceinline__ void pt_field_features(const PtRun &P, const REC *fld, const double s[6],
+                                                  float out[5])
+{
+    int32_t l[3], r[3];
+    float xd[3], xu[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double xn = fma(s[i], P.gsx[i], P.gox[i]);
+        const double fl = floor(xn);
+        xd[i] = pt_d2f(xn - fl);
+        const int32_t ci = (int32_t)fl;
+        int32_t li;
+        if (P.dm_mask[i]) {
+            li = ci & P.dm_mask[i];
+        } else {
+            li = ci % P.dm[i];
+            if (li < 0) li += P.dm[i];
+        }
+        l[i] = li;
+        r[i] = (li + 1 == P.dm[i]) ? 0 : li + 1;
+        xu[i] = 1.0f - xd[i];
+    }
+    const int64_t d1 = P.dm[0], d12 = (int64_t)P.dm[0] * P.dm[1];
+    float U[3] = { 0, 0, 0 }, B[3] = { 0, 0, 0 }, J[3] = { 0, 0, 0 };
+    float G[3][3] = { { 0, 0, 0 }, { 0, 0, 0 }, { 0, 0, 0 } };
+    constexpr bool HJ = (NCR >= 9);
+#pragma unroll
+    for (int qd = 0; qd < 8; ++qd) {
+        const int bx = (qd >> 2) & 1, by = (qd >> 1) & 1, bz = qd & 1;
+        const float wx = bx ? xd[0] : xu[0], wy = by ? xd[1] : xu[1], wz = bz ? xd[2] : xu[2];
+        const float w = wx * wy * wz;
+        const float gx = (bx ? 1.0f : -1.0f) * wy * wz * P.gsxf[0];
+        const float gy = (by ? 1.0f : -1.0f) * wx * wz * P.gsxf[1];
+        const float gz = (bz ? 1.0f : -1.0f) * wx * wy * P.gsxf[2];
+        const int64_t node = (bx ? r[0] : l[0]) + d1 * (by ? r[1] : l[1]) + d12 * (bz ? r[2] : l[2]);
+        const REC *v = fld + node * NCR;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float vu = pt_to_f(v[c]), vb = pt_to_f(v[3 + c]);
+            U[c] = fmaf(w, vu, U[c]);
+            B[c] = fmaf(w, vb, B[c]);
+            if (HJ) J[c] = fmaf(w, pt_to_f(v[6 + c]), J[c]);
+            G[c][0] = fmaf(gx, vb, G[c][0]);
+            G[c][1] = fmaf(gy, vb, G[c][1]);
+            G[c][2] = fmaf(gz, vb, G[c][2]);
+        }
+    }
+    const float eta = P.etaf;
+    const float E0 = -(U[1] * B[2] - U[2] * B[1]) + eta * J[0];
+    const float E1 = -(U[2] * B[0] - U[0] * B[2]) + eta * J[1];
+    const float E2 = -(U[0] * B[1] - U[1] * B[0]) + eta * J[2];
+    const float bm = sqrtf(B[0] * B[0] + B[1] * B[1] + B[2] * B[2]);
+    const float em = sqrtf(E0 * E0 + E1 * E1 + E2 * E2);
+    const float ux = pt_d2f(s[3]), uy = pt_d2f(s[4]), uz = pt_d2f(s[5]);
+    const float um = sqrtf(ux * ux + uy * uy + uz * uz);
+    const float gam = sqrtf(1.0f + um * um);
+    float gn = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) gn = fmaf(G[c][i], G[c][i], gn);
+    out[0] = __logf(bm + 1e-30f);
+    out[1] = __logf(em + 1e-30f);
+    out[2] = __logf(gam);
+    out[3] = (ux * B[0] + uy * B[1] + uz * B[2]) / (um * bm + 1e-30f);
+    out[4] = __logf(sqrtf(gn) / (bm + 1e-30f) + 1e-30f);
+}
+
+#endif /* PT_MLP_CUH */

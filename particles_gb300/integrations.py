@@ -28,12 +28,19 @@ def _f64(a):
 
 
 def _options(precision, *, eta=0.0, jj=None, open_x=False, max_steps=0, t_stop=0.0,
-             status=None, carry=None, time_budget_s=0.0):
+             status=None, carry=None, time_budget_s=0.0, model=None, records=None,
+             order=None):
     o = N.PtOptions()
     o.struct_size = C.sizeof(N.PtOptions)
     o.precision = N.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     o.open_x = int(bool(open_x))
-    o.controller = 0
+    o.controller = 1 if model is not None else 0
+    o.model = model.handle if model is not None else None
+    if records is not None:                       # device tensor (float32) with header
+        o.records = C.c_void_p(records.data_ptr())
+        o.record_capacity = (records.numel() - 4) // 10
+    if order is not None:                         # device int32 tensor
+        o.order = C.c_void_p(order.data_ptr())
     o.max_steps = int(max_steps)
     o.eta = float(eta)
     o.jj = _ptr(jj)
@@ -156,11 +163,16 @@ class Fields:
 
     def run_device(self, method, params, d_time, d_state, d_cnt, d_status=None, d_carry=None,
                    *, eta=0.0, open_x=False, max_steps=0, t_stop=0.0, time_budget_s=0.0,
-                   stream=0):
-        """Launch on device tensors (torch); returns without synchronising."""
+                   stream=0, model=None, records=None, order=None):
+        """Launch on device tensors (torch); returns without synchronising.
+
+        model: a learned.Model for the learned controller; records: a device
+        record buffer (learned.record_buffer); order: device int32 queue order.
+        """
         npart, m, _ = d_state.shape
         opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
-                       t_stop=t_stop, time_budget_s=time_budget_s)
+                       t_stop=t_stop, time_budget_s=time_budget_s, model=model,
+                       records=records, order=order)
         rc = self._L.pt_run_device(
             method_id(method), npart, m, self._h, _ptr(_f64(params)),
             C.c_void_p(d_time.data_ptr()), C.c_void_p(d_state.data_ptr()),
