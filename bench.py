@@ -84,6 +84,8 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-controller leg")
     ap.add_argument("--no-order", action="store_true",
                     help="keep the natural queue order (default: longest first)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="launch every kernel in its default variant (3 blocks per SM)")
     ap.add_argument("--records", type=int, default=10_000_000)
     ap.add_argument("--legs", default="headline,mixed,learned",
                     help="comma list of legs to run (headline always prints the line)")
@@ -325,6 +327,15 @@ class QueueOrder:
             self.order = self.torch.argsort(work, descending=True).to(self.torch.int32)
 
 
+def tune(args, f, method, prm, d_time, d_state, stream, **kw):
+    """pt_autotune of the kernel the next runs launch (launch variant = resident
+    blocks per SM); the choice becomes that kernel's default."""
+    if args.no_autotune:
+        return None
+    v, ms = f.autotune(method, prm, d_time, d_state, stream=stream.cuda_stream, **kw)
+    return {"blocks_per_sm": v, "trial_ms": {str(k): round(t, 3) for k, t in ms.items()}}
+
+
 def ks_distance(a, b):
     """Two-sample Kolmogorov-Smirnov statistic."""
     a, b = np.sort(np.asarray(a)), np.sort(np.asarray(b))
@@ -378,6 +389,7 @@ def mixed_leg(args, dev, stream):
         f = handles[prec]
         mdl = model if name == "fp32_learned" else None
         st, cnt, status, carry = fresh(npart)
+        launch = tune(args, f, "rk5", prm, d_time, st, stream, model=mdl)
         ordq = QueueOrder(torch, cnt, enabled=not args.no_order)
         w = 0
         for _ in range(args.warmup):
@@ -405,7 +417,7 @@ def mixed_leg(args, dev, stream):
                        "rejected_fraction": float(d[2] / max(d[0], 1)),
                        "ms_per_step": 1e3 * sec / args.mixed_steps,
                        "particle_gyroperiods_per_s": npart * window * args.mixed_steps / sec,
-                       "stopped_particles": stopped}
+                       "stopped_particles": stopped, "launch": launch}
         if name == "fp64":
             # the plain integrator writes the learned controller's training records
             rec = LRN.record_buffer(torch, min(args.records, 4_000_000))
@@ -541,6 +553,7 @@ def learned_leg(args, dev, stream):
     snap = (st.clone(), cnt.clone(), carry.clone())
     for name, mdl in (("classical", None), ("learned", model)):
         st.copy_(snap[0]); cnt.copy_(snap[1]); carry.copy_(snap[2])
+        launch = tune(args, f, "dop853", prm, d_time, st, stream, eta=cfg["eta"], model=mdl)
         ordq = QueueOrder(torch, cnt, enabled=not args.no_order)
         w = 0
         for _ in range(args.warmup):
@@ -571,7 +584,7 @@ def learned_leg(args, dev, stream):
                      "rejected_fraction": float(d[2] / max(d[0], 1)),
                      "attempts": int(d[0]), "accepted": int(d[1]),
                      "particle_gyroperiods_per_s": npart * window * args.steps / sec,
-                     "stopped_particles": stopped}
+                     "stopped_particles": stopped, "launch": launch}
     model.close()
     f.close()
     c, l = out["classical"], out["learned"]
@@ -620,6 +633,7 @@ def main():
         d_carry = torch.zeros(int(L.pt_carry_bytes(npart)), dtype=torch.uint8, device=dev)
     stream.synchronize()
 
+    launch = tune(args, f, cfg["method"], prm, d_time, d_state, stream, eta=cfg["eta"])
     ordq = QueueOrder(torch, d_cnt, enabled=not args.no_order)
 
     def window_run(w):
@@ -694,7 +708,7 @@ def main():
         "wall_s_timed": wall, "gpu_launches": args.steps, "stopped_particles": stopped,
         "rejected_fraction": float(dcnt_tot[2] / max(dcnt_tot[0], 1)),
         "attempts_per_s": float(dcnt_tot[0]) / elapsed,
-        "roofline": roof, "clocks": clocks.summary(),
+        "roofline": roof, "clocks": clocks.summary(), "launch": launch,
     }
 
     # end to end through the host-buffer C ABI: pinned host copies every step

@@ -91,7 +91,10 @@ typedef struct pt_options {
     int64_t       record_capacity;/* records that fit after the header */
     const int32_t *order;         /* device: particle index per queue slot, e.g. longest
                                      first (pt_run_device only), or NULL */
-    int64_t       reserved[1];
+    int32_t       blocks_per_sm;  /* resident blocks per SM the kernel is compiled for:
+                                     2, 3 or 4 (register caps 255, 168, 128); 0 = the
+                                     choice of pt_autotune for this kernel, else 3 */
+    int32_t       reserved;
 } pt_options;
 
 /* ---- one-shot, reference-shaped call ----------------------------------- */
@@ -147,6 +150,18 @@ int pt_run_device(int32_t method, int64_t np, int32_t m, const pt_fields *f,
 /* After synchronising the stream of the last pt_run_device on f: PT_OK,
  * PT_ERR_TIMEOUT or PT_ERR_CUDA. */
 int pt_run_check(const pt_fields *f);
+
+/* Launch autotuner: times the kernel that pt_run_device would launch with
+ * these arguments in each of its launch variants (blocks_per_sm 2, 3, 4) on
+ * a sample of the particles -- the first min(np, 2 x 4 x 128 per SM) of them,
+ * their first two output rows, max_steps attempts each (opt->max_steps, else
+ * 32), on scratch copies -- and makes the fastest the default
+ * (blocks_per_sm == 0) of that kernel for the rest of the process.  d_state
+ * is only read.  Synchronises the stream.  chosen: the variant (2, 3 or 4);
+ * ms_out (host, 3 doubles, or NULL): the trial times of variants 2, 3, 4. */
+int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_fields *f,
+                const double params[17], const double *d_time, const double *d_state,
+                const pt_options *opt, void *stream, int32_t *chosen, double ms_out[3]);
 
 /* ---- learned step-size controller (no counterpart in the reference) ----- */
 

@@ -28,7 +28,7 @@ EXPORTS = [
     "pt_run_device", "pt_run_check", "pt_last_error", "pt_abi_version", "pt_tableau",
     "pt_debug_pow", "pt_debug_accel", "pt_probe_peak", "pt_debug_unpack", "pt_debug_echo",
     "pt_integrate_device_noalloc", "pt_mlp_nparam", "pt_mlp_create", "pt_mlp_destroy",
-    "pt_mlp_infer", "pt_mlp_loss_grad", "pt_mlp_adam",
+    "pt_mlp_infer", "pt_mlp_loss_grad", "pt_mlp_adam", "pt_autotune",
 ]
 
 
@@ -39,7 +39,7 @@ class PtOptions(C.Structure):
         ("jj", C.c_void_p), ("t_stop", C.c_double), ("time_budget_s", C.c_double),
         ("status", C.c_void_p), ("carry", C.c_void_p), ("model", C.c_void_p),
         ("records", C.c_void_p), ("record_capacity", C.c_int64), ("order", C.c_void_p),
-        ("reserved", C.c_int64 * 1),
+        ("blocks_per_sm", C.c_int32), ("reserved", C.c_int32),
     ]
 
 
@@ -77,6 +77,7 @@ def load():
     L.pt_carry_bytes.restype = i64
     L.pt_run_device.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.pt_run_check.argtypes = [vp]
+    L.pt_autotune.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp, C.POINTER(i32), vp]
     L.pt_last_error.restype = C.c_char_p
     L.pt_abi_version.restype = i32
     L.pt_tableau.argtypes = [i32, vp]

@@ -3,7 +3,8 @@
 Plain ``nvcc`` invocations, one per translation unit, run in parallel, then
 one link.  The FP64 kernel source is compiled twice: ``exact`` with
 ``--fmad=false`` (bit-identical to the CPU oracle) and ``fma`` with FMA
-contraction.  Host code is compiled with ``-ffp-contract=off`` so that host
+contraction; each integrator source is split by method (``PT_PART``) so the
+launch variants of RK5 and DOP853 compile in parallel.  Host code is compiled with ``-ffp-contract=off`` so that host
 arithmetic (parameter unpacking) rounds the same on x86-64 and aarch64.
 Outputs go to ``particles_gb300/_build/`` (git-ignored).
 """
@@ -31,9 +32,12 @@ COMMON = [
 # (output object, source, extra flags)
 UNITS = [
     ("pt_api.o", "pt_api.cu", ["--fmad=false"]),
-    ("pt_fp64_exact.o", "pt_fp64.cu", ["--fmad=false", "-DPT_SFX=exact", "-DPT_EXACT"]),
-    ("pt_fp64_fma.o", "pt_fp64.cu", ["--fmad=true", "-DPT_SFX=fma"]),
-    ("pt_mixed.o", "pt_mixed.cu", ["--fmad=true"]),
+    ("pt_fp64_exact1.o", "pt_fp64.cu", ["--fmad=false", "-DPT_SFX=exact", "-DPT_EXACT", "-DPT_PART=1"]),
+    ("pt_fp64_exact2.o", "pt_fp64.cu", ["--fmad=false", "-DPT_SFX=exact", "-DPT_EXACT", "-DPT_PART=2"]),
+    ("pt_fp64_fma1.o", "pt_fp64.cu", ["--fmad=true", "-DPT_SFX=fma", "-DPT_PART=1"]),
+    ("pt_fp64_fma2.o", "pt_fp64.cu", ["--fmad=true", "-DPT_SFX=fma", "-DPT_PART=2"]),
+    ("pt_mixed1.o", "pt_mixed.cu", ["--fmad=true", "-DPT_PART=1"]),
+    ("pt_mixed2.o", "pt_mixed.cu", ["--fmad=true", "-DPT_PART=2"]),
     ("pt_probe.o", "pt_probe.cu", ["--fmad=true"]),
     ("pt_noalloc.o", "pt_noalloc.cu", ["--fmad=false"]),
     ("pt_mlp_train.o", "pt_mlp_train.cu", ["--fmad=true"]),

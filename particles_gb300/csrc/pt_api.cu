@@ -11,6 +11,7 @@
  */
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
@@ -291,6 +292,8 @@ static int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
             return set_err(PT_ERR_ARG, "controller 1 needs opt->model%s");
         if (opt->records && opt->record_capacity < 0)
             return set_err(PT_ERR_ARG, "negative record capacity%s");
+        if (opt->blocks_per_sm != 0 && (opt->blocks_per_sm < 2 || opt->blocks_per_sm > 4))
+            return set_err(PT_ERR_ARG, "blocks_per_sm must be 0, 2, 3 or 4%s");
         eta = opt->eta;
         t_stop = opt->t_stop;
         budget = opt->time_budget_s;
@@ -318,8 +321,18 @@ static int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
         R.rec = static_cast<float *>(opt->records);
         R.rec_cap = opt->record_capacity;
         R.order = opt->order;
+        R.minb = opt->blocks_per_sm;
     }
     return PT_OK;
+}
+
+/* Launch variants chosen by pt_autotune, per kernel family
+ * [precision][method - 1][with J][learned]; 0 = not tuned. */
+static std::atomic<int> g_tuned[4][2][2][2];
+
+static std::atomic<int> &tuned_slot(int32_t method, const pt_fields *f, const PtRun &R)
+{
+    return g_tuned[f->precision & 3][method - 1][f->has_j ? 1 : 0][(R.mlp || R.rec) ? 1 : 0];
 }
 
 static RunShape shape_of(const pt_fields *f)
@@ -329,6 +342,16 @@ static RunShape shape_of(const pt_fields *f)
     g.precision = f->precision;
     g.has_j = f->has_j;
     return g;
+}
+
+static cudaError_t launch_run(int32_t method, const pt_fields *f, const PtRun &R, cudaStream_t s)
+{
+    if (f->precision == PT_PREC_FP64)
+        return method == PT_METHOD_RK5 ? pt_launch_rk5_exact(R, f->nc, s) : pt_launch_dp853_exact(R, f->nc, s);
+    if (f->precision == PT_PREC_FP64_FMA)
+        return method == PT_METHOD_RK5 ? pt_launch_rk5_fma(R, f->nc, s) : pt_launch_dp853_fma(R, f->nc, s);
+    return method == PT_METHOD_RK5 ? pt_launch_rk5_mixed(R, f->nc32, s)
+                                   : pt_launch_dp853_mixed(R, f->nc32, s);
 }
 
 static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
@@ -349,6 +372,10 @@ static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
     R.carry = static_cast<unsigned char *>(d_carry);
     R.queue = f->scratch;
     R.flags = reinterpret_cast<int32_t *>(f->scratch + 1);
+    if (R.minb == 0) {
+        const int t = tuned_slot(method, f, R).load(std::memory_order_relaxed);
+        R.minb = t ? t : PT_MINB_DEFAULT;
+    }
 
     cudaError_t e;
     if (d_status && np > 0) {
@@ -357,14 +384,83 @@ static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
     }
     e = cudaMemsetAsync(f->scratch, 0, 2 * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return cuda_err(e, "scratch reset");
-    if (f->precision == PT_PREC_FP64)
-        e = method == PT_METHOD_RK5 ? pt_launch_rk5_exact(R, f->nc, s) : pt_launch_dp853_exact(R, f->nc, s);
-    else if (f->precision == PT_PREC_FP64_FMA)
-        e = method == PT_METHOD_RK5 ? pt_launch_rk5_fma(R, f->nc, s) : pt_launch_dp853_fma(R, f->nc, s);
-    else
-        e = method == PT_METHOD_RK5 ? pt_launch_rk5_mixed(R, f->nc32, s)
-                                    : pt_launch_dp853_mixed(R, f->nc32, s);
+    e = launch_run(method, f, R, s);
     if (e != cudaSuccess) return cuda_err(e, "kernel launch");
+    return PT_OK;
+}
+
+extern "C" int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_fields *f,
+                           const double params[17], const double *d_time, const double *d_state,
+                           const pt_options *opt, void *stream, int32_t *chosen, double ms_out[3])
+{
+    if (!f) return set_err(PT_ERR_ARG, "fields handle is NULL%s");
+    if (np < 1 || !d_time || !d_state) return set_err(PT_ERR_ARG, "autotune needs np >= 1 and buffers%s");
+    PtRun R;
+    int rc = prepare_run(method, np, m, shape_of(f), params, opt, R);
+    if (rc != PT_OK) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_err(e, "pt_autotune");
+    const int64_t ns = np < (int64_t)sms * 4 * 128 * 2 ? np : (int64_t)sms * 4 * 128 * 2;
+    const int32_t mt = m < 2 ? m : 2;
+    double *t_state = nullptr;
+    int64_t *t_cnt = nullptr;
+    float *t_rec = nullptr;            /* a record header with no room: counted, not written */
+    cudaEvent_t ev[2] = { nullptr, nullptr };
+    double ms[3] = { 0, 0, 0 };
+    int best = 0;
+    e = cudaMalloc(&t_state, (size_t)ns * mt * 8 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&t_cnt, (size_t)ns * 3 * sizeof(int64_t));
+    if (e == cudaSuccess && R.rec) e = cudaMalloc(&t_rec, 16);
+    if (e == cudaSuccess && t_rec) e = cudaMemsetAsync(t_rec, 0, 16, s);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[0]);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+    R.np = ns;
+    R.m = mt;
+    R.time = d_time;
+    R.state = t_state;
+    R.cnt = t_cnt;
+    R.status = nullptr;
+    R.carry = nullptr;
+    R.order = nullptr;
+    R.rec = t_rec;
+    R.rec_cap = 0;
+    R.fld = f->rec64;
+    R.fld32 = f->rec32;
+    R.queue = f->scratch;
+    R.flags = reinterpret_cast<int32_t *>(f->scratch + 1);
+    if (!(opt && opt->max_steps > 0)) R.max_steps = 32;
+    for (int round = 0; round < 2 && e == cudaSuccess; ++round) {   /* round 0 warms up */
+        for (int v = 0; v < 3 && e == cudaSuccess; ++v) {
+            R.minb = 2 + v;
+            e = cudaMemcpy2DAsync(t_state, (size_t)mt * 64, d_state, (size_t)m * 64, 64, (size_t)ns,
+                                  cudaMemcpyDeviceToDevice, s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(f->scratch, 0, 2 * sizeof(unsigned long long), s);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
+            if (e == cudaSuccess) e = launch_run(method, f, R, s);
+            if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+            float t = 0.0f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+            if (e == cudaSuccess && round == 1) {
+                ms[v] = t;
+                if (ms[v] < ms[best]) best = v;
+            }
+        }
+    }
+    if (ev[0]) cudaEventDestroy(ev[0]);
+    if (ev[1]) cudaEventDestroy(ev[1]);
+    cudaFree(t_state);
+    cudaFree(t_cnt);
+    cudaFree(t_rec);
+    if (e != cudaSuccess) return cuda_err(e, "pt_autotune");
+    R.minb = 0;
+    tuned_slot(method, f, R).store(2 + best, std::memory_order_relaxed);
+    if (chosen) *chosen = 2 + best;
+    if (ms_out)
+        for (int v = 0; v < 3; ++v) ms_out[v] = ms[v];
     return PT_OK;
 }
 

@@ -57,7 +57,14 @@ struct PtRun {
     int64_t rec_cap;       /* record capacity */
     unsigned long long *queue;  /* work-queue head */
     int32_t *flags;        /* [0] time budget hit, [1] particles with negative status */
+    int32_t minb;          /* launch variant: resident blocks per SM (2, 3 or 4) */
 };
+
+/* Launch variant of an integrator: the same kernel compiled for 2, 3 or 4
+ * resident 128-thread blocks per SM.  The register cap (255 / 168 / 128) is
+ * the trade: more blocks hide more latency, fewer avoid spills (the learned
+ * controller's MLP, DOP853's k rows in flight).  Results do not depend on it. */
+#define PT_MINB_DEFAULT 3
 
 /* Carry (controller memory) SoA layout inside one buffer of 128*np bytes:
  *   double t[np], dt[np], errold[np], si[6][np], k1[6][np]; int32 n[np], flags[np]

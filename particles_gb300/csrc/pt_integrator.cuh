@@ -134,9 +134,9 @@ __device__ __forceinline__ void next_time(const PtRun &P, Lane &L)
  * f(si) if it was saved).  Returns 0 fresh, 1 resumed without f(si),
  * 2 resumed with f(si) loaded into row F1. */
 template <int METHOD>
-__device__ __forceinline__ int lane_open(const PtRun &P, const PtCarry &C, const KRows &K,
-                                         Lane &L, double si[6])
+__device__ __forceinline__ int lane_open(const PtRun &P, const KRows &K, Lane &L, double si[6])
 {
+    const PtCarry C = pt_carry_view(P.carry, P.np);    /* recomputed here, not held in registers */
     const bool fresh = (P.carry == nullptr) || !(C.flags[L.p] & 1);
     if (fresh) {
         const double2 *s = reinterpret_cast<const double2 *>(P.state + (int64_t)8 * P.m * L.p);
@@ -161,10 +161,10 @@ __device__ __forceinline__ int lane_open(const PtRun &P, const PtCarry &C, const
 }
 
 template <int METHOD>
-__device__ __forceinline__ void lane_close(const PtRun &P, const PtCarry &C, const KRows &K,
-                                           const Lane &L, const double si[6], int32_t st,
-                                           bool have_f1)
+__device__ __forceinline__ void lane_close(const PtRun &P, const KRows &K, const Lane &L,
+                                           const double si[6], int32_t st, bool have_f1)
 {
+    const PtCarry C = pt_carry_view(P.carry, P.np);
     P.cnt[3 * L.p] = L.c0;
     P.cnt[3 * L.p + 1] = L.c1;
     P.cnt[3 * L.p + 2] = L.c2;
@@ -386,6 +386,33 @@ __host__ __device__ constexpr int smem_bytes(int block, bool record)
     return Traits<METHOD>::ROWS * 6 * 8 * block + (record ? 8 * 4 * block : 0);
 }
 
+/* Persistent launch of one integrator variant: as many blocks as fit on
+ * every SM (registers of the variant, shared memory of the run), fewer when
+ * the particles run out.  cache = { shared-memory size, blocks per SM } of
+ * the last occupancy query of this variant. */
+template <class KERN>
+cudaError_t launch_persistent(KERN kern, int block, int smem, int smem_full, int cache[2],
+                              const PtRun &P, cudaStream_t s)
+{
+    static int sms = 0;
+    if (cache[0] != smem) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_full);
+        if (e != cudaSuccess) return e;
+        int dev = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, smem);
+        if (e != cudaSuccess) return e;
+        cache[1] = per_sm < 1 ? 1 : per_sm;
+        cache[0] = smem;
+    }
+    int64_t grid = (int64_t)sms * cache[1];
+    const int64_t need = (P.np + block - 1) / block;
+    if (need < grid) grid = need;
+    kern<<<(int)(grid < 1 ? 1 : grid), block, smem, s>>>(P);
+    return cudaGetLastError();
+}
+
 template <int METHOD, class EV, bool LEARN>
 __device__ __forceinline__ void run_machine(const PtRun &P)
 {
@@ -394,15 +421,10 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
     const KRows K{ pt_ksm + threadIdx.x, (int)blockDim.x };
     unsigned char *const smem_tail =
         reinterpret_cast<unsigned char *>(pt_ksm) + T::ROWS * 6 * 8 * blockDim.x;
-    PtMlpSmem M{};
     float *pend = nullptr;                 /* pending features, [8][blockDim] */
     bool have_pend = false;
-    if (LEARN) {
-        if (P.mlp) M = pt_mlp_view(P.mlp);
-        if (P.rec) pend = reinterpret_cast<float *>(smem_tail) + threadIdx.x;
-    }
+    if (LEARN && P.rec) pend = reinterpret_cast<float *>(smem_tail) + threadIdx.x;
     const uint64_t t_start = pt_globaltimer();
-    const PtCarry C = P.carry ? pt_carry_view(P.carry, P.np) : PtCarry{};
     Lane L;
     L.p = 0; L.t = 0.0; L.dt = 0.0; L.errold = 0.0; L.tnext = 0.0; L.n = 0;
     L.rejected = false; L.c0 = L.c1 = L.c2 = 0;
@@ -422,7 +444,7 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
             if (active) {
                 q = finish_attempt<METHOD>(P, K, si, L.dt, pt, dl);
                 if (q != q) {
-                    lane_close<METHOD>(P, C, K, L, si, PT_ST_NONFINITE, true);
+                    lane_close<METHOD>(P, K, L, si, PT_ST_NONFINITE, true);
                     active = false;
                 } else if (q <= 1.0) {
                     mode = M_ACCEPT;
@@ -436,7 +458,7 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
                 const unsigned long long qi = atomicAdd(P.queue, 1ULL);
                 if ((int64_t)qi < P.np) {
                     L.p = P.order ? (int64_t)P.order[qi] : (int64_t)qi;
-                    const int how = lane_open<METHOD>(P, C, K, L, si);
+                    const int how = lane_open<METHOD>(P, K, L, si);
                     have_pend = false;
                     if (how == 2) {
                         mode = M_READY;
@@ -510,7 +532,7 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
                 L.c0++;
                 L.dt = pt_min(L.dt, P.dtm);                             /* :195, :500 */
                 if (escaped_x(P, si[0])) {
-                    lane_close<METHOD>(P, C, K, L, si, PT_ST_ESCAPED, true);
+                    lane_close<METHOD>(P, K, L, si, PT_ST_ESCAPED, true);
                     active = false;
                 }
             } else if (mode == M_REJECT) {                            /* :178-187, :480-490 */
@@ -565,7 +587,7 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
                     }
                 }
                 if (P.mlp && __any_sync(0xffffffffu, want)) {
-                    const float y = pt_mlp_warp(M, feat);
+                    const float y = pt_mlp_warp(pt_mlp_view(P.mlp), feat);
                     if (want) {
                         const double lo = P.fcmn * dt;
                         const double hi = (METHOD == PT_METHOD_DOP853 && was_rejected) ? dt : P.fcmx * dt;
@@ -579,7 +601,7 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
             if (active) {
                 const int32_t st = lane_check(P, L, t_start);
                 if (st != PT_GO) {
-                    lane_close<METHOD>(P, C, K, L, si, st, true);
+                    lane_close<METHOD>(P, K, L, si, st, true);
                     active = false;
                 } else {
                     if (METHOD == PT_METHOD_RK5) {

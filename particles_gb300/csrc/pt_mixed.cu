@@ -31,6 +31,9 @@
 #include "pt_integrator.cuh"
 
 #define PT_BLOCK 128
+#ifndef PT_PART
+#define PT_PART 0
+#endif
 
 namespace {
 
@@ -136,8 +139,8 @@ struct EvalF32 {
     }
 };
 
-template <int METHOD, int NC, bool LEARN>
-__global__ void __launch_bounds__(PT_BLOCK, 3) k_integrate_mixed(const PtRun P)
+template <int METHOD, int NC, bool LEARN, int MINB>
+__global__ void __launch_bounds__(PT_BLOCK, MINB) k_integrate_mixed(const PtRun P)
 {
     pt_sm::run_machine<METHOD, EvalF32<NC>, LEARN>(P);
 }
@@ -159,52 +162,52 @@ __global__ void k_accel_mixed(const PtRun P, int64_t n, const double *vec, doubl
     }
 }
 
-template <int METHOD, int NC, bool LEARN>
+template <int METHOD, int NC, bool LEARN, int MINB>
 cudaError_t launch1(const PtRun &P, cudaStream_t s)
 {
-    auto kern = k_integrate_mixed<METHOD, NC, LEARN>;
-    const int smem = pt_sm::smem_bytes<METHOD>(PT_BLOCK, LEARN && P.rec != nullptr);
-    /* occupancy per shared-memory size (recording runs add 4 KB per block) */
-    static int conf_smem[2] = { -1, -1 }, conf_per_sm[2] = { 1, 1 };
-    static int sms = 0;
-    const int slot = (LEARN && P.rec != nullptr) ? 1 : 0;
-    if (conf_smem[slot] != smem) {
-        const int full = pt_sm::smem_bytes<METHOD>(PT_BLOCK, true);
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, full);
-        if (e != cudaSuccess) return e;
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&conf_per_sm[slot], kern, PT_BLOCK, smem);
-        if (conf_per_sm[slot] < 1) conf_per_sm[slot] = 1;
-        conf_smem[slot] = smem;
+    static int cache[2][2] = { { -1, 1 }, { -1, 1 } };  /* without / with recording */
+    const bool rec = LEARN && P.rec != nullptr;
+    return pt_sm::launch_persistent(k_integrate_mixed<METHOD, NC, LEARN, MINB>, PT_BLOCK,
+                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK, rec),
+                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK, true), cache[rec], P, s);
+}
+
+template <int METHOD, int NC, bool LEARN>
+cudaError_t launch_v(const PtRun &P, cudaStream_t s)
+{
+    switch (P.minb) {
+    case 2: return launch1<METHOD, NC, LEARN, 2>(P, s);
+    case 4: return launch1<METHOD, NC, LEARN, 4>(P, s);
+    default: return launch1<METHOD, NC, LEARN, 3>(P, s);
     }
-    const int per_sm = conf_per_sm[slot];
-    int64_t grid = (int64_t)sms * per_sm;
-    const int64_t need = (P.np + PT_BLOCK - 1) / PT_BLOCK;
-    if (need < grid) grid = need;
-    kern<<<(int)(grid < 1 ? 1 : grid), PT_BLOCK, smem, s>>>(P);
-    return cudaGetLastError();
 }
 
 template <int METHOD, int NC>
 cudaError_t launch(const PtRun &P, cudaStream_t s)
 {
     if (P.np <= 0) return cudaSuccess;
-    return (P.mlp || P.rec) ? launch1<METHOD, NC, true>(P, s) : launch1<METHOD, NC, false>(P, s);
+    return (P.mlp || P.rec) ? launch_v<METHOD, NC, true>(P, s) : launch_v<METHOD, NC, false>(P, s);
 }
 
 }  // namespace
 
+/* PT_PART splits the launchers over two translation units (1: RK5 and the
+ * debug kernel, 2: DOP853) so that they compile in parallel. */
+#if PT_PART != 2
 cudaError_t pt_launch_rk5_mixed(const PtRun &P, int nc, cudaStream_t s)
 {
     return nc == 12 ? launch<PT_METHOD_RK5, 12>(P, s) : launch<PT_METHOD_RK5, 8>(P, s);
 }
+#endif
 
+#if PT_PART != 1
 cudaError_t pt_launch_dp853_mixed(const PtRun &P, int nc, cudaStream_t s)
 {
     return nc == 12 ? launch<PT_METHOD_DOP853, 12>(P, s) : launch<PT_METHOD_DOP853, 8>(P, s);
 }
+#endif
+
+#if PT_PART != 2
 
 cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int64_t n, const double *vec,
                                   double *acc, cudaStream_t s)
@@ -215,3 +218,4 @@ cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int64_t n, const doubl
     else k_accel_mixed<8><<<grid, 128, 0, s>>>(P, n, vec, acc);
     return cudaGetLastError();
 }
+#endif

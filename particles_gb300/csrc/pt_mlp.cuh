@@ -63,6 +63,21 @@ __device__ __forceinline__ void pt_mma16816(float c[4], const uint32_t a[4], uin
 
 __device__ __forceinline__ float pt_silu(float z) { return z / (1.0f + __expf(-z)); }
 
+/* SiLU of two accumulators, packed as the next layer's FP16 pair:
+ * silu(z) = z (1/2 + tanh(z/2)/2), with the one-instruction tanh.approx.f16x2
+ * (absolute error ~1e-3, below the FP16 operand rounding of the next layer). */
+__device__ __forceinline__ uint32_t pt_silu_h2(float z0, float z1)
+{
+    const __half2 z = __floats2half2_rn(z0, z1);
+    const __half2 half = __float2half2_rn(0.5f);
+    const __half2 h = __hmul2(z, half);
+    uint32_t t;
+    asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(*reinterpret_cast<const uint32_t *>(&h)));
+    const __half2 sg = __hfma2(*reinterpret_cast<const __half2 *>(&t), half, half);
+    const __half2 y = __hmul2(z, sg);
+    return *reinterpret_cast<const uint32_t *>(&y);
+}
+
 /* Views of a blob; blob may be shared memory or global memory (the
  * integrator reads it through L1, 11.9 KB, so the k rows keep all of the
  * shared memory and the occupancy of the classical kernel). */
@@ -129,32 +144,35 @@ __device__ __forceinline__ float pt_mlp_warp(const PtMlpSmem &M, const float x[8
             c[1] = c[3] = M.b1[8 * nt + 2 * q + 1];
             pt_mma16816(c, a1, M.frag[PT_MLP_FRAG_W1 + nt * 32 + lane]);
             const int kt = nt >> 1, hiw = (nt & 1) * 2;
-            a2[kt][hiw] = pt_pack_h2(pt_silu(c[0]), pt_silu(c[1]));
-            a2[kt][hiw + 1] = pt_pack_h2(pt_silu(c[2]), pt_silu(c[3]));
+            a2[kt][hiw] = pt_silu_h2(c[0], c[1]);
+            a2[kt][hiw + 1] = pt_silu_h2(c[2], c[3]);
         }
-        /* layer 2 -> SiLU -> layer-3 A fragments */
-        uint32_t a3[4][4];
+        /* layer 2 -> SiLU -> layer 3, one k16 slice of layer 3 per pair of
+         * layer-2 n tiles (keeps 4 fragment registers live instead of 16);
+         * column 0 of layer 3's n8 tile is the output */
+        float c3[4] = { M.b3[0], 0.0f, M.b3[0], 0.0f };
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            float c[4];
-            c[0] = c[2] = M.b2[8 * nt + 2 * q];
-            c[1] = c[3] = M.b2[8 * nt + 2 * q + 1];
+        for (int kt3 = 0; kt3 < 4; ++kt3) {
+            uint32_t a3[4];
 #pragma unroll
-            for (int kt = 0; kt < 4; ++kt)
-                pt_mma16816(c, a2[kt], M.frag[PT_MLP_FRAG_W2 + (kt * 8 + nt) * 32 + lane]);
-            const int kt3 = nt >> 1, hiw = (nt & 1) * 2;
-            a3[kt3][hiw] = pt_pack_h2(pt_silu(c[0]), pt_silu(c[1]));
-            a3[kt3][hiw + 1] = pt_pack_h2(pt_silu(c[2]), pt_silu(c[3]));
+            for (int h = 0; h < 2; ++h) {
+                const int nt = 2 * kt3 + h;
+                float c[4];
+                c[0] = c[2] = M.b2[8 * nt + 2 * q];
+                c[1] = c[3] = M.b2[8 * nt + 2 * q + 1];
+#pragma unroll
+                for (int kt = 0; kt < 4; ++kt)
+                    pt_mma16816(c, a2[kt], M.frag[PT_MLP_FRAG_W2 + (kt * 8 + nt) * 32 + lane]);
+                a3[2 * h] = pt_silu_h2(c[0], c[1]);
+                a3[2 * h + 1] = pt_silu_h2(c[2], c[3]);
+            }
+            pt_mma16816(c3, a3, M.frag[PT_MLP_FRAG_W3 + kt3 * 32 + lane]);
         }
-        /* layer 3: column 0 of the n8 tile is the output */
-        float c[4] = { M.b3[0], 0.0f, M.b3[0], 0.0f };
-#pragma unroll
-        for (int kt = 0; kt < 4; ++kt) pt_mma16816(c, a3[kt], M.frag[PT_MLP_FRAG_W3 + kt * 32 + lane]);
         /* row r0 sits in c0 of lane 4g, row r1 in c2 of lane 4g (q == 0) */
         const int r = lane - 16 * mt;
         const int src = 4 * (r & 7);
-        const float y0 = __shfl_sync(0xffffffffu, c[0], src);
-        const float y1 = __shfl_sync(0xffffffffu, c[2], src);
+        const float y0 = __shfl_sync(0xffffffffu, c3[0], src);
+        const float y1 = __shfl_sync(0xffffffffu, c3[2], src);
         if (r >= 0 && r < 16) out = (r < 8) ? y0 : y1;
     }
     return out;
@@ -166,7 +184,15 @@ __device__ __forceinline__ float pt_mlp_warp(const PtMlpSmem &M, const float x[8
 #include "pt_convert.cuh"
 
 __device__ __forceinline__ float pt_to_f(float v) { return v; }
-__device__ __forceinline__ float pt_to_f(double v) { return pt_d2f(v); }   /* integer pipe */
+/* Features need a few digits: truncate the double's top mantissa bits into a
+ * float on the integer pipe (normal range; zero maps to zero). */
+__device__ __forceinline__ float pt_to_f(double v)
+{
+    const uint32_t hi = (uint32_t)((uint64_t)__double_as_longlong(v) >> 32);
+    const uint32_t e = (hi >> 20) & 0x7ffu;
+    if (e < 897u) return 0.0f;
+    return __uint_as_float((hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3));
+}
 
 /* The five field invariants of the learned controller at the particle state
  * s, in FP32: log|B|, log|E|, log gamma, pitch cosine u.B/(|u||B|) and

@@ -29,7 +29,7 @@ def _f64(a):
 
 def _options(precision, *, eta=0.0, jj=None, open_x=False, max_steps=0, t_stop=0.0,
              status=None, carry=None, time_budget_s=0.0, model=None, records=None,
-             order=None):
+             order=None, blocks_per_sm=0):
     o = N.PtOptions()
     o.struct_size = C.sizeof(N.PtOptions)
     o.precision = N.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
@@ -48,6 +48,7 @@ def _options(precision, *, eta=0.0, jj=None, open_x=False, max_steps=0, t_stop=0
     o.time_budget_s = float(time_budget_s)
     o.status = _ptr(status)
     o.carry = _ptr(carry)
+    o.blocks_per_sm = int(blocks_per_sm)
     return o
 
 
@@ -163,16 +164,17 @@ class Fields:
 
     def run_device(self, method, params, d_time, d_state, d_cnt, d_status=None, d_carry=None,
                    *, eta=0.0, open_x=False, max_steps=0, t_stop=0.0, time_budget_s=0.0,
-                   stream=0, model=None, records=None, order=None):
+                   stream=0, model=None, records=None, order=None, blocks_per_sm=0):
         """Launch on device tensors (torch); returns without synchronising.
 
         model: a learned.Model for the learned controller; records: a device
-        record buffer (learned.record_buffer); order: device int32 queue order.
+        record buffer (learned.record_buffer); order: device int32 queue order;
+        blocks_per_sm: launch variant (0 = tuned or default, else 2, 3, 4).
         """
         npart, m, _ = d_state.shape
         opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
                        t_stop=t_stop, time_budget_s=time_budget_s, model=model,
-                       records=records, order=order)
+                       records=records, order=order, blocks_per_sm=blocks_per_sm)
         rc = self._L.pt_run_device(
             method_id(method), npart, m, self._h, _ptr(_f64(params)),
             C.c_void_p(d_time.data_ptr()), C.c_void_p(d_state.data_ptr()),
@@ -181,6 +183,24 @@ class Fields:
             C.c_void_p(d_carry.data_ptr()) if d_carry is not None else None,
             C.byref(opt), C.c_void_p(stream) if stream else None)
         N.check(rc, "pt_run_device")
+
+    def autotune(self, method, params, d_time, d_state, *, eta=0.0, open_x=False, max_steps=0,
+                 stream=0, model=None, records=None):
+        """Time the launch variants of the kernel run_device would use with
+        these arguments (pt_autotune) and make the fastest its default.
+
+        Returns (blocks_per_sm, {variant: trial ms})."""
+        npart, m, _ = d_state.shape
+        opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
+                       model=model, records=records)
+        chosen = C.c_int32(0)
+        ms = np.zeros(3, np.float64)
+        rc = self._L.pt_autotune(method_id(method), npart, m, self._h, _ptr(_f64(params)),
+                                 C.c_void_p(d_time.data_ptr()), C.c_void_p(d_state.data_ptr()),
+                                 C.byref(opt), C.c_void_p(stream) if stream else None,
+                                 C.byref(chosen), _ptr(ms))
+        N.check(rc, "pt_autotune")
+        return int(chosen.value), {2 + i: float(ms[i]) for i in range(3)}
 
     def run_check(self) -> int:
         return int(self._L.pt_run_check(self._h))

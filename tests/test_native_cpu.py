@@ -74,3 +74,21 @@ def test_options_struct_layout():
     from particles_gb300 import _native as N
     assert C.sizeof(N.PtOptions) == 112
     assert N.PtOptions.max_steps.offset == 16 and N.PtOptions.carry.offset == 64
+
+
+def test_launch_variant_option_checked_on_host(native):
+    """blocks_per_sm must be 0 (tuned or default) or 2..4; checked before any CUDA call."""
+    from particles_gb300 import _native as N
+    from particles_gb300.params import pack_params
+    assert N.PtOptions.blocks_per_sm.offset == 104
+    dm = np.array([8, 8, 8], np.int32)
+    p = pack_params(qom=1.0, vunit=0.1, tmax=1.0)
+    out = np.zeros(8)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)
+    for v, rc in ((0, N.PT_OK), (2, N.PT_OK), (3, N.PT_OK), (4, N.PT_OK), (1, N.PT_ERR_ARG),
+                  (5, N.PT_ERR_ARG), (-3, N.PT_ERR_ARG)):
+        o = N.PtOptions()
+        o.struct_size = C.sizeof(o)
+        o.blocks_per_sm = v
+        assert native.pt_debug_unpack(1, 4, 2, ptr(dm), 0, 0, ptr(p), C.byref(o), ptr(out)) == rc
+    assert native.pt_autotune(1, 4, 2, None, ptr(p), None, None, None, None, None, None) == N.PT_ERR_ARG
