@@ -58,6 +58,11 @@ WORKLOADS = {
     "rk5-512": dict(method="rk5", n=512, spectrum="kolmogorov", nmax=32, db_rms=1.0, v_rms=0.2,
                     eta=0.0, npart=1 << 22, gamma=(1.001, 1e2), speed=None, tol=1e-8,
                     periods=50, seed=2, window=0.02),
+    # uneven batch in one persistent launch (configuration 4): three snapshots
+    "ensemble-3": dict(method="dop853", n=(128, 192, 256), spectrum="kolmogorov", nmax=32,
+                       db_rms=(0.5, 1.0, 2.0), v_rms=0.2, eta=0.0, npart=1 << 21,
+                       split=(1, 2, 4), gamma=(1.0001, 1e4), speed=None,
+                       tol=(1e-6, 1e-8, 1e-10), periods=10, seed=(1, 2, 3), window=0.02),
     # the CPU-runnable configuration (reference RK5, 64^3, 1024 particles)
     "rk5-64": dict(method="rk5", n=64, spectrum="flat", nmax=4, db_rms=0.5, v_rms=0.1,
                    eta=0.0, npart=1024, gamma=None, speed=0.5, tol=1e-8, periods=10, seed=0,
@@ -71,7 +76,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="dop853-256")
+    ap.add_argument("--workload", choices=sorted(k for k in WORKLOADS if k != "ensemble-3"),
+                    default="dop853-256")
     ap.add_argument("--precision", choices=["fp64", "fp64_fma", "fp32"], default="fp64")
     ap.add_argument("--particles", type=int, default=0,
                     help="override the particle count (profiling of small cases only)")
@@ -84,10 +90,12 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-controller leg")
     ap.add_argument("--no-order", action="store_true",
                     help="keep the natural queue order (default: longest first)")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble leg")
+    ap.add_argument("--ensemble-precision", choices=["fp64", "fp64_fma", "fp32"], default="fp64")
     ap.add_argument("--no-autotune", action="store_true",
                     help="launch every kernel in its default variant (3 blocks per SM)")
     ap.add_argument("--records", type=int, default=10_000_000)
-    ap.add_argument("--legs", default="headline,mixed,learned",
+    ap.add_argument("--legs", default="headline,mixed,learned,ensemble",
                     help="comma list of legs to run (headline always prints the line)")
     ap.add_argument("--mixed-steps", type=int, default=5)
     ap.add_argument("--accuracy-particles", type=int, default=32768)
@@ -488,6 +496,95 @@ def mixed_leg(args, dev, stream):
     return out
 
 
+def ensemble_leg(args, dev, stream):
+    """Configuration 4: three snapshots (128^3, 192^3, 256^3; dB_rms 0.5, 1, 2;
+    seeds 1-3) with 2^21 particles split 1:2:4, gamma log-uniform in
+    [1.0001, 1e4], DOP853 at rtol 1e-6, 1e-8, 1e-10 and an open x boundary, in
+    ONE persistent launch per window; finished and escaped particles are
+    compacted out of the work lists between windows, which are reordered
+    longest first.  Timed both as one launch sequence per window and as one
+    captured CUDA graph of the same number of windows."""
+    import torch
+    from particles_gb300 import Ensemble, Fields, fields, initial, params
+    cfg = WORKLOADS["ensemble-3"]
+    prec = args.ensemble_precision
+    tot = cfg["npart"]
+    counts = [tot * w // sum(cfg["split"]) for w in cfg["split"]]
+    counts[-1] = tot - sum(counts[:-1])
+    tmax = cfg["periods"] * T0
+    tg = params.time_grid(cfg["periods"], tmax)
+    members, keep = [], []
+    for k in range(3):
+        prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=tmax, atol=cfg["tol"][k],
+                                 rtol=cfg["tol"][k], facmin=0.333, facmax=6.0, safe=0.9, beta=0.0)
+        uu, bb = fields.snapshot(cfg["n"][k], db_rms=cfg["db_rms"][k], v_rms=cfg["v_rms"],
+                                 vunit=VUN, spectrum=cfg["spectrum"], nmin=1.0, nmax=cfg["nmax"],
+                                 seed=cfg["seed"][k], backend="torch")
+        f = Fields(uu, bb, precision=prec, stream=stream.cuda_stream)
+        del uu, bb
+        torch.cuda.empty_cache()
+        n = counts[k]
+        s0 = initial.isotropic_state(n, cfg["seed"][k], gamma_range=cfg["gamma"])
+        st = torch.zeros((n, tg.size, 8), dtype=torch.float64, device=dev)
+        st[:, 0, :6] = torch.tensor(s0, device=dev)
+        members.append(dict(fields=f, params=prm, open_x=True,
+                            time=torch.tensor(tg, device=dev), state=st,
+                            cnt=torch.zeros((n, 3), dtype=torch.int64, device=dev),
+                            status=torch.zeros(n, dtype=torch.int32, device=dev),
+                            carry=torch.zeros(int(f._L.pt_carry_bytes(n)), dtype=torch.uint8,
+                                              device=dev)))
+        keep.append(f)
+    launch = tune(args, members[2]["fields"], cfg["method"], members[2]["params"],
+                  members[2]["time"], members[2]["state"], stream)
+    ens = Ensemble(cfg["method"], members, precision=prec)
+    win = cfg["window"] * T0
+    out = {"workload": "ensemble-3", "grids": ["128^3", "192^3", "256^3"],
+           "particles": counts, "rtol": list(cfg["tol"]), "gamma": list(cfg["gamma"]),
+           "precision": prec, "window_gyroperiods": cfg["window"], "open_x": True,
+           "launch": launch}
+
+    def accepted():
+        return sum(int(m["cnt"][:, 1].sum()) for m in members)
+
+    t = 0.0
+    for _ in range(args.warmup):
+        t += win
+        ens.run(t, stream=stream.cuda_stream)
+    stream.synchronize()
+    res = {}
+    for mode in ("launches", "graph"):
+        a0 = accepted()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if mode == "graph":
+            ens.capture(args.steps, win, stream=stream.cuda_stream)
+            e0.record(stream)
+            ens.replay(stream=stream.cuda_stream)
+            e1.record(stream)
+            t += args.steps * win
+        else:
+            e0.record(stream)
+            for _ in range(args.steps):
+                t += win
+                ens.run(t, stream=stream.cuda_stream)
+            e1.record(stream)
+        stream.synchronize()
+        sec = e0.elapsed_time(e1) * 1e-3
+        live, esc = ens.counts()
+        res[mode] = {"accepted_steps_per_s": (accepted() - a0) / sec,
+                     "ms_per_step": 1e3 * sec / args.steps,
+                     "live": live.tolist(), "escaped": esc.tolist()}
+    rc = ens.check()
+    live, esc = ens.counts()
+    out.update(res)
+    out["escaped_fraction"] = float(esc.sum()) / tot
+    out["t_gyroperiods"] = t / T0
+    out["check"] = int(rc)
+    ens.close()
+    for f in keep:
+        f.close()
+    return out
+
+
 def learned_leg(args, dev, stream):
     """Configuration 5: a controller trained on accepted-step records of the
     plain integrator on the configuration-2 shape with field seed 10, then
@@ -757,6 +854,9 @@ def main():
     if not args.no_learned and "learned" in legs and rank == 0 and args.workload == "dop853-256":
         torch.cuda.empty_cache()
         line["learned"] = learned_leg(args, dev, stream)
+    if not args.no_ensemble and "ensemble" in legs and rank == 0 and args.workload == "dop853-256":
+        torch.cuda.empty_cache()
+        line["ensemble"] = ensemble_leg(args, dev, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

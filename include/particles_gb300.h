@@ -163,6 +163,66 @@ int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_fields *f,
                 const double params[17], const double *d_time, const double *d_state,
                 const pt_options *opt, void *stream, int32_t *chosen, double ms_out[3]);
 
+/* ---- ensembles: several runs in one persistent launch (no counterpart in
+ *      the reference; each member is what one pt_run_device call would do) -- */
+
+#define PT_ENSEMBLE_MAX 8
+
+/* One member: a snapshot (field handle), its params(1:17), its particles.
+ * All members of an ensemble share the method and the field precision and
+ * either all or none carry J.  Device pointers in the layouts of
+ * pt_run_device; status and carry are required (the ensemble runs in
+ * windows and drops finished particles from its queue between them). */
+typedef struct pt_member {
+    const pt_fields *fields;
+    const double    *params;      /* host: params(1:17) of this member */
+    int64_t          np;
+    int32_t          m;
+    int32_t          open_x;      /* 1: particles escape through the x faces */
+    double           eta;         /* resistivity (needs a handle with J) */
+    int64_t          max_steps;   /* attempt cap per particle; 0 = 1e9 */
+    const double    *time;        /* device: m output times */
+    double          *state;       /* device: state(8,m,np) */
+    int64_t         *cnt;         /* device: cnt(3,np) */
+    int32_t         *status;      /* device: np status words (set to PT_ST_RUNNING) */
+    void            *carry;       /* device: pt_carry_bytes(np), zero-filled = fresh */
+} pt_member;
+
+typedef struct pt_ensemble pt_ensemble;
+
+/* Builds the member table on the device, the per-member work lists (all
+ * particles, in index order) and the escaped lists.  opt: precision,
+ * blocks_per_sm and time_budget_s are used; controller must be 0. */
+int pt_ensemble_create(int32_t method, int32_t nmembers, const pt_member *members,
+                       const pt_options *opt, pt_ensemble **out);
+int pt_ensemble_destroy(pt_ensemble *e);
+
+/* One window: integrate every live particle of every member while
+ * t < min(t_stop, tmax of its member) in ONE persistent launch, then compact
+ * each member's work list -- particles that are done, escaped or failed
+ * leave it; escaped ones are appended to the member's escaped list -- and
+ * order it longest first by the attempts each particle needed in this
+ * window.  Launches on `stream` without synchronising. */
+int pt_ensemble_run(pt_ensemble *e, double t_stop, void *stream);
+
+/* Captures `windows` consecutive windows, each advancing the window end by
+ * dt_window from its current value, as one CUDA graph held by e (replacing
+ * any earlier one); pt_ensemble_replay launches it.  Nothing runs during the
+ * capture. */
+int pt_ensemble_capture(pt_ensemble *e, int32_t windows, double dt_window, void *stream);
+int pt_ensemble_replay(pt_ensemble *e, void *stream);
+
+/* After synchronising: live (still queued) and escaped particle counts per
+ * member (host arrays of nmembers, either may be NULL). */
+int pt_ensemble_counts(const pt_ensemble *e, int64_t *live, int64_t *escaped);
+/* After synchronising: copies up to `capacity` indices of member k's escaped
+ * particles (in the order they were compacted) to host memory; *n = count. */
+int pt_ensemble_escaped(const pt_ensemble *e, int32_t member, int32_t *out, int64_t capacity,
+                        int64_t *n);
+
+/* After synchronising: PT_OK, PT_ERR_TIMEOUT or PT_ERR_PARTICLE as pt_run_check. */
+int pt_ensemble_check(const pt_ensemble *e);
+
 /* ---- learned step-size controller (no counterpart in the reference) ----- */
 
 /* MLP 8 -> 64 -> 64 -> 1 (SiLU) from eight local invariants at the start of

@@ -29,6 +29,8 @@ EXPORTS = [
     "pt_debug_pow", "pt_debug_accel", "pt_probe_peak", "pt_debug_unpack", "pt_debug_echo",
     "pt_integrate_device_noalloc", "pt_mlp_nparam", "pt_mlp_create", "pt_mlp_destroy",
     "pt_mlp_infer", "pt_mlp_loss_grad", "pt_mlp_adam", "pt_autotune",
+    "pt_ensemble_create", "pt_ensemble_destroy", "pt_ensemble_run", "pt_ensemble_capture",
+    "pt_ensemble_replay", "pt_ensemble_counts", "pt_ensemble_escaped", "pt_ensemble_check",
 ]
 
 
@@ -40,6 +42,15 @@ class PtOptions(C.Structure):
         ("status", C.c_void_p), ("carry", C.c_void_p), ("model", C.c_void_p),
         ("records", C.c_void_p), ("record_capacity", C.c_int64), ("order", C.c_void_p),
         ("blocks_per_sm", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
+class PtMember(C.Structure):
+    _fields_ = [
+        ("fields", C.c_void_p), ("params", C.c_void_p), ("np", C.c_int64), ("m", C.c_int32),
+        ("open_x", C.c_int32), ("eta", C.c_double), ("max_steps", C.c_int64),
+        ("time", C.c_void_p), ("state", C.c_void_p), ("cnt", C.c_void_p),
+        ("status", C.c_void_p), ("carry", C.c_void_p),
     ]
 
 
@@ -78,6 +89,14 @@ def load():
     L.pt_run_device.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.pt_run_check.argtypes = [vp]
     L.pt_autotune.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp, C.POINTER(i32), vp]
+    L.pt_ensemble_create.argtypes = [i32, i32, vp, vp, C.POINTER(vp)]
+    L.pt_ensemble_destroy.argtypes = [vp]
+    L.pt_ensemble_run.argtypes = [vp, d, vp]
+    L.pt_ensemble_capture.argtypes = [vp, i32, d, vp]
+    L.pt_ensemble_replay.argtypes = [vp, vp]
+    L.pt_ensemble_counts.argtypes = [vp, vp, vp]
+    L.pt_ensemble_escaped.argtypes = [vp, i32, vp, i64, C.POINTER(i64)]
+    L.pt_ensemble_check.argtypes = [vp]
     L.pt_last_error.restype = C.c_char_p
     L.pt_abi_version.restype = i32
     L.pt_tableau.argtypes = [i32, vp]

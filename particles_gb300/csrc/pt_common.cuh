@@ -58,6 +58,9 @@ struct PtRun {
     unsigned long long *queue;  /* work-queue head */
     int32_t *flags;        /* [0] time budget hit, [1] particles with negative status */
     int32_t minb;          /* launch variant: resident blocks per SM (2, 3 or 4) */
+    int32_t *work;         /* per particle: attempts made in this run, or NULL */
+    const int64_t *qlen;   /* ensembles: device queue length (else np) */
+    const double *tstop;   /* ensembles: device window end (else tend) */
 };
 
 /* Launch variant of an integrator: the same kernel compiled for 2, 3 or 4
@@ -145,12 +148,20 @@ struct PtLaunch {
     cudaError_t pt_launch_dp853_##sfx(const PtRun &P, int nc, cudaStream_t s);   \
     cudaError_t pt_launch_accel_##sfx(const PtRun &P, int nc, int64_t n,         \
                                       const double *vec, double *acc, cudaStream_t s); \
-    cudaError_t pt_launch_echo_##sfx(const PtRun &P, double *out, cudaStream_t s);
+    cudaError_t pt_launch_echo_##sfx(const PtRun &P, double *out, cudaStream_t s);    \
+    cudaError_t pt_launch_rk5_ens_##sfx(const PtRun *tab, int nmem, int nc, int minb, \
+                                        int64_t ntot, cudaStream_t s);              \
+    cudaError_t pt_launch_dp853_ens_##sfx(const PtRun *tab, int nmem, int nc, int minb, \
+                                          int64_t ntot, cudaStream_t s);
 
 PT_DECLARE_FP64_LAUNCHERS(exact)
 PT_DECLARE_FP64_LAUNCHERS(fma)
 
 cudaError_t pt_launch_rk5_mixed(const PtRun &P, int nc, cudaStream_t s);
+cudaError_t pt_launch_rk5_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
+                                    cudaStream_t s);
+cudaError_t pt_launch_dp853_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
+                                      cudaStream_t s);
 cudaError_t pt_launch_dp853_mixed(const PtRun &P, int nc, cudaStream_t s);
 cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int64_t n, const double *vec,
                                   double *acc, cudaStream_t s);

@@ -119,6 +119,7 @@ struct Lane {
     int64_t p;
     double t, dt, errold, tnext;
     int32_t n;
+    int32_t w0;            /* low 32 bits of c0 when the particle was opened */
     bool rejected;
     int64_t c0, c1, c2;
 };
@@ -144,6 +145,7 @@ __device__ __forceinline__ int lane_open(const PtRun &P, const KRows &K, Lane &L
         si[0] = a.x; si[1] = a.y; si[2] = b.x; si[3] = b.y; si[4] = c.x; si[5] = c.y;
         L.t = 0.0; L.n = 1; L.errold = 1.0e-04; L.rejected = false;
         L.c0 = L.c1 = L.c2 = 0;
+        L.w0 = 0;
         return 0;
     }
     const int32_t fl = C.flags[L.p];
@@ -152,6 +154,7 @@ __device__ __forceinline__ int lane_open(const PtRun &P, const KRows &K, Lane &L
 #pragma unroll
     for (int c = 0; c < 6; ++c) si[c] = C.si[(int64_t)c * P.np + L.p];
     L.c0 = P.cnt[3 * L.p]; L.c1 = P.cnt[3 * L.p + 1]; L.c2 = P.cnt[3 * L.p + 2];
+    L.w0 = (int32_t)L.c0;
     if (fl & 4) {
 #pragma unroll
         for (int c = 0; c < 6; ++c) K(Traits<METHOD>::F1, c) = C.k1[(int64_t)c * P.np + L.p];
@@ -169,6 +172,7 @@ __device__ __forceinline__ void lane_close(const PtRun &P, const KRows &K, const
     P.cnt[3 * L.p + 1] = L.c1;
     P.cnt[3 * L.p + 2] = L.c2;
     if (P.status) P.status[L.p] = st;
+    if (P.work) P.work[L.p] = (int32_t)L.c0 - L.w0;     /* attempts made in this run */
     if (P.carry) {
         C.t[L.p] = L.t; C.dt[L.p] = L.dt; C.errold[L.p] = L.errold; C.n[L.p] = L.n;
         C.flags[L.p] = 1 | (L.rejected ? 2 : 0) | (have_f1 ? 4 : 0);
@@ -388,11 +392,12 @@ __host__ __device__ constexpr int smem_bytes(int block, bool record)
 
 /* Persistent launch of one integrator variant: as many blocks as fit on
  * every SM (registers of the variant, shared memory of the run), fewer when
- * the particles run out.  cache = { shared-memory size, blocks per SM } of
- * the last occupancy query of this variant. */
-template <class KERN>
+ * the np particles run out.  cache = { shared-memory size, blocks per SM } of
+ * the last occupancy query of this variant.  np < 0 only configures the
+ * kernel (attributes, occupancy), e.g. before a stream capture. */
+template <class KERN, class... Args>
 cudaError_t launch_persistent(KERN kern, int block, int smem, int smem_full, int cache[2],
-                              const PtRun &P, cudaStream_t s)
+                              int64_t np, cudaStream_t s, Args... args)
 {
     static int sms = 0;
     if (cache[0] != smem) {
@@ -406,15 +411,60 @@ cudaError_t launch_persistent(KERN kern, int block, int smem, int smem_full, int
         cache[1] = per_sm < 1 ? 1 : per_sm;
         cache[0] = smem;
     }
+    if (np < 0) return cudaSuccess;
     int64_t grid = (int64_t)sms * cache[1];
-    const int64_t need = (P.np + block - 1) / block;
+    const int64_t need = (np + block - 1) / block;
     if (need < grid) grid = need;
-    kern<<<(int)(grid < 1 ? 1 : grid), block, smem, s>>>(P);
+    kern<<<(int)(grid < 1 ? 1 : grid), block, smem, s>>>(args...);
     return cudaGetLastError();
 }
 
-template <int METHOD, class EV, bool LEARN>
-__device__ __forceinline__ void run_machine(const PtRun &P)
+/* Ensemble launch: the member table (PT_ENS_MAX runs at most) is copied to
+ * shared memory; each member's window end and queue length come from device
+ * memory, so a captured graph can advance them without host work. */
+#define PT_ENS_MAX PT_ENSEMBLE_MAX
+
+__device__ __forceinline__ void ens_load(const PtRun *__restrict__ tab, int nmem, PtRun *sP,
+                                         int64_t *sN)
+{
+    const int words = nmem * (int)(sizeof(PtRun) / 8);
+    const unsigned long long *src = reinterpret_cast<const unsigned long long *>(tab);
+    unsigned long long *dst = reinterpret_cast<unsigned long long *>(sP);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    if (threadIdx.x < nmem) {
+        PtRun &R = sP[threadIdx.x];
+        sN[threadIdx.x] = R.qlen ? *R.qlen : R.np;
+        if (R.tstop) {
+            const double ts = *R.tstop;
+            R.tend = (ts > 0.0 && ts < R.tmx) ? ts : R.tmx;
+        }
+    }
+    __syncthreads();
+}
+
+/* Which run a lane's particle belongs to.  A single run reads everything
+ * from the kernel parameter P (constant bank).  An ensemble launch holds a
+ * table of runs (members) in shared memory; each lane walks the members'
+ * queues in order and keeps the index of the member it draws from. */
+template <bool ENS> struct Members;
+template <> struct Members<false> {
+    const PtRun &P;
+    __device__ __forceinline__ const PtRun &q(int) const { return P; }
+    __device__ __forceinline__ int64_t queue_len(int) const { return P.np; }
+    __device__ __forceinline__ int count() const { return 1; }
+};
+template <> struct Members<true> {
+    const PtRun *tab;        /* shared memory */
+    const int64_t *nq;       /* shared memory: queue length per member */
+    int n;
+    __device__ __forceinline__ const PtRun &q(int mi) const { return tab[mi]; }
+    __device__ __forceinline__ int64_t queue_len(int mi) const { return nq[mi]; }
+    __device__ __forceinline__ int count() const { return n; }
+};
+
+template <int METHOD, class EV, bool LEARN, bool ENS = false>
+__device__ __forceinline__ void run_machine(const Members<ENS> &MB)
 {
     using T = Traits<METHOD>;
     extern __shared__ double pt_ksm[];
@@ -423,7 +473,9 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
         reinterpret_cast<unsigned char *>(pt_ksm) + T::ROWS * 6 * 8 * blockDim.x;
     float *pend = nullptr;                 /* pending features, [8][blockDim] */
     bool have_pend = false;
-    if (LEARN && P.rec) pend = reinterpret_cast<float *>(smem_tail) + threadIdx.x;
+    int mi = 0;                            /* member this lane draws particles from */
+#define PT_Q (MB.q(mi))
+    if (LEARN && PT_Q.rec) pend = reinterpret_cast<float *>(smem_tail) + threadIdx.x;
     const uint64_t t_start = pt_globaltimer();
     Lane L;
     L.p = 0; L.t = 0.0; L.dt = 0.0; L.errold = 0.0; L.tnext = 0.0; L.n = 0;
@@ -442,9 +494,9 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
         if (j == 0) {
             /* ---- tail: finish the attempt that just ran ---- */
             if (active) {
-                q = finish_attempt<METHOD>(P, K, si, L.dt, pt, dl);
+                q = finish_attempt<METHOD>(PT_Q, K, si, L.dt, pt, dl);
                 if (q != q) {
-                    lane_close<METHOD>(P, K, L, si, PT_ST_NONFINITE, true);
+                    lane_close<METHOD>(PT_Q, K, L, si, PT_ST_NONFINITE, true);
                     active = false;
                 } else if (q <= 1.0) {
                     mode = M_ACCEPT;
@@ -455,10 +507,17 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
             }
             /* ---- idle lanes take the next particle ---- */
             if (!active && !drained) {
-                const unsigned long long qi = atomicAdd(P.queue, 1ULL);
-                if ((int64_t)qi < P.np) {
-                    L.p = P.order ? (int64_t)P.order[qi] : (int64_t)qi;
-                    const int how = lane_open<METHOD>(P, K, L, si);
+                unsigned long long qi = 0;
+                bool got = false;
+                while (!got && mi < MB.count()) {
+                    qi = atomicAdd(PT_Q.queue, 1ULL);
+                    got = (int64_t)qi < MB.queue_len(mi);
+                    if (!got) ++mi;
+                }
+                if (ENS && !got) mi = MB.count() - 1;   /* stay on a valid member */
+                if (got) {
+                    L.p = PT_Q.order ? (int64_t)PT_Q.order[qi] : (int64_t)qi;
+                    const int how = lane_open<METHOD>(PT_Q, K, L, si);
                     have_pend = false;
                     if (how == 2) {
                         mode = M_READY;
@@ -467,7 +526,7 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
                         need = true;
 #pragma unroll
                         for (int c = 0; c < 6; ++c) { pt[c] = si[c]; dl[c] = 0.0; }
-                        EV::begin(P, si, O);
+                        EV::begin(PT_Q, si, O);
                     }
                     active = true;
                     fresh = (how == 0);
@@ -480,7 +539,7 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
             need = true;
         }
 
-        if (need) EV::f(P, pt, dl, O, a);                    /* the one evaluation site */
+        if (need) EV::f(PT_Q, pt, dl, O, a);                    /* the one evaluation site */
 
         if (j != 0) {
             if (active) {
@@ -502,57 +561,57 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
              * :186).  The products below keep the reference's order. */
             double fpow = 0.0;
             if (mode == M_ACCEPT || mode == M_REJECT) {
-                const double y = (METHOD == PT_METHOD_DOP853) ? P.expo
+                const double y = (METHOD == PT_METHOD_DOP853) ? PT_Q.expo
                                : (mode == M_ACCEPT ? -0.20 : -0.25);
-                fpow = P.safe * pt_det_pow(q, y);
+                fpow = PT_Q.safe * pt_det_pow(q, y);
             }
             if (mode == M_ACCEPT) {                                    /* :150-177, :439-476 */
                 L.t = L.t + dt;
-                while (L.n < P.m && L.t >= L.tnext) {
-                    double *row = P.state + (int64_t)8 * ((int64_t)L.n + (int64_t)P.m * L.p);
+                while (L.n < PT_Q.m && L.t >= L.tnext) {
+                    double *row = PT_Q.state + (int64_t)8 * ((int64_t)L.n + (int64_t)PT_Q.m * L.p);
                     if (METHOD == PT_METHOD_DOP853)
                         dense_row(L.t, dt, L.tnext, si, pt, K, 0, a, 0, true, row);
                     else
                         dense_row(L.t, dt, L.tnext, si, pt, K, 0, nullptr, 5, false, row);
                     L.n++;
-                    next_time(P, L);
+                    next_time(PT_Q, L);
                 }
 #pragma unroll
                 for (int c = 0; c < 6; ++c) { si[c] = pt[c]; K(T::F1, c) = a[c]; }
                 L.c1++;
                 if (METHOD == PT_METHOD_DOP853) {
-                    double dtn = pt_max(P.fcmn, fpow * pt_det_pow(L.errold, P.beta));
-                    dtn = L.rejected ? dt * pt_min(dtn, 1.0) : dt * pt_min(dtn, P.fcmx);
+                    double dtn = pt_max(PT_Q.fcmn, fpow * pt_det_pow(L.errold, PT_Q.beta));
+                    dtn = L.rejected ? dt * pt_min(dtn, 1.0) : dt * pt_min(dtn, PT_Q.fcmx);
                     L.errold = pt_max(q, 1.0e-04);
                     L.rejected = false;
                     L.dt = dtn;
                 } else {
-                    L.dt = dt * pt_min(P.fcmx, fpow);
+                    L.dt = dt * pt_min(PT_Q.fcmx, fpow);
                 }
                 L.c0++;
-                L.dt = pt_min(L.dt, P.dtm);                             /* :195, :500 */
-                if (escaped_x(P, si[0])) {
-                    lane_close<METHOD>(P, K, L, si, PT_ST_ESCAPED, true);
+                L.dt = pt_min(L.dt, PT_Q.dtm);                             /* :195, :500 */
+                if (escaped_x(PT_Q, si[0])) {
+                    lane_close<METHOD>(PT_Q, K, L, si, PT_ST_ESCAPED, true);
                     active = false;
                 }
             } else if (mode == M_REJECT) {                            /* :178-187, :480-490 */
                 L.c2++;
-                L.dt = dt * pt_max(P.fcmn, fpow);
+                L.dt = dt * pt_max(PT_Q.fcmn, fpow);
                 if (METHOD == PT_METHOD_DOP853) L.rejected = true;
                 L.c0++;
-                L.dt = pt_min(L.dt, P.dtm);
+                L.dt = pt_min(L.dt, PT_Q.dtm);
             } else if (mode == M_INIT) {
 #pragma unroll
                 for (int c = 0; c < 6; ++c) K(T::F1, c) = a[c];
                 if (fresh) {                                           /* :120-127 */
-                    L.dt = dti_finish(P, T::IORD, si, a);
-                    double *row = P.state + (int64_t)8 * P.m * L.p;
+                    L.dt = dti_finish(PT_Q, T::IORD, si, a);
+                    double *row = PT_Q.state + (int64_t)8 * PT_Q.m * L.p;
                     row[6] = sqrt(si[3] * si[3] + si[4] * si[4] + si[5] * si[5] + 1.0);
                     row[7] = L.dt;
                 }
-                next_time(P, L);
+                next_time(PT_Q, L);
             } else if (mode == M_READY) {
-                next_time(P, L);
+                next_time(PT_Q, L);
             }
             if (LEARN) {
                 /* Features at the new si of an accepted step: the record of
@@ -563,18 +622,18 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
                 const bool want = (mode == M_ACCEPT) && active;
                 float feat[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
                 if (want) {
-                    pt_field_features<typename EV::Rec, EV::NCR>(P, EV::records(P), si, feat);
-                    const float om = P.qomf * __expf(feat[0] - feat[2]);     /* qom |B| / gamma */
+                    pt_field_features<typename EV::Rec, EV::NCR>(PT_Q, EV::records(PT_Q), si, feat);
+                    const float om = PT_Q.qomf * __expf(feat[0] - feat[2]);     /* qom |B| / gamma */
                     const float dtf = pt_d2f(dt);
                     feat[5] = __logf(om * dtf + 1e-30f);
                     feat[6] = __logf(pt_d2f(q) + 1e-30f);
                     feat[7] = __logf(dtf);
-                    if (P.rec) {
+                    if (PT_Q.rec) {
                         if (have_pend) {
                             const unsigned long long i =
-                                atomicAdd(reinterpret_cast<unsigned long long *>(P.rec), 1ULL);
-                            if ((int64_t)i < P.rec_cap) {
-                                float *r = P.rec + PT_REC_HEADER_FLOATS + i * PT_REC_FLOATS;
+                                atomicAdd(reinterpret_cast<unsigned long long *>(PT_Q.rec), 1ULL);
+                            if ((int64_t)i < PT_Q.rec_cap) {
+                                float *r = PT_Q.rec + PT_REC_HEADER_FLOATS + i * PT_REC_FLOATS;
 #pragma unroll
                                 for (int c = 0; c < 8; ++c) r[c] = pend[c * blockDim.x];
                                 r[8] = feat[7];
@@ -586,29 +645,29 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
                         have_pend = true;
                     }
                 }
-                if (P.mlp && __any_sync(0xffffffffu, want)) {
-                    const float y = pt_mlp_warp(pt_mlp_view(P.mlp), feat);
+                if (PT_Q.mlp && __any_sync(0xffffffffu, want)) {
+                    const float y = pt_mlp_warp(pt_mlp_view(PT_Q.mlp), feat);
                     if (want) {
-                        const double lo = P.fcmn * dt;
-                        const double hi = (METHOD == PT_METHOD_DOP853 && was_rejected) ? dt : P.fcmx * dt;
+                        const double lo = PT_Q.fcmn * dt;
+                        const double hi = (METHOD == PT_METHOD_DOP853 && was_rejected) ? dt : PT_Q.fcmx * dt;
                         const double h = pt_f2d(__expf(y));
                         L.dt = pt_min(pt_max(h, lo), hi);
-                        L.dt = pt_min(L.dt, P.dtm);
+                        L.dt = pt_min(L.dt, PT_Q.dtm);
                     }
                 }
             }
             /* ---- start of the next attempt ---- */
             if (active) {
-                const int32_t st = lane_check(P, L, t_start);
+                const int32_t st = lane_check(PT_Q, L, t_start);
                 if (st != PT_GO) {
-                    lane_close<METHOD>(P, K, L, si, st, true);
+                    lane_close<METHOD>(PT_Q, K, L, si, st, true);
                     active = false;
                 } else {
                     if (METHOD == PT_METHOD_RK5) {
 #pragma unroll
                         for (int c = 0; c < 6; ++c) K(0, c) = L.dt * K(T::F1, c);   /* :137, j = 1 */
                     }
-                    EV::begin(P, si, O);
+                    EV::begin(PT_Q, si, O);
                 }
             }
             if (!__any_sync(0xffffffffu, active)) {
@@ -619,6 +678,7 @@ __device__ __forceinline__ void run_machine(const PtRun &P)
         j = (j + 1 < T::SLOTS) ? j + 1 : 0;
     }
 }
+#undef PT_Q
 
 }  // namespace pt_sm
 

@@ -142,7 +142,18 @@ struct EvalF32 {
 template <int METHOD, int NC, bool LEARN, int MINB>
 __global__ void __launch_bounds__(PT_BLOCK, MINB) k_integrate_mixed(const PtRun P)
 {
-    pt_sm::run_machine<METHOD, EvalF32<NC>, LEARN>(P);
+    pt_sm::run_machine<METHOD, EvalF32<NC>, LEARN>(pt_sm::Members<false>{ P });
+}
+
+/* Several runs (members: snapshots, tolerances, particle sets) in one
+ * persistent launch; every lane drains the members' queues in table order. */
+template <int METHOD, int NC, int MINB>
+__global__ void __launch_bounds__(PT_BLOCK, MINB) k_ensemble_mixed(const PtRun *__restrict__ tab, int nmem)
+{
+    __shared__ PtRun sP[PT_ENS_MAX];
+    __shared__ int64_t sN[PT_ENS_MAX];
+    pt_sm::ens_load(tab, nmem, sP, sN);
+    pt_sm::run_machine<METHOD, EvalF32<NC>, false, true>(pt_sm::Members<true>{ sP, sN, nmem });
 }
 
 template <int NC>
@@ -169,7 +180,28 @@ cudaError_t launch1(const PtRun &P, cudaStream_t s)
     const bool rec = LEARN && P.rec != nullptr;
     return pt_sm::launch_persistent(k_integrate_mixed<METHOD, NC, LEARN, MINB>, PT_BLOCK,
                                     pt_sm::smem_bytes<METHOD>(PT_BLOCK, rec),
-                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK, true), cache[rec], P, s);
+                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK, true), cache[rec], P.np, s,
+                                    P);
+}
+
+template <int METHOD, int NC, int MINB>
+cudaError_t launch_ens1(const PtRun *tab, int nmem, int64_t ntot, cudaStream_t s)
+{
+    static int cache[2] = { -1, 1 };
+    const int smem = pt_sm::smem_bytes<METHOD>(PT_BLOCK, false);
+    return pt_sm::launch_persistent(k_ensemble_mixed<METHOD, NC, MINB>, PT_BLOCK, smem, smem, cache, ntot, s,
+                                    tab, nmem);
+}
+
+template <int METHOD, int NC>
+cudaError_t launch_ens(const PtRun *tab, int nmem, int minb, int64_t ntot, cudaStream_t s)
+{
+    if (ntot == 0) return cudaSuccess;          /* ntot < 0: configure only */
+    switch (minb) {
+    case 2: return launch_ens1<METHOD, NC, 2>(tab, nmem, ntot, s);
+    case 4: return launch_ens1<METHOD, NC, 4>(tab, nmem, ntot, s);
+    default: return launch_ens1<METHOD, NC, 3>(tab, nmem, ntot, s);
+    }
 }
 
 template <int METHOD, int NC, bool LEARN>
@@ -198,12 +230,26 @@ cudaError_t pt_launch_rk5_mixed(const PtRun &P, int nc, cudaStream_t s)
 {
     return nc == 12 ? launch<PT_METHOD_RK5, 12>(P, s) : launch<PT_METHOD_RK5, 8>(P, s);
 }
+
+cudaError_t pt_launch_rk5_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
+                                    cudaStream_t s)
+{
+    return nc == 12 ? launch_ens<PT_METHOD_RK5, 12>(tab, nmem, minb, ntot, s)
+                    : launch_ens<PT_METHOD_RK5, 8>(tab, nmem, minb, ntot, s);
+}
 #endif
 
 #if PT_PART != 1
 cudaError_t pt_launch_dp853_mixed(const PtRun &P, int nc, cudaStream_t s)
 {
     return nc == 12 ? launch<PT_METHOD_DOP853, 12>(P, s) : launch<PT_METHOD_DOP853, 8>(P, s);
+}
+
+cudaError_t pt_launch_dp853_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
+                                      cudaStream_t s)
+{
+    return nc == 12 ? launch_ens<PT_METHOD_DOP853, 12>(tab, nmem, minb, ntot, s)
+                    : launch_ens<PT_METHOD_DOP853, 8>(tab, nmem, minb, ntot, s);
 }
 #endif
 

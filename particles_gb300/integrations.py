@@ -204,3 +204,84 @@ class Fields:
 
     def run_check(self) -> int:
         return int(self._L.pt_run_check(self._h))
+
+
+class Ensemble:
+    """Several runs (members) in one persistent launch per window
+    (pt_ensemble_*): each member is a snapshot (a Fields handle), its
+    params(1:17) and its particles on the device.  Between windows the
+    finished and escaped particles leave the work lists, which are ordered
+    longest first; a sequence of windows can be captured as a CUDA graph.
+
+    members: list of dicts with keys fields, params, time, state, cnt,
+    status, carry (torch CUDA tensors for the last five) and optionally
+    open_x, eta, max_steps.
+    """
+
+    def __init__(self, method, members, *, precision="fp64", blocks_per_sm=0,
+                 time_budget_s=0.0):
+        self._L = N.load()
+        self._h = C.c_void_p()
+        self.n = len(members)
+        self._keep = []
+        arr = (N.PtMember * self.n)()
+        for k, mb in enumerate(members):
+            prm = _f64(mb["params"])
+            self._keep.append(prm)
+            st = mb["state"]
+            a = arr[k]
+            a.fields = mb["fields"].handle
+            a.params = prm.ctypes.data_as(C.c_void_p)
+            a.np, a.m = int(st.shape[0]), int(st.shape[1])
+            a.open_x = int(bool(mb.get("open_x", False)))
+            a.eta = float(mb.get("eta", 0.0))
+            a.max_steps = int(mb.get("max_steps", 0))
+            for key in ("time", "state", "cnt", "status", "carry"):
+                setattr(a, key, C.c_void_p(mb[key].data_ptr()))
+        opt = _options(precision, time_budget_s=time_budget_s, blocks_per_sm=blocks_per_sm)
+        N.check(self._L.pt_ensemble_create(method_id(method), self.n, C.byref(arr), C.byref(opt),
+                                           C.byref(self._h)), "pt_ensemble_create")
+
+    def run(self, t_stop, stream=0):
+        """One window up to t_stop (0 = to each member's tmax); no synchronisation."""
+        N.check(self._L.pt_ensemble_run(self._h, float(t_stop), C.c_void_p(stream) if stream else None),
+                "pt_ensemble_run")
+
+    def capture(self, windows, dt_window, stream=0):
+        N.check(self._L.pt_ensemble_capture(self._h, int(windows), float(dt_window),
+                                            C.c_void_p(stream) if stream else None),
+                "pt_ensemble_capture")
+
+    def replay(self, stream=0):
+        N.check(self._L.pt_ensemble_replay(self._h, C.c_void_p(stream) if stream else None),
+                "pt_ensemble_replay")
+
+    def counts(self):
+        """(live, escaped) particle counts per member, after synchronising."""
+        live = np.zeros(self.n, np.int64)
+        esc = np.zeros(self.n, np.int64)
+        N.check(self._L.pt_ensemble_counts(self._h, _ptr(live), _ptr(esc)), "pt_ensemble_counts")
+        return live, esc
+
+    def escaped(self, k):
+        """Indices of member k's escaped particles, after synchronising."""
+        n = C.c_int64()
+        N.check(self._L.pt_ensemble_escaped(self._h, int(k), None, 0, C.byref(n)), "pt_ensemble_escaped")
+        out = np.zeros(n.value, np.int32)
+        N.check(self._L.pt_ensemble_escaped(self._h, int(k), _ptr(out), out.size, C.byref(n)),
+                "pt_ensemble_escaped")
+        return out
+
+    def check(self) -> int:
+        return int(self._L.pt_ensemble_check(self._h))
+
+    def close(self):
+        if self._h:
+            self._L.pt_ensemble_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

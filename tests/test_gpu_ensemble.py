@@ -1,0 +1,104 @@
+"""Ensembles: several snapshots, tolerances and particle sets in one
+persistent launch per window, work-list compaction with escaped-particle
+lists, and CUDA-graph capture of a window sequence.
+
+Every member of an exact-FP64 ensemble must reproduce, bit for bit, the CPU
+oracle run of that member alone (windows continue trajectories bit for bit,
+and a particle's arithmetic does not depend on which lane or launch runs it).
+"""
+import numpy as np
+import pytest
+
+from conftest import small_problem
+
+pytestmark = pytest.mark.gpu
+
+T0 = 2.0 * np.pi / 200.0
+
+
+def _members(torch, precision, method="dop853"):
+    from particles_gb300 import Fields
+    specs = [  # grid, particles, tolerance, open x
+        dict(n=12, npart=150, tol=1e-7, open_x=False, seed=51),
+        dict(n=16, npart=300, tol=1e-9, open_x=True, seed=52),
+        dict(n=20, npart=600, tol=1e-8, open_x=True, seed=53),
+    ]
+    probs, members = [], []
+    for sp in specs:
+        pr = small_problem(method, n=sp["n"], npart=sp["npart"], periods=1.0, seed=sp["seed"],
+                           tol=sp["tol"])
+        pr["open_x"] = sp["open_x"]
+        uu, bb = pr["fields"]
+        f = Fields(uu, bb, precision=precision)
+        npart = pr["state"].shape[0]
+        members.append(dict(
+            fields=f, params=pr["params"], open_x=sp["open_x"],
+            time=torch.tensor(pr["time"], device="cuda"),
+            state=torch.tensor(pr["state"], device="cuda"),
+            cnt=torch.zeros((npart, 3), dtype=torch.int64, device="cuda"),
+            status=torch.zeros(npart, dtype=torch.int32, device="cuda"),
+            carry=torch.zeros(int(f._L.pt_carry_bytes(npart)), dtype=torch.uint8, device="cuda")))
+        probs.append(pr)
+    return probs, members
+
+
+@pytest.mark.parametrize("method", ["rk5", "dop853"])
+def test_ensemble_exact_matches_oracle_per_member(cuda, oracle_lib, method):
+    torch = cuda
+    import oracle
+    from particles_gb300 import Ensemble
+    probs, members = _members(torch, "fp64", method)
+    ens = Ensemble(method, members, precision="fp64")
+    live_hist = []
+    for w in range(1, 6):
+        ens.run(w * 0.25 * T0)                  # the last window runs to tmax
+        torch.cuda.synchronize()
+        live_hist.append(ens.counts()[0].copy())
+    assert ens.check() == 0
+    live, esc = ens.counts()
+    assert (live == 0).all()                    # every particle done or escaped
+    assert (np.diff(np.array(live_hist), axis=0) <= 0).all()   # lists only shrink
+    for k, (pr, mb) in enumerate(zip(probs, members)):
+        uu, bb = pr["fields"]
+        so, co, sto = oracle.integrate(method, pr["params"], pr["time"], uu, bb,
+                                       pr["state"].copy(), open_x=pr["open_x"])
+        st = mb["status"].cpu().numpy()
+        assert np.array_equal(st, sto), k
+        assert np.array_equal(mb["cnt"].cpu().numpy(), co), k
+        assert np.array_equal(mb["state"].cpu().numpy(), so), k
+        escaped = np.sort(ens.escaped(k))
+        assert np.array_equal(escaped, np.flatnonzero(sto == 2)), k
+        assert esc[k] == escaped.size
+        if pr["open_x"]:
+            assert escaped.size > 0
+    ens.close()
+
+
+def test_ensemble_graph_replay_equals_stepwise(cuda):
+    """Mixed precision: a captured sequence of windows gives the same bits as
+    the same windows launched one by one."""
+    torch = cuda
+    from particles_gb300 import Ensemble
+    outs = []
+    for use_graph in (False, True):
+        probs, members = _members(torch, "fp32", "rk5")
+        ens = Ensemble("rk5", members, precision="fp32")
+        stream = torch.cuda.Stream()
+        if use_graph:
+            ens.capture(4, 0.25 * T0, stream=stream.cuda_stream)
+            ens.replay(stream=stream.cuda_stream)
+            ens.run(0.0, stream=stream.cuda_stream)            # the rest of the run
+        else:
+            for w in range(1, 5):
+                ens.run(w * 0.25 * T0, stream=stream.cuda_stream)
+            ens.run(0.0, stream=stream.cuda_stream)
+        stream.synchronize()
+        assert ens.check() == 0
+        live, esc = ens.counts()
+        assert (live == 0).all() and esc.sum() > 0
+        outs.append([(m["state"].cpu().numpy(), m["cnt"].cpu().numpy(), m["status"].cpu().numpy())
+                     for m in members])
+        ens.close()
+    for a, b in zip(outs[0], outs[1]):
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)

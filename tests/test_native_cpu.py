@@ -92,3 +92,19 @@ def test_launch_variant_option_checked_on_host(native):
         o.blocks_per_sm = v
         assert native.pt_debug_unpack(1, 4, 2, ptr(dm), 0, 0, ptr(p), C.byref(o), ptr(out)) == rc
     assert native.pt_autotune(1, 4, 2, None, ptr(p), None, None, None, None, None, None) == N.PT_ERR_ARG
+
+
+def test_ensemble_argument_errors_need_no_gpu(native):
+    from particles_gb300 import _native as N
+    h = C.c_void_p()
+    assert native.pt_ensemble_create(1, 0, None, None, C.byref(h)) == N.PT_ERR_ARG
+    arr = (N.PtMember * 9)()
+    assert native.pt_ensemble_create(1, 9, C.byref(arr), None, C.byref(h)) == N.PT_ERR_ARG
+    o = N.PtOptions()
+    o.struct_size = C.sizeof(o)
+    o.controller = 1
+    assert native.pt_ensemble_create(1, 1, C.byref(arr), C.byref(o), C.byref(h)) == N.PT_ERR_UNSUPPORTED
+    assert native.pt_ensemble_create(1, 1, C.byref(arr), None, C.byref(h)) == N.PT_ERR_ARG  # no fields
+    assert native.pt_ensemble_run(None, 1.0, None) == N.PT_ERR_ARG
+    assert native.pt_ensemble_replay(None, None) == N.PT_ERR_ARG
+    assert native.pt_ensemble_destroy(None) == N.PT_OK
