@@ -9,6 +9,7 @@
  * Nothing here calls a CPU fallback: without a usable GPU every entry point
  * returns PT_ERR_CUDA.
  */
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -65,6 +66,10 @@ struct pt_fields {
     double *rec64;              /* FP64 records (PT_PREC_FP64, PT_PREC_FP64_FMA) */
     float *rec32;               /* FP32 records (PT_PREC_FP32) */
     int32_t nc32;               /* FP32 record width: 8 or 12 */
+    uint4 *rec16;               /* BF16 brick records (PT_PREC_BF16) */
+    float *bscale;              /* per brick: offsets and scales (16 or 24 floats) */
+    int32_t nb[3];              /* bricks per axis */
+    int32_t nc16;               /* BF16 record width: 8 or 16 */
     int64_t bytes;
     unsigned long long *scratch;   /* [0] queue head, [1] flags (2 x int32) */
 };
@@ -105,6 +110,82 @@ __global__ void k_pack_records32(int64_t nn, const double *__restrict__ uu,
     }
 }
 
+/* Planar reference layout -> BF16 8^3 bricks with a one-node halo on the
+ * high faces (9^3 records per brick; record (lx, ly, lz) of brick (bx, by,
+ * bz) holds node ((8 bx + lx) mod d0, ...)), one block of 768 threads per
+ * brick, one thread per record.  Per component the brick's offset is the
+ * midpoint and its scale the half-range of the component over the records a
+ * stencil can reach (8 b + l <= d on every axis), both rounded to FP32; a
+ * record stores q = (v - offset) / scale rounded to BF16 (|q| <= 1). */
+template <int NV>
+__global__ void __launch_bounds__(768) k_pack_bricks16(int32_t d0, int32_t d1, int32_t d2,
+                                                       int32_t nbx, int32_t nby,
+                                                       const double *__restrict__ uu,
+                                                       const double *__restrict__ bb,
+                                                       const double *__restrict__ jj,
+                                                       uint4 *__restrict__ rec,
+                                                       float *__restrict__ bscale)
+{
+    constexpr int NC16 = (NV == 9) ? 16 : 8, NS = (NV == 9) ? 20 : 12;
+    __shared__ double smin[24][NV], smax[24][NV];
+    __shared__ float soff[NV], ssc[NV];
+    const int64_t b = blockIdx.x;
+    const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((int64_t)nbx * nby));
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int lx = t % 9, ly = (t / 9) % 9, lz = t / 81;
+    const int gi = bx * 8 + lx, gj = by * 8 + ly, gk = bz * 8 + lz;
+    const bool slot = t < 729;
+    const bool reach = slot && gi <= d0 && gj <= d1 && gk <= d2;
+    const int i = gi % d0, j = gj % d1, k = gk % d2;
+    const int64_t nn = (int64_t)d0 * d1 * d2;
+    const int64_t g = i + (int64_t)d0 * (j + (int64_t)d1 * k);
+    double v[NV];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        v[c] = reach ? uu[g + c * nn] : 0.0;
+        v[3 + c] = reach ? bb[g + c * nn] : 0.0;
+        if (NV == 9) v[(6 + c) % NV] = reach ? jj[g + c * nn] : 0.0;
+    }
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        double mn = reach ? v[c] : INFINITY, mx = reach ? v[c] : -INFINITY;
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        }
+        if (lane == 0) { smin[warp][c] = mn; smax[warp][c] = mx; }
+    }
+    __syncthreads();
+    if (t < NV) {
+        double mn = smin[0][t], mx = smax[0][t];
+        for (int w = 1; w < 24; ++w) { mn = fmin(mn, smin[w][t]); mx = fmax(mx, smax[w][t]); }
+        const float off = (float)(0.5 * (mn + mx));
+        float sc = (float)(0.5 * (mx - mn));
+        if (!(sc > 0.0f)) sc = 1.0f;
+        soff[t] = off;
+        ssc[t] = sc;
+        bscale[b * NS + 2 * t] = off;
+        bscale[b * NS + 2 * t + 1] = sc;
+    } else if (t >= 2 * NV && t < NS) {
+        bscale[b * NS + t] = 0.0f;
+    }
+    __syncthreads();
+    if (!slot) return;
+    unsigned short q[NC16];
+#pragma unroll
+    for (int c = 0; c < NC16; ++c) q[c] = 0;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        const float x = reach ? (float)((v[c] - (double)soff[c]) / (double)ssc[c]) : 0.0f;
+        q[c] = __bfloat16_as_ushort(__float2bfloat16_rn(x));
+    }
+    uint4 *o = rec + (b * 729 + t) * (NC16 / 8);
+#pragma unroll
+    for (int w = 0; w < NC16 / 8; ++w)
+        o[w] = make_uint4(q[8 * w] | ((uint32_t)q[8 * w + 1] << 16), q[8 * w + 2] | ((uint32_t)q[8 * w + 3] << 16),
+                          q[8 * w + 4] | ((uint32_t)q[8 * w + 5] << 16), q[8 * w + 6] | ((uint32_t)q[8 * w + 7] << 16));
+}
+
 static bool dims_ok(const int32_t dm[3])
 {
     if (!dm) return false;
@@ -122,7 +203,8 @@ static int fields_create_impl(const int32_t dm[3], const double *uu, const doubl
     *out = nullptr;
     if (!dims_ok(dm)) return set_err(PT_ERR_ARG, "pt_fields_create: bad dm%s");
     if (!uu || !bb) return set_err(PT_ERR_ARG, "pt_fields_create: uu/bb is NULL%s");
-    if (precision != PT_PREC_FP64 && precision != PT_PREC_FP64_FMA && precision != PT_PREC_FP32)
+    if (precision != PT_PREC_FP64 && precision != PT_PREC_FP64_FMA && precision != PT_PREC_FP32 &&
+        precision != PT_PREC_BF16)
         return set_err(PT_ERR_UNSUPPORTED, "pt_fields_create: precision not built%s");
 
     int rc = PT_OK;
@@ -135,10 +217,18 @@ static int fields_create_impl(const int32_t dm[3], const double *uu, const doubl
     f->has_j = jj != nullptr;
     f->nc = f->has_j ? 10 : 6;
     f->nc32 = f->has_j ? 12 : 8;
+    f->nc16 = f->has_j ? 16 : 8;
+    for (int i = 0; i < 3; ++i) f->nb[i] = (dm[i] + 7) / 8;
     f->nodes = nn;
     PT_CU(cudaGetDevice(&f->device));
     PT_CU(cudaMalloc(&f->scratch, 256));
-    if (precision == PT_PREC_FP32) {
+    if (precision == PT_PREC_BF16) {
+        const int64_t nbk = (int64_t)f->nb[0] * f->nb[1] * f->nb[2];
+        const int ns = f->has_j ? 20 : 12;
+        PT_CU(cudaMalloc(&f->rec16, (size_t)nbk * 729 * f->nc16 * 2));
+        PT_CU(cudaMalloc(&f->bscale, (size_t)nbk * ns * sizeof(float)));
+        f->bytes = nbk * 729 * f->nc16 * 2 + nbk * ns * 4 + 256;
+    } else if (precision == PT_PREC_FP32) {
         PT_CU(cudaMalloc(&f->rec32, (size_t)nn * f->nc32 * sizeof(float)));
         f->bytes = (int64_t)nn * f->nc32 * sizeof(float) + 256;
     } else {
@@ -162,7 +252,14 @@ static int fields_create_impl(const int32_t dm[3], const double *uu, const doubl
     {
         int64_t blocks = (nn + 255) / 256;
         if (blocks > 65536) blocks = 65536;
-        if (precision == PT_PREC_FP32)
+        const int64_t nbk = (int64_t)f->nb[0] * f->nb[1] * f->nb[2];
+        if (precision == PT_PREC_BF16 && f->has_j)
+            k_pack_bricks16<9><<<(unsigned)nbk, 768, 0, stream>>>(dm[0], dm[1], dm[2], f->nb[0], f->nb[1],
+                                                                  d_uu, d_bb, d_jj, f->rec16, f->bscale);
+        else if (precision == PT_PREC_BF16)
+            k_pack_bricks16<6><<<(unsigned)nbk, 768, 0, stream>>>(dm[0], dm[1], dm[2], f->nb[0], f->nb[1],
+                                                                  d_uu, d_bb, d_jj, f->rec16, f->bscale);
+        else if (precision == PT_PREC_FP32)
             k_pack_records32<<<(int)blocks, 256, 0, stream>>>(nn, d_uu, d_bb, d_jj, f->nc32, f->rec32);
         else
             k_pack_records64<<<(int)blocks, 256, 0, stream>>>(nn, d_uu, d_bb, d_jj, f->nc, f->rec64);
@@ -178,6 +275,8 @@ done:
     if (rc != PT_OK) {
         cudaFree(f->rec64);
         cudaFree(f->rec32);
+        cudaFree(f->rec16);
+        cudaFree(f->bscale);
         cudaFree(f->scratch);
         delete f;
         return rc;
@@ -204,6 +303,8 @@ extern "C" int pt_fields_destroy(pt_fields *f)
     if (!f) return PT_OK;
     cudaFree(f->rec64);
     cudaFree(f->rec32);
+    cudaFree(f->rec16);
+    cudaFree(f->bscale);
     cudaFree(f->scratch);
     delete f;
     return PT_OK;
@@ -350,8 +451,21 @@ static cudaError_t launch_run(int32_t method, const pt_fields *f, const PtRun &R
         return method == PT_METHOD_RK5 ? pt_launch_rk5_exact(R, f->nc, s) : pt_launch_dp853_exact(R, f->nc, s);
     if (f->precision == PT_PREC_FP64_FMA)
         return method == PT_METHOD_RK5 ? pt_launch_rk5_fma(R, f->nc, s) : pt_launch_dp853_fma(R, f->nc, s);
+    if (f->precision == PT_PREC_BF16)
+        return method == PT_METHOD_RK5 ? pt_launch_rk5_bf16(R, f->nc16, s)
+                                       : pt_launch_dp853_bf16(R, f->nc16, s);
     return method == PT_METHOD_RK5 ? pt_launch_rk5_mixed(R, f->nc32, s)
                                    : pt_launch_dp853_mixed(R, f->nc32, s);
+}
+
+/* The device pointers of a field handle in a run. */
+static void attach_fields(const pt_fields *f, PtRun &R)
+{
+    R.fld = f->rec64;
+    R.fld32 = f->rec32;
+    R.fld16 = f->rec16;
+    R.bscale = f->bscale;
+    for (int i = 0; i < 3; ++i) R.nb[i] = f->nb[i];
 }
 
 static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
@@ -363,8 +477,9 @@ static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
     PtRun R;
     int rc = prepare_run(method, np, m, shape_of(f), params, opt, R);
     if (rc != PT_OK) return rc;
-    R.fld = f->rec64;
-    R.fld32 = f->rec32;
+    if (f->precision == PT_PREC_BF16 && (R.mlp || R.rec))
+        return set_err(PT_ERR_UNSUPPORTED, "the learned controller and step records need FP32 or FP64 fields%s");
+    attach_fields(f, R);
     R.time = d_time;
     R.state = d_state;
     R.cnt = d_cnt;
@@ -398,6 +513,8 @@ extern "C" int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_field
     PtRun R;
     int rc = prepare_run(method, np, m, shape_of(f), params, opt, R);
     if (rc != PT_OK) return rc;
+    if (f->precision == PT_PREC_BF16 && (R.mlp || R.rec))
+        return set_err(PT_ERR_UNSUPPORTED, "the learned controller and step records need FP32 or FP64 fields%s");
     cudaStream_t s = (cudaStream_t)stream;
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -427,8 +544,7 @@ extern "C" int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_field
     R.order = nullptr;
     R.rec = t_rec;
     R.rec_cap = 0;
-    R.fld = f->rec64;
-    R.fld32 = f->rec32;
+    attach_fields(f, R);
     R.queue = f->scratch;
     R.flags = reinterpret_cast<int32_t *>(f->scratch + 1);
     if (!(opt && opt->max_steps > 0)) R.max_steps = 32;
@@ -677,8 +793,7 @@ extern "C" int pt_debug_accel(const pt_fields *f, int64_t n, const double params
     PtRun R;
     RunShape g = shape_of(f);
     unpack_params(params, g, R);
-    R.fld = f->rec64;
-    R.fld32 = f->rec32;
+    attach_fields(f, R);
     R.has_j = f->has_j;
     R.eta = 0.0;
     cudaError_t e;
@@ -686,8 +801,10 @@ extern "C" int pt_debug_accel(const pt_fields *f, int64_t n, const double params
         e = pt_launch_accel_exact(R, f->nc, n, d_vec, d_acc, (cudaStream_t)stream);
     else if (f->precision == PT_PREC_FP64_FMA)
         e = pt_launch_accel_fma(R, f->nc, n, d_vec, d_acc, (cudaStream_t)stream);
+    else if (f->precision == PT_PREC_BF16)
+        e = pt_launch_accel_mixed(R, f->nc16, 1, n, d_vec, d_acc, (cudaStream_t)stream);
     else
-        e = pt_launch_accel_mixed(R, f->nc32, n, d_vec, d_acc, (cudaStream_t)stream);
+        e = pt_launch_accel_mixed(R, f->nc32, 0, n, d_vec, d_acc, (cudaStream_t)stream);
     return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_accel");
 }
 
@@ -879,6 +996,10 @@ static cudaError_t ens_launch(const pt_ensemble *e, int64_t ntot, cudaStream_t s
         return e->method == PT_METHOD_RK5
                    ? pt_launch_rk5_ens_fma(e->d_tab, e->nmem, e->nc, e->minb, ntot, s)
                    : pt_launch_dp853_ens_fma(e->d_tab, e->nmem, e->nc, e->minb, ntot, s);
+    if (e->precision == PT_PREC_BF16)
+        return e->method == PT_METHOD_RK5
+                   ? pt_launch_rk5_ens_bf16(e->d_tab, e->nmem, e->nc, e->minb, ntot, s)
+                   : pt_launch_dp853_ens_bf16(e->d_tab, e->nmem, e->nc, e->minb, ntot, s);
     return e->method == PT_METHOD_RK5
                ? pt_launch_rk5_ens_mixed(e->d_tab, e->nmem, e->nc, e->minb, ntot, s)
                : pt_launch_dp853_ens_mixed(e->d_tab, e->nmem, e->nc, e->minb, ntot, s);
@@ -952,7 +1073,7 @@ extern "C" int pt_ensemble_create(int32_t method, int32_t nmembers, const pt_mem
     memset(&e->B, 0, sizeof e->B);
     e->method = method;
     e->precision = prec;
-    e->nc = prec == PT_PREC_FP32 ? f0->nc32 : f0->nc;
+    e->nc = prec == PT_PREC_FP32 ? f0->nc32 : (prec == PT_PREC_BF16 ? f0->nc16 : f0->nc);
     e->nmem = nmembers;
     e->ntot = ntot;
     e->npmax = npmax;
@@ -979,8 +1100,7 @@ extern "C" int pt_ensemble_create(int32_t method, int32_t nmembers, const pt_mem
         e->B.base[k] = off;
         e->B.np[k] = M.np;
         e->B.status[k] = M.status;
-        R.fld = M.fields->rec64;
-        R.fld32 = M.fields->rec32;
+        attach_fields(M.fields, R);
         R.time = M.time;
         R.state = M.state;
         R.cnt = M.cnt;

@@ -46,6 +46,9 @@ struct PtRun {
     /* device pointers */
     const double *fld;     /* FP64 records */
     const float *fld32;    /* FP32 records (mixed precision) */
+    const uint4 *fld16;    /* BF16 brick records (PT_PREC_BF16) */
+    const float *bscale;   /* per brick: FP32 offsets then scales of each component */
+    int32_t nb[3];         /* bricks per axis, ceil(dm / 8) */
     const double *time;
     double *state;
     int64_t *cnt;
@@ -163,7 +166,13 @@ cudaError_t pt_launch_rk5_ens_mixed(const PtRun *tab, int nmem, int nc, int minb
 cudaError_t pt_launch_dp853_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
                                       cudaStream_t s);
 cudaError_t pt_launch_dp853_mixed(const PtRun &P, int nc, cudaStream_t s);
-cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int64_t n, const double *vec,
+cudaError_t pt_launch_rk5_bf16(const PtRun &P, int nc, cudaStream_t s);
+cudaError_t pt_launch_dp853_bf16(const PtRun &P, int nc, cudaStream_t s);
+cudaError_t pt_launch_rk5_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
+                                   cudaStream_t s);
+cudaError_t pt_launch_dp853_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
+                                     cudaStream_t s);
+cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int brick, int64_t n, const double *vec,
                                   double *acc, cudaStream_t s);
 
 cudaError_t pt_launch_debug_pow(int64_t n, const double *x, const double *y, double *out,

@@ -1,11 +1,11 @@
 /*
- * pt_mixed.cu -- mixed-precision fused integrators (PT_PREC_FP32).
+ * pt_mixed.cu -- mixed-precision fused integrators (PT_PREC_FP32, PT_PREC_BF16).
  *
  * The step machine of pt_integrator.cuh keeps everything that accumulates in
  * FP64: the particle state si/sf, every stage sum, the embedded error norm,
  * the step-size controller and the dense output.  Only the evaluation f(s)
- * changes: the field records are FP32 and the trilinear gather and the
- * Lorentz force run in FP32 (128 FMA/clk/SM on GB300 against 2 DP ops/clk/SM).
+ * changes: the trilinear gather and the Lorentz force run in FP32 (128
+ * FMA/clk/SM on GB300 against 2 DP ops/clk/SM).
  *
  * f(s) in FP32 (same physics as accelerations.F90:59-96 with
  * interpolations.F90:104-226):
@@ -20,8 +20,14 @@
  *     integer pipe (pt_convert.cuh), so an evaluation issues no FP64-pipe
  *     instruction at all (the exact FP64 evaluation issues ~290).
  *
- * Field records (HBM): 8 floats {Ux,Uy,Uz,Bx,By,Bz,0,0} = one 32-B sector per
- * node, or 12 floats {U,B,J,0,0,0} = 48 B with eta J; x-fastest node order.
+ * Field stores (HBM), chosen by the gather policy:
+ *   GatherF32:   8 floats {Ux,Uy,Uz,Bx,By,Bz,0,0} = one 32-B sector per node,
+ *                or 12 floats {U,B,J,0,0,0} = 48 B with eta J; x-fastest.
+ *   GatherBrick: 8^3-node bricks stored with a one-node halo on their high
+ *                faces (9^3 records, bricks x-fastest, records x-fastest),
+ *                one record of 8 BF16 {U,B,0,0} = 16 B per node, or 16 BF16
+ *                {U,B,J,0...} = 32 B with J; per brick and component an FP32
+ *                offset and scale, value = offset + scale * q.
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -37,25 +43,97 @@
 
 namespace {
 
+/* Trilinear sums of FP32 node records: acc[c] = sum_q w8[q] rec(node q)[c]. */
 template <int NC>
-__device__ __forceinline__ void load_rec32(const float *__restrict__ fld, int64_t node, float v[NC])
-{
-    const float4 *q = reinterpret_cast<const float4 *>(fld + node * NC);
+struct GatherF32 {
+    static constexpr int NV = (NC == 12) ? 9 : 6;
+    static constexpr int NCR = NC;            /* record width for the feature gather */
+    static __device__ __forceinline__ void load(const float *__restrict__ fld, int64_t node,
+                                                float v[NC])
+    {
+        const float4 *q = reinterpret_cast<const float4 *>(fld + node * NC);
 #pragma unroll
-    for (int i = 0; i < NC / 4; ++i) {
-        const float4 x = __ldg(q + i);
-        v[4 * i] = x.x;
-        v[4 * i + 1] = x.y;
-        v[4 * i + 2] = x.z;
-        v[4 * i + 3] = x.w;
+        for (int i = 0; i < NC / 4; ++i) {
+            const float4 x = __ldg(q + i);
+            v[4 * i] = x.x;
+            v[4 * i + 1] = x.y;
+            v[4 * i + 2] = x.z;
+            v[4 * i + 3] = x.w;
+        }
     }
-}
+    static __device__ __forceinline__ void gather(const PtRun &P, const int32_t l[3],
+                                                  const int32_t r[3], const float w8[8],
+                                                  float acc[NV])
+    {
+        const int64_t d1 = P.dm[0], d12 = (int64_t)P.dm[0] * P.dm[1];
+        const int64_t yl = d1 * l[1], yr = d1 * r[1], zl = d12 * l[2], zr = d12 * r[2];
+        const int64_t node[8] = { l[0] + yl + zl, l[0] + yl + zr, l[0] + yr + zl, l[0] + yr + zr,
+                                  r[0] + yl + zl, r[0] + yl + zr, r[0] + yr + zl, r[0] + yr + zr };
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            float v[NC];
+            load(P.fld32, node[q], v);
+#pragma unroll
+            for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * v[cc] : fmaf(w8[q], v[cc], acc[cc]);
+        }
+    }
+};
 
-template <int NC>
-struct EvalF32 {
+/* Trilinear sums over BF16 bricks.  A brick holds the 8^3 nodes it owns
+ * plus a one-node halo on its high faces (9^3 records: node (l + 1) mod dm of
+ * the last owned node), so every stencil -- left corner l, right corner the
+ * periodic neighbour (l + 1) mod dm -- lies inside the brick of l.  Each
+ * brick stores per component an FP32 offset and scale: value = offset +
+ * scale * q, so the trilinear sum is offset + scale * sum_q w_q q_q. */
+template <int NC16>
+struct GatherBrick {
+    static constexpr int NV = (NC16 == 16) ? 9 : 6;
+    static constexpr int NCR = 8;             /* unused: no learned controller on bricks */
+    static constexpr int NS = (NC16 == 16) ? 20 : 12;   /* floats per brick: (offset, scale) pairs */
+    static __device__ __forceinline__ float lo(uint32_t w) { return __uint_as_float(w << 16); }
+    static __device__ __forceinline__ float hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
+    static __device__ __forceinline__ void load_node(const uint4 *__restrict__ fld, int64_t node,
+                                                     float v[NV])
+    {
+        const uint4 a = __ldg(fld + node * (NC16 / 8));
+        v[0] = lo(a.x); v[1] = hi(a.x); v[2] = lo(a.y);
+        v[3] = hi(a.y); v[4] = lo(a.z); v[5] = hi(a.z);
+        if (NV == 9) {
+            v[6 % NV] = lo(a.w); v[7 % NV] = hi(a.w);
+            const uint4 b = __ldg(fld + node * (NC16 / 8) + 1);
+            v[8 % NV] = lo(b.x);
+        }
+    }
+    static __device__ __forceinline__ void gather(const PtRun &P, const int32_t l[3],
+                                                  const int32_t *, const float w8[8], float acc[NV])
+    {
+        const int64_t b = (l[0] >> 3) + (int64_t)P.nb[0] * ((l[1] >> 3) + (int64_t)P.nb[1] * (l[2] >> 3));
+        const int64_t base = b * 729 + (l[0] & 7) + 9 * (l[1] & 7) + 81 * (l[2] & 7);
+        float sum[NV];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            float v[NV];
+            load_node(P.fld16, base + ((q & 4) ? 1 : 0) + ((q & 2) ? 9 : 0) + ((q & 1) ? 81 : 0), v);
+#pragma unroll
+            for (int c = 0; c < NV; ++c) sum[c] = (q == 0) ? w8[0] * v[c] : fmaf(w8[q], v[c], sum[c]);
+        }
+        const float4 *sp = reinterpret_cast<const float4 *>(P.bscale + b * NS);
+        float os[NS];
+#pragma unroll
+        for (int i = 0; i < NS / 4; ++i) {
+            const float4 x = __ldg(sp + i);
+            os[4 * i] = x.x; os[4 * i + 1] = x.y; os[4 * i + 2] = x.z; os[4 * i + 3] = x.w;
+        }
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] = fmaf(os[2 * c + 1], sum[c], os[2 * c]);
+    }
+};
+
+template <class G>
+struct EvalMixed {
     static constexpr bool kDelta = true;
     using Rec = float;
-    static constexpr int NCR = NC;
+    static constexpr int NCR = G::NCR;
     static __device__ __forceinline__ const float *records(const PtRun &P) { return P.fld32; }
     /* Cell of si and the offset of si inside it (FP32), fixed for one attempt. */
     struct Origin {
@@ -81,7 +159,7 @@ struct EvalF32 {
     static __device__ __forceinline__ void f(const PtRun &P, const double s[6], const double d[6],
                                              const Origin &O, double a[6])
     {
-        constexpr int NV = (NC == 12) ? 9 : 6;
+        constexpr int NV = G::NV;
         int32_t l[3], r[3];
         float xd[3], xu[3];
 #pragma unroll
@@ -105,18 +183,8 @@ struct EvalF32 {
         const float pdu = xd[0] * xu[1], pdd = xd[0] * xd[1];
         const float w8[8] = { puu * xu[2], puu * xd[2], pud * xu[2], pud * xd[2],
                               pdu * xu[2], pdu * xd[2], pdd * xu[2], pdd * xd[2] };
-        const int64_t d1 = P.dm[0], d12 = (int64_t)P.dm[0] * P.dm[1];
-        const int64_t yl = d1 * l[1], yr = d1 * r[1], zl = d12 * l[2], zr = d12 * r[2];
-        const int64_t node[8] = { l[0] + yl + zl, l[0] + yl + zr, l[0] + yr + zl, l[0] + yr + zr,
-                                  r[0] + yl + zl, r[0] + yl + zr, r[0] + yr + zl, r[0] + yr + zr };
         float acc[NV];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            float v[NC];
-            load_rec32<NC>(P.fld32, node[q], v);
-#pragma unroll
-            for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * v[cc] : fmaf(w8[q], v[cc], acc[cc]);
-        }
+        G::gather(P, l, r, w8, acc);
         const float ux = pt_d2f(s[3]), uy = pt_d2f(s[4]), uz = pt_d2f(s[5]);
         const float g = sqrtf(fmaf(ux, ux, fmaf(uy, uy, fmaf(uz, uz, 1.0f))));
         const float ig = 1.0f / g;
@@ -128,7 +196,7 @@ struct EvalF32 {
         float f3 = w1 * acc[5] - w2 * acc[4];
         float f4 = w2 * acc[3] - w0 * acc[5];
         float f5 = w0 * acc[4] - w1 * acc[3];
-        if (NC == 12) {
+        if (NV == 9) {
             f3 = fmaf(P.etaf, acc[6 % NV], f3);
             f4 = fmaf(P.etaf, acc[7 % NV], f4);
             f5 = fmaf(P.etaf, acc[8 % NV], f5);
@@ -139,24 +207,24 @@ struct EvalF32 {
     }
 };
 
-template <int METHOD, int NC, bool LEARN, int MINB>
+template <int METHOD, class EV, bool LEARN, int MINB>
 __global__ void __launch_bounds__(PT_BLOCK, MINB) k_integrate_mixed(const PtRun P)
 {
-    pt_sm::run_machine<METHOD, EvalF32<NC>, LEARN>(pt_sm::Members<false>{ P });
+    pt_sm::run_machine<METHOD, EV, LEARN>(pt_sm::Members<false>{ P });
 }
 
 /* Several runs (members: snapshots, tolerances, particle sets) in one
  * persistent launch; every lane drains the members' queues in table order. */
-template <int METHOD, int NC, int MINB>
+template <int METHOD, class EV, int MINB>
 __global__ void __launch_bounds__(PT_BLOCK, MINB) k_ensemble_mixed(const PtRun *__restrict__ tab, int nmem)
 {
     __shared__ PtRun sP[PT_ENS_MAX];
     __shared__ int64_t sN[PT_ENS_MAX];
     pt_sm::ens_load(tab, nmem, sP, sN);
-    pt_sm::run_machine<METHOD, EvalF32<NC>, false, true>(pt_sm::Members<true>{ sP, sN, nmem });
+    pt_sm::run_machine<METHOD, EV, false, true>(pt_sm::Members<true>{ sP, sN, nmem });
 }
 
-template <int NC>
+template <class EV>
 __global__ void k_accel_mixed(const PtRun P, int64_t n, const double *vec, double *acc)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -165,61 +233,69 @@ __global__ void k_accel_mixed(const PtRun P, int64_t n, const double *vec, doubl
         const double d[6] = { 0, 0, 0, 0, 0, 0 };
 #pragma unroll
         for (int c = 0; c < 6; ++c) s[c] = vec[6 * i + c];
-        typename EvalF32<NC>::Origin o;
-        EvalF32<NC>::begin(P, s, o);
-        EvalF32<NC>::f(P, s, d, o, a);
+        typename EV::Origin o;
+        EV::begin(P, s, o);
+        EV::f(P, s, d, o, a);
 #pragma unroll
         for (int c = 0; c < 6; ++c) acc[6 * i + c] = a[c];
     }
 }
 
-template <int METHOD, int NC, bool LEARN, int MINB>
+template <int METHOD, class EV, bool LEARN, int MINB>
 cudaError_t launch1(const PtRun &P, cudaStream_t s)
 {
     static int cache[2][2] = { { -1, 1 }, { -1, 1 } };  /* without / with recording */
     const bool rec = LEARN && P.rec != nullptr;
-    return pt_sm::launch_persistent(k_integrate_mixed<METHOD, NC, LEARN, MINB>, PT_BLOCK,
+    return pt_sm::launch_persistent(k_integrate_mixed<METHOD, EV, LEARN, MINB>, PT_BLOCK,
                                     pt_sm::smem_bytes<METHOD>(PT_BLOCK, rec),
                                     pt_sm::smem_bytes<METHOD>(PT_BLOCK, true), cache[rec], P.np, s,
                                     P);
 }
 
-template <int METHOD, int NC, int MINB>
+template <int METHOD, class EV, int MINB>
 cudaError_t launch_ens1(const PtRun *tab, int nmem, int64_t ntot, cudaStream_t s)
 {
     static int cache[2] = { -1, 1 };
     const int smem = pt_sm::smem_bytes<METHOD>(PT_BLOCK, false);
-    return pt_sm::launch_persistent(k_ensemble_mixed<METHOD, NC, MINB>, PT_BLOCK, smem, smem, cache, ntot, s,
-                                    tab, nmem);
+    return pt_sm::launch_persistent(k_ensemble_mixed<METHOD, EV, MINB>, PT_BLOCK, smem, smem, cache,
+                                    ntot, s, tab, nmem);
 }
 
-template <int METHOD, int NC>
+template <int METHOD, class EV>
 cudaError_t launch_ens(const PtRun *tab, int nmem, int minb, int64_t ntot, cudaStream_t s)
 {
     if (ntot == 0) return cudaSuccess;          /* ntot < 0: configure only */
     switch (minb) {
-    case 2: return launch_ens1<METHOD, NC, 2>(tab, nmem, ntot, s);
-    case 4: return launch_ens1<METHOD, NC, 4>(tab, nmem, ntot, s);
-    default: return launch_ens1<METHOD, NC, 3>(tab, nmem, ntot, s);
+    case 2: return launch_ens1<METHOD, EV, 2>(tab, nmem, ntot, s);
+    case 4: return launch_ens1<METHOD, EV, 4>(tab, nmem, ntot, s);
+    default: return launch_ens1<METHOD, EV, 3>(tab, nmem, ntot, s);
     }
 }
 
-template <int METHOD, int NC, bool LEARN>
+template <int METHOD, class EV, bool LEARN>
 cudaError_t launch_v(const PtRun &P, cudaStream_t s)
 {
     switch (P.minb) {
-    case 2: return launch1<METHOD, NC, LEARN, 2>(P, s);
-    case 4: return launch1<METHOD, NC, LEARN, 4>(P, s);
-    default: return launch1<METHOD, NC, LEARN, 3>(P, s);
+    case 2: return launch1<METHOD, EV, LEARN, 2>(P, s);
+    case 4: return launch1<METHOD, EV, LEARN, 4>(P, s);
+    default: return launch1<METHOD, EV, LEARN, 3>(P, s);
     }
 }
 
-template <int METHOD, int NC>
+/* LEARNABLE: the store supports the learned controller's feature gather
+ * (FP32 records); BF16 bricks run the classical controller only. */
+template <int METHOD, class EV, bool LEARNABLE>
 cudaError_t launch(const PtRun &P, cudaStream_t s)
 {
     if (P.np <= 0) return cudaSuccess;
-    return (P.mlp || P.rec) ? launch_v<METHOD, NC, true>(P, s) : launch_v<METHOD, NC, false>(P, s);
+    if (LEARNABLE && (P.mlp || P.rec)) return launch_v<METHOD, EV, LEARNABLE>(P, s);
+    return launch_v<METHOD, EV, false>(P, s);
 }
+
+using F32_8 = EvalMixed<GatherF32<8>>;
+using F32_12 = EvalMixed<GatherF32<12>>;
+using B16_8 = EvalMixed<GatherBrick<8>>;
+using B16_16 = EvalMixed<GatherBrick<16>>;
 
 }  // namespace
 
@@ -228,40 +304,73 @@ cudaError_t launch(const PtRun &P, cudaStream_t s)
 #if PT_PART != 2
 cudaError_t pt_launch_rk5_mixed(const PtRun &P, int nc, cudaStream_t s)
 {
-    return nc == 12 ? launch<PT_METHOD_RK5, 12>(P, s) : launch<PT_METHOD_RK5, 8>(P, s);
+    return nc == 12 ? launch<PT_METHOD_RK5, F32_12, true>(P, s) : launch<PT_METHOD_RK5, F32_8, true>(P, s);
 }
 
 cudaError_t pt_launch_rk5_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
                                     cudaStream_t s)
 {
-    return nc == 12 ? launch_ens<PT_METHOD_RK5, 12>(tab, nmem, minb, ntot, s)
-                    : launch_ens<PT_METHOD_RK5, 8>(tab, nmem, minb, ntot, s);
+    return nc == 12 ? launch_ens<PT_METHOD_RK5, F32_12>(tab, nmem, minb, ntot, s)
+                    : launch_ens<PT_METHOD_RK5, F32_8>(tab, nmem, minb, ntot, s);
+}
+
+cudaError_t pt_launch_rk5_bf16(const PtRun &P, int nc, cudaStream_t s)
+{
+    return nc == 16 ? launch<PT_METHOD_RK5, B16_16, false>(P, s) : launch<PT_METHOD_RK5, B16_8, false>(P, s);
+}
+
+cudaError_t pt_launch_rk5_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
+                                   cudaStream_t s)
+{
+    return nc == 16 ? launch_ens<PT_METHOD_RK5, B16_16>(tab, nmem, minb, ntot, s)
+                    : launch_ens<PT_METHOD_RK5, B16_8>(tab, nmem, minb, ntot, s);
 }
 #endif
 
 #if PT_PART != 1
 cudaError_t pt_launch_dp853_mixed(const PtRun &P, int nc, cudaStream_t s)
 {
-    return nc == 12 ? launch<PT_METHOD_DOP853, 12>(P, s) : launch<PT_METHOD_DOP853, 8>(P, s);
+    return nc == 12 ? launch<PT_METHOD_DOP853, F32_12, true>(P, s)
+                    : launch<PT_METHOD_DOP853, F32_8, true>(P, s);
 }
 
 cudaError_t pt_launch_dp853_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
                                       cudaStream_t s)
 {
-    return nc == 12 ? launch_ens<PT_METHOD_DOP853, 12>(tab, nmem, minb, ntot, s)
-                    : launch_ens<PT_METHOD_DOP853, 8>(tab, nmem, minb, ntot, s);
+    return nc == 12 ? launch_ens<PT_METHOD_DOP853, F32_12>(tab, nmem, minb, ntot, s)
+                    : launch_ens<PT_METHOD_DOP853, F32_8>(tab, nmem, minb, ntot, s);
+}
+
+cudaError_t pt_launch_dp853_bf16(const PtRun &P, int nc, cudaStream_t s)
+{
+    return nc == 16 ? launch<PT_METHOD_DOP853, B16_16, false>(P, s)
+                    : launch<PT_METHOD_DOP853, B16_8, false>(P, s);
+}
+
+cudaError_t pt_launch_dp853_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
+                                     cudaStream_t s)
+{
+    return nc == 16 ? launch_ens<PT_METHOD_DOP853, B16_16>(tab, nmem, minb, ntot, s)
+                    : launch_ens<PT_METHOD_DOP853, B16_8>(tab, nmem, minb, ntot, s);
 }
 #endif
 
 #if PT_PART != 2
 
-cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int64_t n, const double *vec,
+/* f(vec) of the mixed-precision evaluation: nc = record width of the store
+ * (8 / 12 FP32 records, or 8 / 16 BF16 brick records when brick != 0). */
+cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int brick, int64_t n, const double *vec,
                                   double *acc, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
     const int grid = (int)((n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096);
-    if (nc == 12) k_accel_mixed<12><<<grid, 128, 0, s>>>(P, n, vec, acc);
-    else k_accel_mixed<8><<<grid, 128, 0, s>>>(P, n, vec, acc);
+    if (brick) {
+        if (nc == 16) k_accel_mixed<B16_16><<<grid, 128, 0, s>>>(P, n, vec, acc);
+        else k_accel_mixed<B16_8><<<grid, 128, 0, s>>>(P, n, vec, acc);
+    } else {
+        if (nc == 12) k_accel_mixed<F32_12><<<grid, 128, 0, s>>>(P, n, vec, acc);
+        else k_accel_mixed<F32_8><<<grid, 128, 0, s>>>(P, n, vec, acc);
+    }
     return cudaGetLastError();
 }
 #endif

@@ -74,15 +74,16 @@ def test_ensemble_exact_matches_oracle_per_member(cuda, oracle_lib, method):
     ens.close()
 
 
-def test_ensemble_graph_replay_equals_stepwise(cuda):
-    """Mixed precision: a captured sequence of windows gives the same bits as
-    the same windows launched one by one."""
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_ensemble_graph_replay_equals_stepwise(cuda, precision):
+    """Mixed precision (FP32 records or BF16 bricks): a captured sequence of
+    windows gives the same bits as the same windows launched one by one."""
     torch = cuda
     from particles_gb300 import Ensemble
     outs = []
     for use_graph in (False, True):
-        probs, members = _members(torch, "fp32", "rk5")
-        ens = Ensemble("rk5", members, precision="fp32")
+        probs, members = _members(torch, precision, "rk5")
+        ens = Ensemble("rk5", members, precision=precision)
         stream = torch.cuda.Stream()
         if use_graph:
             ens.capture(4, 0.25 * T0, stream=stream.cuda_stream)
