@@ -55,9 +55,11 @@ WORKLOADS = {
                        v_rms=0.2, eta=1e-3, npart=1 << 20, gamma=(1.001, 1e3), speed=None,
                        tol=1e-10, periods=100, seed=1, window=0.05),
     # the mixed-precision configuration (configuration 3)
+    # windows of 0.1 gyro-periods: the slowest particles need ~100x the mean
+    # attempts of a window, so shorter windows are set by their duration
     "rk5-512": dict(method="rk5", n=512, spectrum="kolmogorov", nmax=32, db_rms=1.0, v_rms=0.2,
                     eta=0.0, npart=1 << 22, gamma=(1.001, 1e2), speed=None, tol=1e-8,
-                    periods=50, seed=2, window=0.02),
+                    periods=50, seed=2, window=0.1),
     # uneven batch in one persistent launch (configuration 4): three snapshots
     "ensemble-3": dict(method="dop853", n=(128, 192, 256), spectrum="kolmogorov", nmax=32,
                        db_rms=(0.5, 1.0, 2.0), v_rms=0.2, eta=0.0, npart=1 << 21,
@@ -68,6 +70,12 @@ WORKLOADS = {
                    eta=0.0, npart=1024, gamma=None, speed=0.5, tol=1e-8, periods=10, seed=0,
                    window=1.0),
 }
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum of one timed full-size window,
+# from a single-pass ncu capture of the same command
+# (profiles/k_integrate_full_size_single_pass.md)
+DRAM_BYTES_PER_WINDOW = {("dop853-256", "fp64"): 27380003072 + 4665027584}
 
 
 def parse():
@@ -335,13 +343,18 @@ class QueueOrder:
             self.order = self.torch.argsort(work, descending=True).to(self.torch.int32)
 
 
-def tune(args, f, method, prm, d_time, d_state, stream, **kw):
+def tune(args, f, method, prm, d_time, d_state, stream, t_stop, **kw):
     """pt_autotune of the kernel the next runs launch (launch variant = resident
-    blocks per SM); the choice becomes that kernel's default."""
+    blocks per SM); the choice becomes that kernel's default.  The trial is
+    the first window itself, on all particles (scratch copies): per-particle
+    work spreads over ~100x within a window, so short capped trials on a
+    sample mispredict the full launch."""
     if args.no_autotune:
         return None
-    v, ms = f.autotune(method, prm, d_time, d_state, stream=stream.cuda_stream, **kw)
-    return {"blocks_per_sm": v, "trial_ms": {str(k): round(t, 3) for k, t in ms.items()}}
+    v, ms = f.autotune(method, prm, d_time, d_state, stream=stream.cuda_stream, t_stop=t_stop,
+                       sample=-1, **kw)
+    return {"blocks_per_sm": v, "trial": "first window, all particles",
+            "trial_ms": {str(k): round(t, 3) for k, t in ms.items()}}
 
 
 def mixed_leg(args, dev, stream):
@@ -388,7 +401,7 @@ def mixed_leg(args, dev, stream):
         f = handles[prec]
         mdl = model if name == "fp32_learned" else None
         st, cnt, status, carry = fresh(npart)
-        launch = tune(args, f, "rk5", prm, d_time, st, stream, model=mdl)
+        launch = tune(args, f, "rk5", prm, d_time, st, stream, window * T0, model=mdl)
         ordq = QueueOrder(torch, cnt, enabled=not args.no_order)
         w = 0
         for _ in range(args.warmup):
@@ -513,7 +526,7 @@ def ensemble_leg(args, dev, stream):
                                               device=dev)))
         keep.append(f)
     launch = tune(args, members[2]["fields"], cfg["method"], members[2]["params"],
-                  members[2]["time"], members[2]["state"], stream)
+                  members[2]["time"], members[2]["state"], stream, cfg["window"] * T0)
     ens = Ensemble(cfg["method"], members, precision=prec)
     win = cfg["window"] * T0
     out = {"workload": "ensemble-3", "grids": ["128^3", "192^3", "256^3"],
@@ -628,7 +641,8 @@ def learned_leg(args, dev, stream):
     snap = (st.clone(), cnt.clone(), carry.clone())
     for name, mdl in (("classical", None), ("learned", model)):
         st.copy_(snap[0]); cnt.copy_(snap[1]); carry.copy_(snap[2])
-        launch = tune(args, f, "dop853", prm, d_time, st, stream, eta=cfg["eta"], model=mdl)
+        launch = tune(args, f, "dop853", prm, d_time, st, stream, window * T0, eta=cfg["eta"],
+                      model=mdl)
         ordq = QueueOrder(torch, cnt, enabled=not args.no_order)
         w = 0
         for _ in range(args.warmup):
@@ -708,7 +722,7 @@ def main():
         d_carry = torch.zeros(int(L.pt_carry_bytes(npart)), dtype=torch.uint8, device=dev)
     stream.synchronize()
 
-    launch = tune(args, f, cfg["method"], prm, d_time, d_state, stream, eta=cfg["eta"])
+    launch = tune(args, f, cfg["method"], prm, d_time, d_state, stream, window * T0, eta=cfg["eta"])
     ordq = QueueOrder(torch, d_cnt, enabled=not args.no_order)
 
     def window_run(w):
@@ -765,8 +779,11 @@ def main():
     pk = C.c_double()
     L.pt_probe_peak(0, 16384, C.byref(pk))
     peak = pk.value
+    traffic = DRAM_BYTES_PER_WINDOW.get((args.workload, args.precision))
     roof = {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,
-            "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+            "unit": "TFLOP/s", "frac": achieved / peak,
+            "traffic": traffic, "traffic_unit": "DRAM bytes per launch (one window)",
+            "traffic_source": "profiles/k_integrate_full_size_single_pass.md" if traffic else None,
             "peak_source": "FP64 FMA peak measured live on this GPU (pt_probe_peak); "
                            "the measured-peaks file lists only HBM and bf16",
             "flops_per_step": flops / args.steps,

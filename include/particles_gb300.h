@@ -94,7 +94,9 @@ typedef struct pt_options {
     int32_t       blocks_per_sm;  /* resident blocks per SM the kernel is compiled for:
                                      2, 3 or 4 (register caps 255, 168, 128); 0 = the
                                      choice of pt_autotune for this kernel, else 3 */
-    int32_t       reserved;
+    int32_t       interpolation;  /* 0: trilinear, interpolate_lin (interpolations.F90:104-226),
+                                     the reference's choice; 1: the node at the lower
+                                     corner of the cell, interpolate_near (:55-83) */
 } pt_options;
 
 /* ---- one-shot, reference-shaped call ----------------------------------- */
@@ -152,16 +154,19 @@ int pt_run_device(int32_t method, int64_t np, int32_t m, const pt_fields *f,
 int pt_run_check(const pt_fields *f);
 
 /* Launch autotuner: times the kernel that pt_run_device would launch with
- * these arguments in each of its launch variants (blocks_per_sm 2, 3, 4) on
- * a sample of the particles -- the first min(np, 2 x 4 x 128 per SM) of them,
- * their first two output rows, max_steps attempts each (opt->max_steps, else
- * 32), on scratch copies -- and makes the fastest the default
- * (blocks_per_sm == 0) of that kernel for the rest of the process.  d_state
- * is only read.  Synchronises the stream.  chosen: the variant (2, 3 or 4);
- * ms_out (host, 3 doubles, or NULL): the trial times of variants 2, 3, 4. */
+ * these arguments in each of its launch variants (blocks_per_sm 2, 3, 4) and
+ * makes the fastest the default (blocks_per_sm == 0) of that kernel family
+ * for the rest of the process.  The trial runs the first `sample` particles
+ * (0: min(np, 2 x 4 x 128 per SM); < 0: all np) from state(:,1,:) on
+ * scratch copies: up to opt->t_stop when it is > 0 -- a real first window,
+ * outliers and tail included -- else max_steps attempts each (opt->max_steps,
+ * else 32).  d_state is only read.  Synchronises the stream.  chosen: the
+ * variant (2, 3 or 4); ms_out (host, 3 doubles, or NULL): the trial times of
+ * variants 2, 3, 4. */
 int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_fields *f,
                 const double params[17], const double *d_time, const double *d_state,
-                const pt_options *opt, void *stream, int32_t *chosen, double ms_out[3]);
+                const pt_options *opt, int64_t sample, void *stream, int32_t *chosen,
+                double ms_out[3]);
 
 /* ---- ensembles: several runs in one persistent launch (no counterpart in
  *      the reference; each member is what one pt_run_device call would do) -- */

@@ -198,6 +198,7 @@ struct Ctx {
     R eta;
     bool has_j;
     bool faithful;
+    bool near;        /* nearest-node gather instead of trilinear */
     Field F;
 };
 
@@ -227,6 +228,7 @@ Ctx<R> make_ctx(const double p[17], const Field &F, double eta, const double *jj
     C.eta = eta;
     C.has_j = (eta != 0.0) && (jj != nullptr);
     C.faithful = faithful;
+    C.near = false;
     return C;
 }
 
@@ -290,7 +292,8 @@ void interp_lin(const Field &F, const R xl[3], const R xs[3], const R pos[3],
 }
 
 template <class R>
-void interp_near(const Field &F, const R xl[3], const R xs[3], const R pos[3], R u[3], R b[3])
+void interp_near(const Field &F, const R xl[3], const R xs[3], const R pos[3], R u[3], R b[3],
+                 R j[3] = nullptr, bool has_j = false)
 {
     int32_t p[3];
     for (int i = 0; i < 3; ++i) {                              /* :76-77 */
@@ -301,6 +304,7 @@ void interp_near(const Field &F, const R xl[3], const R xs[3], const R pos[3], R
     for (int m = 0; m < 3; ++m) {                              /* :79-80 */
         u[m] = F.uu[F.plane * m + o];
         b[m] = F.bb[F.plane * m + o];
+        if (has_j) j[m] = F.jj[F.plane * m + o];               /* extension: J at the node */
     }
 }
 
@@ -312,7 +316,10 @@ template <class R>
 void accel(const Ctx<R> &C, const R vec[6], R acc[6])
 {
     R u[3], b[3], j[3];
-    interp_lin(C.F, C.xl, C.xs, vec, u, b, j, C.has_j);       /* :82 */
+    if (C.near)                                                /* extension: :55-83 */
+        interp_near(C.F, C.xl, C.xs, vec, u, b, j, C.has_j);
+    else
+        interp_lin(C.F, C.xl, C.xs, vec, u, b, j, C.has_j);   /* :82 */
     R s = vec[3] * vec[3] + vec[4] * vec[4] + vec[5] * vec[5];
     R g = r_sqrt(s + 1.0);                                     /* :84 */
     R v[3] = { vec[3] / g, vec[4] / g, vec[5] / g };           /* :85 */
@@ -674,6 +681,7 @@ extern "C" int or_integrate(int32_t method, int64_t np, int32_t m, const int32_t
     if (e.eta != 0.0 && !e.jj) return -3;
     Field F = make_field(dm, uu, bb, e.jj);
     Ctx<double> C = make_ctx<double>(params, F, e.eta, e.jj, e.faithful != 0);
+    C.near = e.near != 0;
     RunOpts O;
     O.open_x = e.open_x;
     O.max_steps = e.max_steps;

@@ -55,6 +55,9 @@ typedef struct or_ext {
     double        t_stop;       /* window end; <= 0 means tmx */
     or_carry     *carry;        /* np entries for resume; NULL = fresh, not saved */
     int32_t      *status;       /* np entries, or NULL */
+    int32_t       near;         /* 1: interpolate_near (interpolations.F90:55-83) in the
+                                   acceleration instead of interpolate_lin */
+    int32_t       pad;
 } or_ext;
 
 /* Batched equivalent of the dispatch loop particles.F90:337-356.

@@ -395,6 +395,10 @@ static int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
             return set_err(PT_ERR_ARG, "negative record capacity%s");
         if (opt->blocks_per_sm != 0 && (opt->blocks_per_sm < 2 || opt->blocks_per_sm > 4))
             return set_err(PT_ERR_ARG, "blocks_per_sm must be 0, 2, 3 or 4%s");
+        if (opt->interpolation != 0 && opt->interpolation != 1)
+            return set_err(PT_ERR_ARG, "interpolation must be 0 (trilinear) or 1 (nearest node)%s");
+        if (opt->interpolation == 1 && opt->controller == 1)
+            return set_err(PT_ERR_UNSUPPORTED, "the learned controller's features need the trilinear gather%s");
         eta = opt->eta;
         t_stop = opt->t_stop;
         budget = opt->time_budget_s;
@@ -423,6 +427,7 @@ static int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
         R.rec_cap = opt->record_capacity;
         R.order = opt->order;
         R.minb = opt->blocks_per_sm;
+        R.near = opt->interpolation;
     }
     return PT_OK;
 }
@@ -506,7 +511,8 @@ static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
 
 extern "C" int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_fields *f,
                            const double params[17], const double *d_time, const double *d_state,
-                           const pt_options *opt, void *stream, int32_t *chosen, double ms_out[3])
+                           const pt_options *opt, int64_t sample, void *stream, int32_t *chosen,
+                           double ms_out[3])
 {
     if (!f) return set_err(PT_ERR_ARG, "fields handle is NULL%s");
     if (np < 1 || !d_time || !d_state) return set_err(PT_ERR_ARG, "autotune needs np >= 1 and buffers%s");
@@ -520,7 +526,10 @@ extern "C" int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_field
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return cuda_err(e, "pt_autotune");
-    const int64_t ns = np < (int64_t)sms * 4 * 128 * 2 ? np : (int64_t)sms * 4 * 128 * 2;
+    const int64_t dflt = (int64_t)sms * 4 * 128 * 2;
+    const int64_t want = sample < 0 ? np : (sample == 0 ? dflt : sample);
+    const int64_t ns = np < want ? np : want;
+    const bool windowed = opt && opt->t_stop > 0.0;   /* a real window, else an attempt cap */
     const int32_t mt = m < 2 ? m : 2;
     double *t_state = nullptr;
     int64_t *t_cnt = nullptr;
@@ -547,8 +556,10 @@ extern "C" int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_field
     attach_fields(f, R);
     R.queue = f->scratch;
     R.flags = reinterpret_cast<int32_t *>(f->scratch + 1);
-    if (!(opt && opt->max_steps > 0)) R.max_steps = 32;
-    for (int round = 0; round < 2 && e == cudaSuccess; ++round) {   /* round 0 warms up */
+    if (!windowed && !(opt && opt->max_steps > 0)) R.max_steps = 32;
+    /* short attempt-capped trials get a warm-up round; window trials last
+     * long enough that the first launch's set-up does not matter */
+    for (int round = windowed ? 1 : 0; round < 2 && e == cudaSuccess; ++round) {
         for (int v = 0; v < 3 && e == cudaSuccess; ++v) {
             R.minb = 2 + v;
             e = cudaMemcpy2DAsync(t_state, (size_t)mt * 64, d_state, (size_t)m * 64, 64, (size_t)ns,
@@ -1063,6 +1074,7 @@ extern "C" int pt_ensemble_create(int32_t method, int32_t nmembers, const pt_mem
         o.eta = M.eta;
         o.time_budget_s = opt ? opt->time_budget_s : 0.0;
         o.blocks_per_sm = opt ? opt->blocks_per_sm : 0;
+        o.interpolation = opt ? opt->interpolation : 0;
         int rc = prepare_run(method, M.np, M.m, shape_of(M.fields), M.params, &o, tab[k]);
         if (rc != PT_OK) return rc;
         ntot += M.np;

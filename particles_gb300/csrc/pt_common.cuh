@@ -33,6 +33,7 @@ struct PtRun {
     int32_t dm[3];
     int32_t dm_mask[3];     /* dm - 1 when dm is a power of two, else 0 */
     int32_t unit_map;      /* xl == +0 and xs == 1: (pos - xl) / xs == pos exactly */
+    int32_t near;          /* 1: interpolate_near (the node at the cell's lower corner) */
     /* extensions */
     double eta;
     int32_t has_j;

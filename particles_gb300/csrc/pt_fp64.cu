@@ -98,12 +98,19 @@ struct EvalF64 {
         const int64_t node[8] = { l[0] + yl + zl, l[0] + yl + zr, l[0] + yr + zl, l[0] + yr + zr,
                                   r[0] + yl + zl, r[0] + yl + zr, r[0] + yr + zl, r[0] + yr + zr };
         double acc[NV];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {                             /* :212-220 in order */
+        if (P.near) {                          /* interpolate_near (:76-80): the node l */
             double v[NC];
-            load_rec<NC>(P.fld, node[q], v);
+            load_rec<NC>(P.fld, node[0], v);
 #pragma unroll
-            for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * v[cc] : acc[cc] + w8[q] * v[cc];
+            for (int cc = 0; cc < NV; ++cc) acc[cc] = v[cc];
+        } else {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {                         /* :212-220 in order */
+                double v[NC];
+                load_rec<NC>(P.fld, node[q], v);
+#pragma unroll
+                for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * v[cc] : acc[cc] + w8[q] * v[cc];
+            }
         }
         const double g = sqrt(s[3] * s[3] + s[4] * s[4] + s[5] * s[5] + 1.0);
         const double v0 = s[3] / g, v1 = s[4] / g, v2 = s[5] / g;

@@ -69,6 +69,13 @@ struct GatherF32 {
         const int64_t yl = d1 * l[1], yr = d1 * r[1], zl = d12 * l[2], zr = d12 * r[2];
         const int64_t node[8] = { l[0] + yl + zl, l[0] + yl + zr, l[0] + yr + zl, l[0] + yr + zr,
                                   r[0] + yl + zl, r[0] + yl + zr, r[0] + yr + zl, r[0] + yr + zr };
+        if (P.near) {                          /* interpolate_near: the node l */
+            float v[NC];
+            load(P.fld32, node[0], v);
+#pragma unroll
+            for (int cc = 0; cc < NV; ++cc) acc[cc] = v[cc];
+            return;
+        }
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             float v[NC];
@@ -110,12 +117,16 @@ struct GatherBrick {
         const int64_t b = (l[0] >> 3) + (int64_t)P.nb[0] * ((l[1] >> 3) + (int64_t)P.nb[1] * (l[2] >> 3));
         const int64_t base = b * 729 + (l[0] & 7) + 9 * (l[1] & 7) + 81 * (l[2] & 7);
         float sum[NV];
+        if (P.near) {                          /* interpolate_near: the node l */
+            load_node(P.fld16, base, sum);
+        } else {
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            float v[NV];
-            load_node(P.fld16, base + ((q & 4) ? 1 : 0) + ((q & 2) ? 9 : 0) + ((q & 1) ? 81 : 0), v);
+            for (int q = 0; q < 8; ++q) {
+                float v[NV];
+                load_node(P.fld16, base + ((q & 4) ? 1 : 0) + ((q & 2) ? 9 : 0) + ((q & 1) ? 81 : 0), v);
 #pragma unroll
-            for (int c = 0; c < NV; ++c) sum[c] = (q == 0) ? w8[0] * v[c] : fmaf(w8[q], v[c], sum[c]);
+                for (int c = 0; c < NV; ++c) sum[c] = (q == 0) ? w8[0] * v[c] : fmaf(w8[q], v[c], sum[c]);
+            }
         }
         const float4 *sp = reinterpret_cast<const float4 *>(P.bscale + b * NS);
         float os[NS];

@@ -19,6 +19,11 @@ from . import _native as N
 from .params import method_id
 
 
+# gather: "linear" = interpolate_lin (interpolations.F90:104-226, the reference's
+# choice in accelerations.F90:82); "near" = interpolate_near (:55-83)
+INTERPOLATIONS = {"linear": 0, "near": 1}
+
+
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
@@ -29,7 +34,7 @@ def _f64(a):
 
 def _options(precision, *, eta=0.0, jj=None, open_x=False, max_steps=0, t_stop=0.0,
              status=None, carry=None, time_budget_s=0.0, model=None, records=None,
-             order=None, blocks_per_sm=0):
+             order=None, blocks_per_sm=0, interpolation=0):
     o = N.PtOptions()
     o.struct_size = C.sizeof(N.PtOptions)
     o.precision = N.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
@@ -49,6 +54,7 @@ def _options(precision, *, eta=0.0, jj=None, open_x=False, max_steps=0, t_stop=0
     o.status = _ptr(status)
     o.carry = _ptr(carry)
     o.blocks_per_sm = int(blocks_per_sm)
+    o.interpolation = INTERPOLATIONS[interpolation] if isinstance(interpolation, str) else int(interpolation)
     return o
 
 
@@ -59,7 +65,7 @@ def carry_buffer(npart: int) -> np.ndarray:
 
 def integrate(method, params, time, uu, bb, state, cnt=None, *, precision="fp64", eta=0.0,
               jj=None, open_x=False, max_steps=0, t_stop=0.0, carry=None, status=None,
-              time_budget_s=0.0, check=True):
+              time_budget_s=0.0, check=True, interpolation="linear"):
     """Integrate every particle of ``state`` in place on the GPU.
 
     Returns (state, cnt, status).  With ``check`` a negative return code
@@ -78,7 +84,8 @@ def integrate(method, params, time, uu, bb, state, cnt=None, *, precision="fp64"
     jj = _f64(jj) if jj is not None else None
     dm = np.array(uu.shape[:0:-1], np.int32)
     opt = _options(precision, eta=eta, jj=jj, open_x=open_x, max_steps=max_steps,
-                   t_stop=t_stop, status=status, carry=carry, time_budget_s=time_budget_s)
+                   t_stop=t_stop, status=status, carry=carry, time_budget_s=time_budget_s,
+                   interpolation=interpolation)
     rc = L.pt_integrate(mid, npart, m, _ptr(dm), _ptr(_f64(params)), _ptr(_f64(time)),
                         _ptr(uu), _ptr(bb), _ptr(state), _ptr(cnt), C.byref(opt))
     if check:
@@ -146,7 +153,7 @@ class Fields:
 
     def integrate(self, method, params, time, state, cnt=None, *, eta=0.0, open_x=False,
                   max_steps=0, t_stop=0.0, carry=None, status=None, time_budget_s=0.0,
-                  check=True):
+                  check=True, interpolation="linear"):
         """Host-buffer run on these fields (pt_integrate_fields)."""
         npart, m, _ = state.shape
         if cnt is None:
@@ -154,7 +161,8 @@ class Fields:
         if status is None:
             status = np.zeros(npart, np.int32)
         opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
-                       t_stop=t_stop, status=status, carry=carry, time_budget_s=time_budget_s)
+                       t_stop=t_stop, status=status, carry=carry, time_budget_s=time_budget_s,
+                       interpolation=interpolation)
         rc = self._L.pt_integrate_fields(method_id(method), npart, m, self._h,
                                          _ptr(_f64(params)), _ptr(_f64(time)), _ptr(state),
                                          _ptr(cnt), C.byref(opt))
@@ -164,7 +172,8 @@ class Fields:
 
     def run_device(self, method, params, d_time, d_state, d_cnt, d_status=None, d_carry=None,
                    *, eta=0.0, open_x=False, max_steps=0, t_stop=0.0, time_budget_s=0.0,
-                   stream=0, model=None, records=None, order=None, blocks_per_sm=0):
+                   stream=0, model=None, records=None, order=None, blocks_per_sm=0,
+                   interpolation="linear"):
         """Launch on device tensors (torch); returns without synchronising.
 
         model: a learned.Model for the learned controller; records: a device
@@ -174,7 +183,8 @@ class Fields:
         npart, m, _ = d_state.shape
         opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
                        t_stop=t_stop, time_budget_s=time_budget_s, model=model,
-                       records=records, order=order, blocks_per_sm=blocks_per_sm)
+                       records=records, order=order, blocks_per_sm=blocks_per_sm,
+                       interpolation=interpolation)
         rc = self._L.pt_run_device(
             method_id(method), npart, m, self._h, _ptr(_f64(params)),
             C.c_void_p(d_time.data_ptr()), C.c_void_p(d_state.data_ptr()),
@@ -185,19 +195,22 @@ class Fields:
         N.check(rc, "pt_run_device")
 
     def autotune(self, method, params, d_time, d_state, *, eta=0.0, open_x=False, max_steps=0,
-                 stream=0, model=None, records=None):
+                 t_stop=0.0, sample=0, stream=0, model=None, records=None,
+                 interpolation="linear"):
         """Time the launch variants of the kernel run_device would use with
         these arguments (pt_autotune) and make the fastest its default.
 
+        t_stop > 0 times a real window up to t_stop (else max_steps attempts);
+        sample: particles in the trial (0 default, -1 all).
         Returns (blocks_per_sm, {variant: trial ms})."""
         npart, m, _ = d_state.shape
         opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
-                       model=model, records=records)
+                       t_stop=t_stop, model=model, records=records, interpolation=interpolation)
         chosen = C.c_int32(0)
         ms = np.zeros(3, np.float64)
         rc = self._L.pt_autotune(method_id(method), npart, m, self._h, _ptr(_f64(params)),
                                  C.c_void_p(d_time.data_ptr()), C.c_void_p(d_state.data_ptr()),
-                                 C.byref(opt), C.c_void_p(stream) if stream else None,
+                                 C.byref(opt), int(sample), C.c_void_p(stream) if stream else None,
                                  C.byref(chosen), _ptr(ms))
         N.check(rc, "pt_autotune")
         return int(chosen.value), {2 + i: float(ms[i]) for i in range(3)}
@@ -219,7 +232,7 @@ class Ensemble:
     """
 
     def __init__(self, method, members, *, precision="fp64", blocks_per_sm=0,
-                 time_budget_s=0.0):
+                 time_budget_s=0.0, interpolation="linear"):
         self._L = N.load()
         self._h = C.c_void_p()
         self.n = len(members)
@@ -238,7 +251,8 @@ class Ensemble:
             a.max_steps = int(mb.get("max_steps", 0))
             for key in ("time", "state", "cnt", "status", "carry"):
                 setattr(a, key, C.c_void_p(mb[key].data_ptr()))
-        opt = _options(precision, time_budget_s=time_budget_s, blocks_per_sm=blocks_per_sm)
+        opt = _options(precision, time_budget_s=time_budget_s, blocks_per_sm=blocks_per_sm,
+                       interpolation=interpolation)
         N.check(self._L.pt_ensemble_create(method_id(method), self.n, C.byref(arr), C.byref(opt),
                                            C.byref(self._h)), "pt_ensemble_create")
 

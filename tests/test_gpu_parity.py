@@ -14,15 +14,16 @@ from conftest import small_problem
 pytestmark = pytest.mark.gpu
 
 
-def _run_both(prob, precision="fp64", **kw):
+def _run_both(prob, precision="fp64", near=False, **kw):
     import oracle
     from particles_gb300 import integrate
     uu, bb = prob["fields"][:2]
     jj = prob["fields"][2] if len(prob["fields"]) > 2 else None
     so, co, sto = oracle.integrate(prob["method"], prob["params"], prob["time"], uu, bb,
-                                   prob["state"].copy(), jj=jj, **kw)
+                                   prob["state"].copy(), jj=jj, near=near, **kw)
     sg, cg, stg = integrate(prob["method"], prob["params"], prob["time"], uu, bb,
-                            prob["state"].copy(), precision=precision, jj=jj, check=False, **kw)
+                            prob["state"].copy(), precision=precision, jj=jj, check=False,
+                            interpolation="near" if near else "linear", **kw)
     return (so, co, sto), (sg, cg, stg)
 
 
@@ -145,3 +146,12 @@ def test_windowed_resume_bitwise(cuda, oracle_lib, method):
         assert np.array_equal(so, sg), w
     assert (st_g == 0).all()
     assert np.array_equal(full_o[0], sg) and np.array_equal(full_o[1], cg)
+
+
+@pytest.mark.parametrize("method", ["rk5", "dop853"])
+def test_near_gather_exact_bitwise(cuda, oracle_lib, method):
+    """interpolate_near (interpolations.F90:55-83) selected by the options:
+    the exact kernel still reproduces the oracle bit for bit."""
+    prob = small_problem(method, n=16, npart=96, periods=1.0, seed=8)
+    (so, co, sto), (sg, cg, stg) = _run_both(prob, near=True)
+    assert np.array_equal(co, cg) and np.array_equal(sto, stg) and np.array_equal(so, sg)

@@ -91,7 +91,7 @@ def test_launch_variant_option_checked_on_host(native):
         o.struct_size = C.sizeof(o)
         o.blocks_per_sm = v
         assert native.pt_debug_unpack(1, 4, 2, ptr(dm), 0, 0, ptr(p), C.byref(o), ptr(out)) == rc
-    assert native.pt_autotune(1, 4, 2, None, ptr(p), None, None, None, None, None, None) == N.PT_ERR_ARG
+    assert native.pt_autotune(1, 4, 2, None, ptr(p), None, None, None, 0, None, None, None) == N.PT_ERR_ARG
 
 
 def test_ensemble_argument_errors_need_no_gpu(native):
@@ -108,3 +108,20 @@ def test_ensemble_argument_errors_need_no_gpu(native):
     assert native.pt_ensemble_run(None, 1.0, None) == N.PT_ERR_ARG
     assert native.pt_ensemble_replay(None, None) == N.PT_ERR_ARG
     assert native.pt_ensemble_destroy(None) == N.PT_OK
+
+
+def test_interpolation_option_checked_on_host(native):
+    from particles_gb300 import _native as N
+    from particles_gb300.params import pack_params
+    assert N.PtOptions.interpolation.offset == 108 and C.sizeof(N.PtOptions) == 112
+    dm = np.array([8, 8, 8], np.int32)
+    p = pack_params(qom=1.0, vunit=0.1, tmax=1.0)
+    out = np.zeros(8)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)
+    for v, ctl, rc in ((0, 0, N.PT_OK), (1, 0, N.PT_OK), (2, 0, N.PT_ERR_ARG),
+                       (1, 1, N.PT_ERR_ARG)):       # controller 1 without a model: ARG first
+        o = N.PtOptions()
+        o.struct_size = C.sizeof(o)
+        o.interpolation = v
+        o.controller = ctl
+        assert native.pt_debug_unpack(1, 4, 2, ptr(dm), 0, 0, ptr(p), C.byref(o), ptr(out)) == rc

@@ -307,3 +307,24 @@ def test_flop_counts_are_the_benchmark_constants():
     from particles_gb300 import roofline
     for key, (method, what, eta) in roofline.COUNT_KEYS.items():
         assert sum(oracle.count_ops(method, what, eta)) == roofline.FLOPS[key], key
+
+
+def test_near_gather_option(oracle_lib):
+    """interpolate_near (interpolations.F90:55-83) in the acceleration: in a
+    uniform field it agrees with the trilinear run to rounding (the trilinear
+    weights sum to 1 only to rounding); in a turbulent field the particles see
+    the lower-corner node values and the runs differ."""
+    import oracle
+    from conftest import small_problem
+    prob = small_problem("rk5", n=8, npart=16, periods=0.5, seed=3, db_rms=0.0, v_rms=0.0)
+    uu, bb = prob["fields"]
+    a = oracle.integrate("rk5", prob["params"], prob["time"], uu, bb, prob["state"].copy())
+    b = oracle.integrate("rk5", prob["params"], prob["time"], uu, bb, prob["state"].copy(), near=True)
+    assert np.allclose(a[0], b[0], rtol=1e-9, atol=1e-12)
+    assert np.abs(a[1] - b[1]).max() <= 2
+    prob = small_problem("rk5", n=8, npart=16, periods=0.5, seed=3)
+    uu, bb = prob["fields"]
+    a = oracle.integrate("rk5", prob["params"], prob["time"], uu, bb, prob["state"].copy())
+    b = oracle.integrate("rk5", prob["params"], prob["time"], uu, bb, prob["state"].copy(), near=True)
+    assert not np.array_equal(a[0], b[0])
+    assert (b[2] == 0).all() and np.isfinite(b[0]).all()
