@@ -168,6 +168,14 @@ int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_fields *f,
                 const pt_options *opt, int64_t sample, void *stream, int32_t *chosen,
                 double ms_out[3]);
 
+/* Streaming output: copies output rows [row0, row1) of every particle of a
+ * device state(8,m,np) to host memory laid out (np, row1 - row0, 8), as one
+ * strided asynchronous copy on `stream` (pinned host memory makes it overlap
+ * with kernels on other streams).  Rows whose time is <= the window end of a
+ * finished window are final for every particle that is still running. */
+int pt_copy_rows(const double *d_state, int64_t np, int32_t m, int32_t row0, int32_t row1,
+                 double *h_out, void *stream);
+
 /* ---- ensembles: several runs in one persistent launch (no counterpart in
  *      the reference; each member is what one pt_run_device call would do) -- */
 
@@ -300,6 +308,10 @@ int pt_probe_peak(int32_t kind, int32_t iters, double *flops_per_s);
 
 /* Device-side evaluation helpers for the parity tests (device pointers). */
 int pt_debug_pow(int64_t n, const double *d_x, const double *d_y, double *d_out, void *stream);
+/* The step controller's power in the FP64-FMA and mixed builds (Newton
+ * roots for the exponents -1/5, -1/4, -1/8; the deterministic pow otherwise). */
+int pt_debug_ctl_pow(int64_t n, const double *d_x, const double *d_y, double *d_out,
+                     void *stream);
 int pt_debug_accel(const pt_fields *f, int64_t n, const double params[17],
                    const double *d_vec, double *d_acc, void *stream);
 

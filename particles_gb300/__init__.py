@@ -7,11 +7,11 @@ Python face of that ABI plus the host-side helpers the reference driver
 provides (parameter vector, time grid, initial states, synthetic fields).
 """
 from . import fields, initial, params
-from .integrations import (Ensemble, Fields, carry_buffer, integrate, integrate_dp853,
-                           integrate_rk5)
+from .integrations import (Ensemble, Fields, OutputStream, carry_buffer, integrate,
+                           integrate_dp853, integrate_rk5)
 from .params import method_id, pack_params, time_grid
 
 __all__ = [
-    "Ensemble", "Fields", "carry_buffer", "fields", "initial", "integrate", "integrate_dp853",
+    "Ensemble", "Fields", "OutputStream", "carry_buffer", "fields", "initial", "integrate", "integrate_dp853",
     "integrate_rk5", "method_id", "pack_params", "params", "time_grid",
 ]

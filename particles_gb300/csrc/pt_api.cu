@@ -796,6 +796,14 @@ extern "C" int pt_debug_pow(int64_t n, const double *d_x, const double *d_y, dou
     return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_pow");
 }
 
+extern "C" int pt_debug_ctl_pow(int64_t n, const double *d_x, const double *d_y, double *d_out,
+                                void *stream)
+{
+    if (n < 0 || (n > 0 && (!d_x || !d_y || !d_out))) return set_err(PT_ERR_ARG, "bad argument%s");
+    const cudaError_t e = pt_launch_ctl_pow(n, d_x, d_y, d_out, (cudaStream_t)stream);
+    return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_ctl_pow");
+}
+
 extern "C" int pt_debug_accel(const pt_fields *f, int64_t n, const double params[17],
                               const double *d_vec, double *d_acc, void *stream)
 {
@@ -817,6 +825,20 @@ extern "C" int pt_debug_accel(const pt_fields *f, int64_t n, const double params
     else
         e = pt_launch_accel_mixed(R, f->nc32, 0, n, d_vec, d_acc, (cudaStream_t)stream);
     return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_accel");
+}
+
+extern "C" int pt_copy_rows(const double *d_state, int64_t np, int32_t m, int32_t row0,
+                            int32_t row1, double *h_out, void *stream)
+{
+    if (np < 0 || m < 1 || row0 < 0 || row1 > m || row0 > row1)
+        return set_err(PT_ERR_ARG, "bad row range%s");
+    if (np == 0 || row0 == row1) return PT_OK;
+    if (!d_state || !h_out) return set_err(PT_ERR_ARG, "NULL buffer%s");
+    const size_t w = (size_t)(row1 - row0) * 8 * sizeof(double);
+    const cudaError_t e = cudaMemcpy2DAsync(h_out, w, d_state + (size_t)row0 * 8,
+                                            (size_t)m * 8 * sizeof(double), w, (size_t)np,
+                                            cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+    return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_copy_rows");
 }
 
 /* ---------------------------------------------------------------------- */

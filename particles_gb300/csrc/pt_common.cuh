@@ -178,5 +178,7 @@ cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int brick, int64_t n, 
 
 cudaError_t pt_launch_debug_pow(int64_t n, const double *x, const double *y, double *out,
                                 cudaStream_t s);
+cudaError_t pt_launch_ctl_pow(int64_t n, const double *x, const double *y, double *out,
+                              cudaStream_t s);
 
 #endif /* PT_COMMON_CUH */

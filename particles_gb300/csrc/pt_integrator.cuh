@@ -319,6 +319,8 @@ __device__ __forceinline__ double pt_rcp(double x)
 #define PT_DIV(a, b) ((a) * pt_rcp(b))
 #endif
 
+#include "pt_ctlpow.cuh"
+
 /* Final combination and error norm: sf and the scaled error (DOP853 err,
  * RK5 del).  Row 3 receives the 8th-order increment as in :418. */
 template <int METHOD>
@@ -563,7 +565,7 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
             if (mode == M_ACCEPT || mode == M_REJECT) {
                 const double y = (METHOD == PT_METHOD_DOP853) ? PT_Q.expo
                                : (mode == M_ACCEPT ? -0.20 : -0.25);
-                fpow = PT_Q.safe * pt_det_pow(q, y);
+                fpow = PT_Q.safe * pt_ctl_pow(q, y);
             }
             if (mode == M_ACCEPT) {                                    /* :150-177, :439-476 */
                 L.t = L.t + dt;

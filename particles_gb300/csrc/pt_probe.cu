@@ -10,8 +10,17 @@
 #include <cuda_runtime.h>
 
 #include "pt_common.cuh"
+#include "pt_ctlpow.cuh"
 
 namespace {
+
+/* The non-exact builds' controller power, for its accuracy test. */
+__global__ void k_ctl_pow(int64_t n, const double *x, const double *y, double *o)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        o[i] = pt_ctl_pow(x[i], y[i]);
+}
 
 template <class T>
 __global__ void k_fma_chains(T *out, int iters, T a, T b)
@@ -66,4 +75,13 @@ extern "C" int pt_probe_peak(int32_t kind, int32_t iters, double *flops_per_s)
     double r = (kind == 0) ? measure<double>(iters) : measure<float>(iters);
     *flops_per_s = r;
     return r > 0 ? PT_OK : PT_ERR_CUDA;
+}
+
+cudaError_t pt_launch_ctl_pow(int64_t n, const double *x, const double *y, double *out,
+                              cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    k_ctl_pow<<<grid, 256, 0, s>>>(n, x, y, out);
+    return cudaGetLastError();
 }

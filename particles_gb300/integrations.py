@@ -299,3 +299,51 @@ class Ensemble:
             self.close()
         except Exception:
             pass
+
+
+class OutputStream:
+    """Streams finished output rows to the host while later windows run.
+
+    After each window, call `window_done(t_stop, compute_stream)`: the rows
+    whose time is <= t_stop are final for every particle still running, so
+    they are copied (pt_copy_rows, one strided copy) on a side stream that
+    waits for the window's kernel through an event and overlaps the next
+    window.  `rows()` synchronises and returns the host array (np, m, 8)
+    with every row streamed so far.
+    """
+
+    def __init__(self, torch, d_state, time):
+        self._L = N.load()
+        self.torch = torch
+        self.d_state = d_state
+        self.time = np.asarray(time, np.float64)
+        npart, m, _ = d_state.shape
+        self.host = torch.zeros((npart, m, 8), dtype=torch.float64).pin_memory()
+        self.side = torch.cuda.Stream(device=d_state.device)
+        self.done = 0
+        self._bufs = []
+
+    def window_done(self, t_stop, compute_stream=None):
+        torch = self.torch
+        n = int(np.searchsorted(self.time, t_stop, side="right")) if t_stop > 0 else self.time.size
+        if n <= self.done:
+            return 0
+        ev = torch.cuda.Event()
+        ev.record(compute_stream or torch.cuda.current_stream())
+        self.side.wait_event(ev)
+        npart, m, _ = self.d_state.shape
+        buf = torch.empty((npart, n - self.done, 8), dtype=torch.float64).pin_memory()
+        N.check(self._L.pt_copy_rows(C.c_void_p(self.d_state.data_ptr()), npart, m, self.done, n,
+                                     C.c_void_p(buf.data_ptr()), C.c_void_p(self.side.cuda_stream)),
+                "pt_copy_rows")
+        self._bufs.append((self.done, n, buf))
+        rows = n - self.done
+        self.done = n
+        return rows
+
+    def rows(self):
+        self.side.synchronize()
+        for a, b, buf in self._bufs:
+            self.host[:, a:b] = buf
+        self._bufs = []
+        return self.host.numpy()

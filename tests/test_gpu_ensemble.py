@@ -103,3 +103,31 @@ def test_ensemble_graph_replay_equals_stepwise(cuda, precision):
     for a, b in zip(outs[0], outs[1]):
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
+
+
+def test_output_stream_rows_match_final_state(cuda):
+    """Rows streamed to the host after each window equal the final state."""
+    torch = cuda
+    from particles_gb300 import Fields, OutputStream
+    prob = small_problem("rk5", n=16, npart=200, periods=2.0, seed=61, nsteps=16)
+    uu, bb = prob["fields"]
+    f = Fields(uu, bb, precision="fp32")
+    npart = prob["state"].shape[0]
+    st = torch.tensor(prob["state"], device="cuda")
+    cnt = torch.zeros((npart, 3), dtype=torch.int64, device="cuda")
+    status = torch.zeros(npart, dtype=torch.int32, device="cuda")
+    carry = torch.zeros(int(f._L.pt_carry_bytes(npart)), dtype=torch.uint8, device="cuda")
+    d_time = torch.tensor(prob["time"], device="cuda")
+    stream = torch.cuda.Stream()
+    out = OutputStream(torch, st, prob["time"])
+    tmax = prob["time"][-1]
+    streamed = 0
+    for w in range(1, 6):
+        t = min(w * 0.45 * T0, tmax) if w < 5 else 0.0
+        f.run_device("rk5", prob["params"], d_time, st, cnt, status, carry, t_stop=t,
+                     stream=stream.cuda_stream)
+        streamed += out.window_done(t, stream)
+    rows = out.rows()
+    stream.synchronize()
+    assert f.run_check() == 0 and streamed == prob["time"].size
+    assert np.array_equal(rows, st.cpu().numpy())

@@ -155,3 +155,25 @@ def test_near_gather_exact_bitwise(cuda, oracle_lib, method):
     prob = small_problem(method, n=16, npart=96, periods=1.0, seed=8)
     (so, co, sto), (sg, cg, stg) = _run_both(prob, near=True)
     assert np.array_equal(co, cg) and np.array_equal(sto, stg) and np.array_equal(so, sg)
+
+
+def test_controller_pow_of_the_fast_builds(cuda, oracle_lib):
+    """pt_ctl_pow (FP64-FMA and mixed builds): Newton roots for the
+    controllers' exponents agree with the deterministic pow to a few ulp;
+    other exponents and extreme ratios are the deterministic pow itself."""
+    torch = cuda
+    from particles_gb300 import _native as N
+    rng = np.random.default_rng(5)
+    q = np.concatenate([10.0 ** rng.uniform(-29.5, 29.5, 6000), [1.0, 1e-31, 1e31, 0.0, 3e-12]])
+    y = np.concatenate([rng.choice([-0.2, -0.25, -0.125], 6000), [-0.2, -0.25, -0.2, -0.2, -0.3]])
+    dq, dy = torch.tensor(q, device="cuda"), torch.tensor(y, device="cuda")
+    out = torch.empty_like(dq)
+    N.check(N.load().pt_debug_ctl_pow(q.size, C.c_void_p(dq.data_ptr()), C.c_void_p(dy.data_ptr()),
+                                      C.c_void_p(out.data_ptr()), None), "pt_debug_ctl_pow")
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    true = q[:6001] ** y[:6001]                        # libm, within 1 ulp
+    rel = np.abs(got[:6001] - true) / true
+    assert rel.max() < 4 * 2.2e-16, rel.max()
+    ref = np.array([oracle_lib.det_pow(a, b) for a, b in zip(q[6001:], y[6001:])])
+    assert np.array_equal(got[6001:], ref)             # outside the Newton range: same bits
