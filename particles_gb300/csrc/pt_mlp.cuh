@@ -112,7 +112,7 @@ __device__ __forceinline__ PtMlpSmem pt_mlp_load(const unsigned char *blob, unsi
 
 /* y = MLP(x) for the 32 lanes of a converged warp; every lane passes its own
  * eight raw features and receives its own output (log trial step). */
-__device__ __forceinline__ float pt_mlp_warp(const PtMlpSmem &M, const float x[8])
+static __device__ __noinline__ float pt_mlp_warp(const PtMlpSmem &M, const float x[8])
 {
     const int lane = threadIdx.x & 31;
     const int g = lane >> 2, q = lane & 3;
