@@ -86,7 +86,10 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(k for k in WORKLOADS if k != "ensemble-3"),
                     default="dop853-256")
-    ap.add_argument("--precision", choices=["fp64", "fp64_fma", "fp32"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "fp64_fma", "fp32", "bf16"], default="fp64")
+    ap.add_argument("--controller", choices=["classical", "learned"], default="classical",
+                    help="learned: the first warm-up window records accepted steps, a model "
+                         "is trained on them and the later windows use it")
     ap.add_argument("--particles", type=int, default=0,
                     help="override the particle count (profiling of small cases only)")
     ap.add_argument("--window", type=float, default=0.0,
@@ -710,8 +713,9 @@ def main():
     if big:                                   # host copies only for the CPU baseline
         out = tuple(a.cpu().numpy() for a in out) if not args.no_cpu else None
         torch.cuda.empty_cache()
-    rec_bytes = ((10 if cfg["eta"] != 0.0 else 6) * 8 if args.precision != "fp32"
-                 else (12 if cfg["eta"] != 0.0 else 8) * 4)
+    rec_bytes = {"fp32": (12 if cfg["eta"] != 0.0 else 8) * 4,
+                 "bf16": (16 if cfg["eta"] != 0.0 else 8) * 2}.get(
+        args.precision, (10 if cfg["eta"] != 0.0 else 6) * 8)
     stream = torch.cuda.Stream(device=dev)
     with torch.cuda.stream(stream):
         d_time = torch.tensor(tg, device=dev)
@@ -722,18 +726,34 @@ def main():
         d_carry = torch.zeros(int(L.pt_carry_bytes(npart)), dtype=torch.uint8, device=dev)
     stream.synchronize()
 
-    launch = tune(args, f, cfg["method"], prm, d_time, d_state, stream, window * T0, eta=cfg["eta"])
+    model = None
+    training = None
     ordq = QueueOrder(torch, d_cnt, enabled=not args.no_order)
 
-    def window_run(w):
+    def window_run(w, records=None):
         order = ordq.before()
         f.run_device(cfg["method"], prm, d_time, d_state, d_cnt, d_status, d_carry,
                      eta=cfg["eta"], t_stop=w * window * T0, time_budget_s=900.0,
-                     stream=stream.cuda_stream, order=order)
+                     stream=stream.cuda_stream, order=order, model=model, records=records)
         ordq.after()
 
     w = 0
-    for _ in range(args.warmup):
+    if args.controller == "learned":
+        from particles_gb300 import learned as LRN
+        rec = LRN.record_buffer(torch, min(args.records, 4_000_000))
+        w += 1
+        window_run(w, records=rec)
+        stream.synchronize()
+        X, T = LRN.dataset(LRN.records_from_buffer(rec), cfg["method"])
+        norm = LRN.normalisation(X, T)
+        pm, hist = LRN.train(torch, X, T, norm, epochs=2, batch=16384, lr=2e-3)
+        model = LRN.Model(pm, norm, safety=0.9)
+        training = {"records": int(X.shape[0]), "mse_per_epoch": hist,
+                    "recorded_in": "the first warm-up window (classical controller)"}
+        del rec
+    launch = tune(args, f, cfg["method"], prm, d_time, d_state, stream, window * T0,
+                  eta=cfg["eta"], model=model)
+    for _ in range(args.warmup - w):
         w += 1
         window_run(w)
     stream.synchronize()
@@ -791,17 +811,24 @@ def main():
                                                            record_bytes=rec_bytes) / args.steps}
 
     line = {
-        "metric": "accepted particle-steps/s (plain FP64 kernel)",
+        "metric": ("accepted particle-steps/s (plain FP64 kernel)"
+                   if args.precision == "fp64" and args.controller == "classical"
+                   else f"accepted particle-steps/s ({args.precision}, {args.controller} controller)"),
         "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp64": "f64", "fp64_fma": "f64", "fp32": "f64 step machine, f32 gather/force",
+                  "bf16": "f64 step machine, f32 gather/force, bf16 field store"}[args.precision],
         "data": "synthetic (seeded fields and particles)",
         "config": workload_config(cfg, npart, window, args),
         "wall_s_timed": wall, "gpu_launches": args.steps, "stopped_particles": stopped,
         "rejected_fraction": float(dcnt_tot[2] / max(dcnt_tot[0], 1)),
         "attempts_per_s": float(dcnt_tot[0]) / elapsed,
         "roofline": roof, "clocks": clocks.summary(), "launch": launch,
+        "controller": args.controller,
     }
+    if training:
+        line["learned_training"] = training
 
     # end to end through the host-buffer C ABI: pinned host copies every step
     if not args.no_e2e and rank == 0:
@@ -820,7 +847,7 @@ def main():
         for _ in range(k_e2e):
             w += 1
             o = _options(args.precision, eta=cfg["eta"], t_stop=w * window * T0,
-                         status=None, carry=None, time_budget_s=900.0)
+                         status=None, carry=None, time_budget_s=900.0, model=model)
             o.status = C.c_void_p(h_status.data_ptr())
             o.carry = C.c_void_p(h_carry.data_ptr())
             rc = L.pt_integrate_fields(method_id(cfg["method"]), npart, m, f.handle, prm.ctypes.data_as(C.c_void_p),
@@ -854,6 +881,8 @@ def main():
         line["ensemble"] = ensemble_leg(args, dev, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
+    if model is not None:
+        model.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     f.close()

@@ -70,6 +70,12 @@ struct EvalF64 {
     static __device__ __forceinline__ const double *records(const PtRun &P) { return P.fld; }
     struct Origin {};
     static __device__ __forceinline__ void begin(const PtRun &, const double *, Origin &) {}
+    static __device__ __forceinline__ void feature_cell(const PtRun &P, const double si[6],
+                                                        const Origin &, int32_t l[3], int32_t r[3],
+                                                        float xd[3])
+    {
+        pt_feature_cell(P, si, l, r, xd);
+    }
     static __device__ __forceinline__ void f(const PtRun &P, const double s[6], const double *,
                                              const Origin &, double a[6])
     {

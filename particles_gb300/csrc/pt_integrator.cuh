@@ -615,6 +615,10 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
             } else if (mode == M_READY) {
                 next_time(PT_Q, L);
             }
+            /* The evaluation origin of the next attempt: a new si after an
+             * accept or a resume; a rejected or just-initialised lane keeps
+             * the origin of its unchanged si. */
+            if (active && (mode == M_ACCEPT || mode == M_READY)) EV::begin(PT_Q, si, O);
             if (LEARN) {
                 /* Features at the new si of an accepted step: the record of
                  * the step that just completed pairs the features at its
@@ -624,7 +628,11 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
                 const bool want = (mode == M_ACCEPT) && active;
                 float feat[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
                 if (want) {
-                    pt_field_features<typename EV::Rec, EV::NCR>(PT_Q, EV::records(PT_Q), si, feat);
+                    int32_t fl_[3], fr_[3];
+                    float fx_[3];
+                    EV::feature_cell(PT_Q, si, O, fl_, fr_, fx_);
+                    pt_field_features<typename EV::Rec, EV::NCR>(PT_Q, EV::records(PT_Q), si, fl_, fr_,
+                                                                 fx_, feat);
                     const float om = PT_Q.qomf * __expf(feat[0] - feat[2]);     /* qom |B| / gamma */
                     const float dtf = pt_d2f(dt);
                     feat[5] = __logf(om * dtf + 1e-30f);
@@ -669,7 +677,6 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
 #pragma unroll
                         for (int c = 0; c < 6; ++c) K(0, c) = L.dt * K(T::F1, c);   /* :137, j = 1 */
                     }
-                    EV::begin(PT_Q, si, O);
                 }
             }
             if (!__any_sync(0xffffffffu, active)) {

@@ -164,6 +164,26 @@ struct EvalMixed {
         }
     }
 
+    /* The cell of si for the learned controller's features: the origin. */
+    static __device__ __forceinline__ void feature_cell(const PtRun &P, const double *,
+                                                        const Origin &O, int32_t l[3], int32_t r[3],
+                                                        float xd[3])
+    {
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            int32_t li;
+            if (P.dm_mask[i]) {
+                li = O.cell[i] & P.dm_mask[i];
+            } else {
+                li = O.cell[i] % P.dm[i];
+                if (li < 0) li += P.dm[i];
+            }
+            l[i] = li;
+            r[i] = (li + 1 == P.dm[i]) ? 0 : li + 1;
+            xd[i] = O.off[i];
+        }
+    }
+
     /* f(s) with s = si + d: the stage position relative to the origin cell is
      * off + d * dm / xs in FP32 (d is at most a few cells); momenta, gather and
      * force in FP32; every FP64 <-> FP32 conversion on the integer pipe. */

@@ -194,17 +194,11 @@ __device__ __forceinline__ float pt_to_f(double v)
     return __uint_as_float((hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3));
 }
 
-/* The five field invariants of the learned controller at the particle state
- * s, in FP32: log|B|, log|E|, log gamma, pitch cosine u.B/(|u||B|) and
- * log(|grad B|/|B|), with E = -U x B + eta J and grad B the analytic
- * derivative of the trilinear interpolant (the derivatives of the same eight
- * corner weights).  REC/NCR: record type and width of the field records. */
-template <class REC, int NCR>
-__device__ __forceinline__ void pt_field_features(const PtRun &P, const REC *fld, const double s[6],
-                                                  float out[5])
+/* Cell of s for the feature gather (FP64 position, FP32 offsets): left node
+ * l, periodic right node r = (l + 1) mod dm, and the offset xd in the cell. */
+__device__ __forceinline__ void pt_feature_cell(const PtRun &P, const double s[6], int32_t l[3],
+                                                int32_t r[3], float xd[3])
 {
-    int32_t l[3], r[3];
-    float xd[3], xu[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         const double xn = fma(s[i], P.gsx[i], P.gox[i]);
@@ -220,8 +214,47 @@ __device__ __forceinline__ void pt_field_features(const PtRun &P, const REC *fld
         }
         l[i] = li;
         r[i] = (li + 1 == P.dm[i]) ? 0 : li + 1;
-        xu[i] = 1.0f - xd[i];
     }
+}
+
+/* One record's U, B (and J) as floats: vector loads of the FP32 or FP64
+ * records (16-B aligned). */
+template <int NCR>
+__device__ __forceinline__ void pt_feature_rec(const float *fld, int64_t node, float v[NCR])
+{
+    const float4 *q = reinterpret_cast<const float4 *>(fld + node * NCR);
+#pragma unroll
+    for (int i = 0; i < NCR / 4; ++i) {
+        const float4 x = __ldg(q + i);
+        v[4 * i] = x.x; v[4 * i + 1] = x.y; v[4 * i + 2] = x.z; v[4 * i + 3] = x.w;
+    }
+}
+template <int NCR>
+__device__ __forceinline__ void pt_feature_rec(const double *fld, int64_t node, float v[NCR])
+{
+    const double2 *q = reinterpret_cast<const double2 *>(fld + node * NCR);
+#pragma unroll
+    for (int i = 0; i < NCR / 2; ++i) {
+        const double2 x = __ldg(q + i);
+        v[2 * i] = pt_to_f(x.x); v[2 * i + 1] = pt_to_f(x.y);
+    }
+}
+
+/* The five field invariants of the learned controller at the particle state
+ * s, in FP32: log|B|, log|E|, log gamma, pitch cosine u.B/(|u||B|) and
+ * log(|grad B|/|B|), with E = -U x B + eta J and grad B the analytic
+ * derivative of the trilinear interpolant (the derivatives of the same eight
+ * corner weights).  REC/NCR: record type and width of the field records;
+ * (l, r, xd): the cell of s (pt_feature_cell, or the attempt origin of the
+ * mixed evaluation). */
+template <class REC, int NCR>
+__device__ __forceinline__ void pt_field_features(const PtRun &P, const REC *fld, const double s[6],
+                                                  const int32_t l[3], const int32_t r[3],
+                                                  const float xd[3], float out[5])
+{
+    float xu[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) xu[i] = 1.0f - xd[i];
     const int64_t d1 = P.dm[0], d12 = (int64_t)P.dm[0] * P.dm[1];
     float U[3] = { 0, 0, 0 }, B[3] = { 0, 0, 0 }, J[3] = { 0, 0, 0 };
     float G[3][3] = { { 0, 0, 0 }, { 0, 0, 0 }, { 0, 0, 0 } };
@@ -235,13 +268,14 @@ __device__ __forceinline__ void pt_field_features(const PtRun &P, const REC *fld
         const float gy = (by ? 1.0f : -1.0f) * wx * wz * P.gsxf[1];
         const float gz = (bz ? 1.0f : -1.0f) * wx * wy * P.gsxf[2];
         const int64_t node = (bx ? r[0] : l[0]) + d1 * (by ? r[1] : l[1]) + d12 * (bz ? r[2] : l[2]);
-        const REC *v = fld + node * NCR;
+        float v[NCR];
+        pt_feature_rec<NCR>(fld, node, v);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float vu = pt_to_f(v[c]), vb = pt_to_f(v[3 + c]);
+            const float vu = v[c], vb = v[3 + c];
             U[c] = fmaf(w, vu, U[c]);
             B[c] = fmaf(w, vb, B[c]);
-            if (HJ) J[c] = fmaf(w, pt_to_f(v[6 + c]), J[c]);
+            if (HJ) J[c] = fmaf(w, v[(6 + c) % NCR], J[c]);
             G[c][0] = fmaf(gx, vb, G[c][0]);
             G[c][1] = fmaf(gy, vb, G[c][1]);
             G[c][2] = fmaf(gz, vb, G[c][2]);
