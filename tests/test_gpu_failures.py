@@ -1,0 +1,70 @@
+"""Failure handling on the GPU without faulting it.
+
+The reference loops forever on a NaN or a vanishing step
+(sources/integrations.F90:129,361) and has no time limit.  The kernels stop
+such particles with a status and bound every launch by a wall-clock budget;
+each failure here is made on the host (a tiny budget, an attempt cap, NaN
+field values), the kernel returns normally and the host reads the statuses.
+"""
+import numpy as np
+import pytest
+
+from conftest import small_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.int64)
+
+
+def test_time_budget_interrupts_and_the_carry_resumes(cuda, oracle_lib):
+    import oracle
+    from particles_gb300 import _native as N
+    from particles_gb300 import carry_buffer, integrate
+    prob = small_problem("dop853", n=16, npart=3000, periods=2.0, seed=71)
+    uu, bb = prob["fields"]
+    so, co, sto = oracle.integrate("dop853", prob["params"], prob["time"], uu, bb,
+                                   prob["state"].copy())
+    s = prob["state"].copy()
+    c = np.zeros((s.shape[0], 3), np.int64)
+    carry = carry_buffer(s.shape[0])
+    _, _, st1 = integrate("dop853", prob["params"], prob["time"], uu, bb, s, c, carry=carry,
+                          time_budget_s=2e-4, check=False)
+    assert N.load().pt_last_error() and (st1 == N.PT_ST_TIMEOUT).any()
+    assert set(np.unique(st1)) <= {N.PT_ST_TIMEOUT, N.PT_ST_NOT_RUN, N.PT_ST_DONE}
+    _, _, st2 = integrate("dop853", prob["params"], prob["time"], uu, bb, s, c, carry=carry)
+    assert (st2 == 0).all()
+    assert np.array_equal(c, co) and np.array_equal(s, so)     # as if never interrupted
+
+
+@pytest.mark.parametrize("method", ["rk5", "dop853"])
+def test_attempt_cap_matches_oracle(cuda, oracle_lib, method):
+    import oracle
+    from particles_gb300 import _native as N
+    from particles_gb300 import integrate
+    prob = small_problem(method, n=16, npart=128, periods=1.0, seed=72)
+    uu, bb = prob["fields"]
+    so, co, sto = oracle.integrate(method, prob["params"], prob["time"], uu, bb,
+                                   prob["state"].copy(), max_steps=7)
+    sg, cg, stg = integrate(method, prob["params"], prob["time"], uu, bb, prob["state"].copy(),
+                            max_steps=7, check=False)
+    assert (stg == N.PT_ST_STEP_LIMIT).all() and (cg[:, 0] == 7).all()
+    assert np.array_equal(stg, sto) and np.array_equal(cg, co) and np.array_equal(sg, so)
+
+
+def test_nonfinite_field_stops_particles_like_the_oracle(cuda, oracle_lib):
+    import oracle
+    from particles_gb300 import _native as N
+    from particles_gb300 import integrate
+    prob = small_problem("rk5", n=16, npart=256, periods=1.0, seed=73)
+    uu, bb = prob["fields"]
+    bb = bb.copy()
+    bb[:, 5:7, :, :] = np.nan                       # a slab of NaN field values
+    so, co, sto = oracle.integrate("rk5", prob["params"], prob["time"], uu, bb,
+                                   prob["state"].copy())
+    sg, cg, stg = integrate("rk5", prob["params"], prob["time"], uu, bb, prob["state"].copy(),
+                            check=False)
+    assert (sto == N.PT_ST_NONFINITE).any() and (sto == 0).any()
+    assert np.array_equal(stg, sto) and np.array_equal(cg, co)
+    assert np.array_equal(_bits(sg), _bits(so))     # NaN payloads included
