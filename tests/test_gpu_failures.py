@@ -68,3 +68,42 @@ def test_nonfinite_field_stops_particles_like_the_oracle(cuda, oracle_lib):
     assert (sto == N.PT_ST_NONFINITE).any() and (sto == 0).any()
     assert np.array_equal(stg, sto) and np.array_equal(cg, co)
     assert np.array_equal(_bits(sg), _bits(so))     # NaN payloads included
+
+
+def test_checkpoint_file_resume_is_bit_identical(cuda, oracle_lib, tmp_path):
+    """Windows 1-2, a checkpoint file, a new field handle, the rest of the
+    run: the same bits as the oracle's uninterrupted run."""
+    torch = cuda
+    import oracle
+    from particles_gb300 import Fields, checkpoint
+    prob = small_problem("dop853", n=16, npart=200, periods=1.0, seed=74)
+    uu, bb = prob["fields"]
+    so, co, _ = oracle.integrate("dop853", prob["params"], prob["time"], uu, bb,
+                                 prob["state"].copy())
+    T0 = 2.0 * np.pi / 200.0
+    f = Fields(uu, bb)
+    npart = prob["state"].shape[0]
+    st = torch.tensor(prob["state"], device="cuda")
+    cnt = torch.zeros((npart, 3), dtype=torch.int64, device="cuda")
+    status = torch.zeros(npart, dtype=torch.int32, device="cuda")
+    carry = torch.zeros(int(f._L.pt_carry_bytes(npart)), dtype=torch.uint8, device="cuda")
+    d_time = torch.tensor(prob["time"], device="cuda")
+    for w in (0.3, 0.55):
+        f.run_device("dop853", prob["params"], d_time, st, cnt, status, carry, t_stop=w * T0)
+    torch.cuda.synchronize()
+    p = checkpoint.save(tmp_path / "ck", state=st, cnt=cnt, carry=carry, status=status,
+                        t_reached=0.55 * T0, params=prob["params"], time=prob["time"],
+                        method="dop853")
+    f.close()
+    del st, cnt, status, carry
+    ck = checkpoint.load(p)
+    f2 = Fields(uu, bb)
+    st = torch.tensor(ck["state"], device="cuda")
+    cnt = torch.tensor(ck["cnt"], device="cuda")
+    status = torch.tensor(ck["status"], device="cuda")
+    carry = torch.tensor(ck["carry"], device="cuda")
+    f2.run_device("dop853", ck["params"], torch.tensor(ck["time"], device="cuda"), st, cnt,
+                  status, carry)
+    torch.cuda.synchronize()
+    assert f2.run_check() == 0
+    assert np.array_equal(cnt.cpu().numpy(), co) and np.array_equal(st.cpu().numpy(), so)
