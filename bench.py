@@ -843,6 +843,7 @@ def main():
         k_e2e = max(1, min(args.steps, 4))
         from particles_gb300.integrations import _options
         from particles_gb300.params import method_id
+        xfer_sum = np.zeros(2, np.int64)
         t_e = time.perf_counter()
         for _ in range(k_e2e):
             w += 1
@@ -856,13 +857,16 @@ def main():
                                        C.byref(o))
             if rc != N.PT_OK:
                 raise RuntimeError(f"e2e step failed: {N.last_error()}")
+            xfer = np.zeros(2, np.int64)
+            L.pt_last_transfer_bytes(xfer.ctypes.data_as(C.c_void_p))
+            xfer_sum += xfer
         el_e = time.perf_counter() - t_e
         acc_e = float(h_cnt[:, 1].sum()) - e2e_acc0
-        bytes_in = tg.nbytes + h_state.numel() * 8 + h_cnt.numel() * 8 + h_carry.numel()
-        bytes_out = h_state.numel() * 8 + h_cnt.numel() * 8 + h_carry.numel() + h_status.numel() * 4
         line["e2e"] = {"value": acc_e / el_e, "unit": "particle-steps/s",
-                       "h2d_bytes_per_step": int(bytes_in), "d2h_bytes_per_step": int(bytes_out),
-                       "steps": k_e2e, "api": "pt_integrate_fields (host pinned buffers)"}
+                       "h2d_bytes_per_step": int(xfer_sum[0] // k_e2e),
+                       "d2h_bytes_per_step": int(xfer_sum[1] // k_e2e),
+                       "steps": k_e2e, "api": "pt_integrate_fields (host pinned buffers: "
+                       "state(8,m,np), counters, carry, status in and out every step)"}
 
     if not args.no_cpu and rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline(cfg, prm, tg, out, s0, window, args.warmup,

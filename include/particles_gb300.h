@@ -134,6 +134,12 @@ int64_t pt_fields_bytes(const pt_fields *f);
 int pt_integrate_fields(int32_t method, int64_t np, int32_t m, const pt_fields *f,
                         const double params[17], const double *time,
                         double *state, int64_t *cnt, const pt_options *opt);
+/* Bytes the calling thread's last pt_integrate_fields (or pt_integrate)
+ * moved host -> device (out[0]) and device -> host (out[1]).  Only what a
+ * call reads or writes crosses: the first row of each particle, the carry
+ * and the counters in; the output rows each particle wrote, the counters, the
+ * carry and the status out. */
+int pt_last_transfer_bytes(int64_t out[2]);
 
 /* ---- device-resident run (inputs already in HBM) ------------------------ */
 

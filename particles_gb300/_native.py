@@ -31,7 +31,7 @@ EXPORTS = [
     "pt_mlp_infer", "pt_mlp_loss_grad", "pt_mlp_adam", "pt_autotune",
     "pt_ensemble_create", "pt_ensemble_destroy", "pt_ensemble_run", "pt_ensemble_capture",
     "pt_ensemble_replay", "pt_ensemble_counts", "pt_ensemble_escaped", "pt_ensemble_check",
-    "pt_copy_rows", "pt_debug_ctl_pow",
+    "pt_copy_rows", "pt_debug_ctl_pow", "pt_last_transfer_bytes",
 ]
 
 
@@ -99,6 +99,7 @@ def load():
     L.pt_ensemble_escaped.argtypes = [vp, i32, vp, i64, C.POINTER(i64)]
     L.pt_ensemble_check.argtypes = [vp]
     L.pt_copy_rows.argtypes = [vp, i64, i32, i32, i32, vp, vp]
+    L.pt_last_transfer_bytes.argtypes = [vp]
     L.pt_last_error.restype = C.c_char_p
     L.pt_abi_version.restype = i32
     L.pt_tableau.argtypes = [i32, vp]

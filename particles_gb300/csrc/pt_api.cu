@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <vector>
 #include <math.h>
 #include <stdio.h>
 #include <string.h>
@@ -72,7 +73,14 @@ struct pt_fields {
     int32_t nc16;               /* BF16 record width: 8 or 16 */
     int64_t bytes;
     unsigned long long *scratch;   /* [0] queue head, [1] flags (2 x int32) */
+    unsigned char *ws;          /* host-buffer runs: device copies, reused across calls */
+    size_t ws_bytes;
+    unsigned char *pack;        /* host-buffer runs: the output rows a call wrote, packed */
+    size_t pack_bytes;
 };
+
+/* Bytes the last host-buffer run moved between host and device. */
+static thread_local int64_t g_xfer[2] = { 0, 0 };
 
 /* Planar reference layout -> node records { U, B, (J, 0) }. */
 __global__ void k_pack_records64(int64_t nn, const double *__restrict__ uu,
@@ -306,6 +314,8 @@ extern "C" int pt_fields_destroy(pt_fields *f)
     cudaFree(f->rec16);
     cudaFree(f->bscale);
     cudaFree(f->scratch);
+    cudaFree(f->ws);
+    cudaFree(f->pack);
     delete f;
     return PT_OK;
 }
@@ -671,57 +681,163 @@ extern "C" int pt_run_check(const pt_fields *f)
     return PT_OK;
 }
 
-extern "C" int pt_integrate_fields(int32_t method, int64_t np, int32_t m, const pt_fields *f,
+/* Rows [start, n1) of each particle, where start is the next output row
+ * when the call began (0 for a particle that starts fresh) and n1 the next
+ * row after it: the only rows a call can write. */
+__global__ void k_rows_written(int64_t np, const int32_t *__restrict__ nf0,
+                               const int32_t *__restrict__ n1, int64_t *__restrict__ count)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t start = (nf0[np + p] & 1) ? nf0[p] : 0;
+        const int32_t c = n1[p] - start;
+        count[p] = c > 0 ? c : 0;
+    }
+}
+
+/* Packs the written rows of every particle at its offset (64-B rows). */
+__global__ void k_pack_rows(int64_t np, int32_t m, const int32_t *__restrict__ nf0,
+                            const int64_t *__restrict__ off, const int64_t *__restrict__ count,
+                            const double2 *__restrict__ state, double2 *__restrict__ pack)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t start = (nf0[np + p] & 1) ? nf0[p] : 0;
+        const double2 *src = state + 4 * (start + (int64_t)m * p);
+        double2 *dst = pack + 4 * off[p];
+        for (int64_t i = 0; i < 4 * count[p]; ++i) dst[i] = src[i];
+    }
+}
+
+static size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+/* Host buffers in, host buffers out (pt_integrate_fields): the device copies
+ * live in a workspace of the field handle, reused across calls.  Only what a
+ * call reads or writes crosses the link: in, the output times, the first row
+ * of each particle (initial state) and, with a carry, the carry and the
+ * counters; out, the rows each particle wrote (packed on the device, placed
+ * on the host), the counters, the carry and the status.  Rows a call does
+ * not touch keep their host values. */
+extern "C" int pt_integrate_fields(int32_t method, int64_t np, int32_t m, const pt_fields *fc,
                                    const double params[17], const double *time, double *state,
                                    int64_t *cnt, const pt_options *opt)
 {
     if (np < 0 || m < 1) return set_err(PT_ERR_ARG, "np < 0 or m < 1%s");
     if (np > 0 && (!time || !state || !cnt)) return set_err(PT_ERR_ARG, "NULL buffer%s");
+    if (!fc) return set_err(PT_ERR_ARG, "fields handle is NULL%s");
+    g_xfer[0] = g_xfer[1] = 0;
     if (np == 0) return PT_OK;
-    int rc = PT_OK;
-    double *d_time = nullptr, *d_state = nullptr;
-    int64_t *d_cnt = nullptr;
-    int32_t *d_status = nullptr;
-    void *d_carry = nullptr;
-    const size_t sbytes = (size_t)8 * m * np * sizeof(double);
-    const size_t cbytes = (size_t)3 * np * sizeof(int64_t);
-    int32_t *h_status = opt ? opt->status : nullptr;
-    void *h_carry = opt ? opt->carry : nullptr;
     if (opt && (opt->records || opt->order))
         return set_err(PT_ERR_UNSUPPORTED, "records and order are device-API options (pt_run_device)%s");
+    pt_fields *f = const_cast<pt_fields *>(fc);
+    int rc = PT_OK;
+    int32_t *h_status = opt ? opt->status : nullptr;
+    void *h_carry = opt ? opt->carry : nullptr;
+    const size_t crb = (size_t)pt_carry_bytes(np);
+    const size_t o_time = 0, o_state = up256(o_time + (size_t)m * 8);
+    const size_t o_cnt = up256(o_state + (size_t)np * m * 64), o_status = up256(o_cnt + (size_t)np * 24);
+    const size_t o_carry = up256(o_status + (size_t)np * 4), o_nf0 = up256(o_carry + crb);
+    const size_t o_count = up256(o_nf0 + (size_t)np * 8), o_off = up256(o_count + (size_t)np * 8);
+    const size_t need = up256(o_off + (size_t)np * 8);
     cudaStream_t s = nullptr;
+    std::vector<int64_t> hcount, hoff;
+    int64_t rows = 0;
+    const int grid = (int)((np + 255) / 256 < 4096 ? (np + 255) / 256 : 4096);
     PT_CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    PT_CU(cudaMalloc(&d_time, (size_t)m * sizeof(double)));
-    PT_CU(cudaMalloc(&d_state, sbytes));
-    PT_CU(cudaMalloc(&d_cnt, cbytes));
-    PT_CU(cudaMalloc(&d_status, (size_t)np * sizeof(int32_t)));
-    PT_CU(cudaMemcpyAsync(d_time, time, (size_t)m * sizeof(double), cudaMemcpyHostToDevice, s));
-    PT_CU(cudaMemcpyAsync(d_state, state, sbytes, cudaMemcpyHostToDevice, s));
-    if (h_carry) {
-        PT_CU(cudaMalloc(&d_carry, (size_t)pt_carry_bytes(np)));
-        PT_CU(cudaMemcpyAsync(d_carry, h_carry, (size_t)pt_carry_bytes(np), cudaMemcpyHostToDevice, s));
-        PT_CU(cudaMemcpyAsync(d_cnt, cnt, cbytes, cudaMemcpyHostToDevice, s));
+    if (f->ws_bytes < need) {
+        cudaFree(f->ws);
+        f->ws = nullptr;
+        f->ws_bytes = 0;
+        PT_CU(cudaMalloc(&f->ws, need));
+        f->ws_bytes = need;
     }
-    rc = run_impl(method, np, m, f, params, d_time, d_state, d_cnt, d_status, d_carry, opt, s);
-    if (rc != PT_OK) goto done;
-    PT_CU(cudaMemcpyAsync(state, d_state, sbytes, cudaMemcpyDeviceToHost, s));
-    PT_CU(cudaMemcpyAsync(cnt, d_cnt, cbytes, cudaMemcpyDeviceToHost, s));
-    if (h_status)
-        PT_CU(cudaMemcpyAsync(h_status, d_status, (size_t)np * sizeof(int32_t),
-                              cudaMemcpyDeviceToHost, s));
-    if (h_carry)
-        PT_CU(cudaMemcpyAsync(h_carry, d_carry, (size_t)pt_carry_bytes(np), cudaMemcpyDeviceToHost, s));
-    PT_CU(cudaStreamSynchronize(s));
+    {
+        unsigned char *w = f->ws;
+        double *d_time = reinterpret_cast<double *>(w + o_time);
+        double *d_state = reinterpret_cast<double *>(w + o_state);
+        int64_t *d_cnt = reinterpret_cast<int64_t *>(w + o_cnt);
+        int32_t *d_status = reinterpret_cast<int32_t *>(w + o_status);
+        unsigned char *d_carry = w + o_carry;
+        int32_t *d_nf0 = reinterpret_cast<int32_t *>(w + o_nf0);
+        int64_t *d_count = reinterpret_cast<int64_t *>(w + o_count);
+        int64_t *d_off = reinterpret_cast<int64_t *>(w + o_off);
+        int32_t *d_n = reinterpret_cast<int32_t *>(d_carry + (size_t)np * 15 * 8);  /* carry n[], flags[] */
+        PT_CU(cudaMemcpyAsync(d_time, time, (size_t)m * 8, cudaMemcpyHostToDevice, s));
+        PT_CU(cudaMemcpy2DAsync(d_state, (size_t)m * 64, state, (size_t)m * 64, 64, (size_t)np,
+                                cudaMemcpyHostToDevice, s));
+        g_xfer[0] += (int64_t)m * 8 + np * 64;
+        if (h_carry) {
+            PT_CU(cudaMemcpyAsync(d_carry, h_carry, crb, cudaMemcpyHostToDevice, s));
+            PT_CU(cudaMemcpyAsync(d_cnt, cnt, (size_t)np * 24, cudaMemcpyHostToDevice, s));
+            g_xfer[0] += (int64_t)crb + np * 24;
+        } else {
+            PT_CU(cudaMemsetAsync(d_carry, 0, crb, s));              /* every particle fresh */
+        }
+        PT_CU(cudaMemcpyAsync(d_nf0, d_n, (size_t)np * 8, cudaMemcpyDeviceToDevice, s));
+        rc = run_impl(method, np, m, f, params, d_time, d_state, d_cnt, d_status, d_carry, opt, s);
+        if (rc != PT_OK) goto done;
+        k_rows_written<<<grid, 256, 0, s>>>(np, d_nf0, d_n, d_count);
+        PT_CU(cudaGetLastError());
+        hcount.resize(np);
+        hoff.resize(np + 1);
+        PT_CU(cudaMemcpyAsync(hcount.data(), d_count, (size_t)np * 8, cudaMemcpyDeviceToHost, s));
+        PT_CU(cudaStreamSynchronize(s));
+        hoff[0] = 0;
+        for (int64_t p = 0; p < np; ++p) hoff[p + 1] = hoff[p] + hcount[p];
+        rows = hoff[np];
+        PT_CU(cudaMemcpyAsync(d_off, hoff.data(), (size_t)np * 8, cudaMemcpyHostToDevice, s));
+        if (f->pack_bytes < (size_t)rows * 64) {
+            cudaFree(f->pack);
+            f->pack = nullptr;
+            f->pack_bytes = 0;
+            PT_CU(cudaMalloc(&f->pack, (size_t)rows * 64));
+            f->pack_bytes = (size_t)rows * 64;
+        }
+        if (rows > 0) {
+            k_pack_rows<<<grid, 256, 0, s>>>(np, m, d_nf0, d_off, d_count,
+                                             reinterpret_cast<const double2 *>(d_state),
+                                             reinterpret_cast<double2 *>(f->pack));
+            PT_CU(cudaGetLastError());
+        }
+        /* the packed rows go to a staging copy, then to their places */
+        std::vector<double> staged((size_t)rows * 8);
+        if (rows > 0)
+            PT_CU(cudaMemcpyAsync(staged.data(), f->pack, (size_t)rows * 64, cudaMemcpyDeviceToHost, s));
+        PT_CU(cudaMemcpyAsync(cnt, d_cnt, (size_t)np * 24, cudaMemcpyDeviceToHost, s));
+        g_xfer[1] += rows * 64 + np * 24;
+        if (h_status) {
+            PT_CU(cudaMemcpyAsync(h_status, d_status, (size_t)np * 4, cudaMemcpyDeviceToHost, s));
+            g_xfer[1] += np * 4;
+        }
+        if (h_carry) {
+            PT_CU(cudaMemcpyAsync(h_carry, d_carry, crb, cudaMemcpyDeviceToHost, s));
+            g_xfer[1] += (int64_t)crb;
+        }
+        std::vector<int32_t> start(np);
+        PT_CU(cudaMemcpyAsync(start.data(), d_nf0, (size_t)np * 4, cudaMemcpyDeviceToHost, s));
+        std::vector<int32_t> flag0(np);
+        PT_CU(cudaMemcpyAsync(flag0.data(), d_nf0 + np, (size_t)np * 4, cudaMemcpyDeviceToHost, s));
+        PT_CU(cudaStreamSynchronize(s));
+        for (int64_t p = 0; p < np; ++p) {
+            if (!hcount[p]) continue;
+            const int64_t r0 = (flag0[p] & 1) ? start[p] : 0;
+            memcpy(state + 8 * (r0 + (int64_t)m * p), staged.data() + 8 * hoff[p],
+                   (size_t)hcount[p] * 64);
+        }
+    }
     rc = pt_run_check(f);
 done:
     if (s) cudaStreamSynchronize(s);
-    cudaFree(d_time);
-    cudaFree(d_state);
-    cudaFree(d_cnt);
-    cudaFree(d_status);
-    cudaFree(d_carry);
     if (s) cudaStreamDestroy(s);
     return rc;
+}
+
+extern "C" int pt_last_transfer_bytes(int64_t out[2])
+{
+    if (!out) return set_err(PT_ERR_ARG, "NULL argument%s");
+    out[0] = g_xfer[0];
+    out[1] = g_xfer[1];
+    return PT_OK;
 }
 
 extern "C" int pt_integrate(int32_t method, int64_t np, int32_t m, const int32_t dm[3],

@@ -177,3 +177,30 @@ def test_controller_pow_of_the_fast_builds(cuda, oracle_lib):
     assert rel.max() < 8 * 2.2e-16, rel.max()          # two Newton steps + rounding
     ref = np.array([oracle_lib.det_pow(a, b) for a, b in zip(q[6001:], y[6001:])])
     assert np.array_equal(got[6001:], ref)             # outside the Newton range: same bits
+
+
+def test_host_buffer_calls_move_only_the_rows_they_write(cuda, oracle_lib):
+    """pt_integrate_fields copies in the first row (and the carry), copies out
+    only the rows each particle wrote: host rows beyond the window keep their
+    values, and the result equals the oracle's windowed run."""
+    import oracle
+    from particles_gb300 import Fields, carry_buffer
+    from particles_gb300 import _native as N
+    prob = small_problem("dop853", n=16, npart=150, periods=2.0, seed=81, nsteps=20)
+    uu, bb = prob["fields"]
+    T0 = 2.0 * np.pi / 200.0
+    f = Fields(uu, bb)
+    s = prob["state"].copy()
+    s[:, 1:, :] = 12345.0                              # sentinel in every output row
+    c = np.zeros((s.shape[0], 3), np.int64)
+    carry = carry_buffer(s.shape[0])
+    f.integrate("dop853", prob["params"], prob["time"], s, c, carry=carry, t_stop=0.7 * T0)
+    xfer = np.zeros(2, np.int64)
+    N.load().pt_last_transfer_bytes(xfer.ctypes.data_as(C.c_void_p))
+    assert 0 < xfer[1] < s.nbytes                       # far less than the whole state out
+    n_done = int(np.searchsorted(prob["time"], 0.7 * T0, side="right"))
+    assert (s[:, n_done + 2:, :] == 12345.0).all()      # rows beyond the window untouched
+    f.integrate("dop853", prob["params"], prob["time"], s, c, carry=carry)
+    so, co, _ = oracle.integrate("dop853", prob["params"], prob["time"], uu, bb,
+                                 prob["state"].copy())
+    assert np.array_equal(c, co) and np.array_equal(s, so)
