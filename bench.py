@@ -400,9 +400,9 @@ def mixed_leg(args, dev, stream):
     rates = {}
     model = None
     for name, prec in (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"),
-                       ("bf16", "bf16"), ("fp32_learned", "fp32")):
+                       ("bf16", "bf16"), ("fp32_learned", "fp32"), ("bf16_learned", "bf16")):
         f = handles[prec]
-        mdl = model if name == "fp32_learned" else None
+        mdl = model if name.endswith("_learned") else None
         st, cnt, status, carry = fresh(npart)
         launch = tune(args, f, "rk5", prm, d_time, st, stream, window * T0, model=mdl)
         ordq = QueueOrder(torch, cnt, enabled=not args.no_order)
@@ -459,6 +459,10 @@ def mixed_leg(args, dev, stream):
     out["mixed_learned_over_plain_exact"] = rates["fp32_learned"]["value"] / rates["fp64"]["value"]
     out["physics_rate_mixed_learned_over_plain_exact"] = (
         rates["fp32_learned"]["particle_gyroperiods_per_s"]
+        / rates["fp64"]["particle_gyroperiods_per_s"])
+    out["bf16_learned_over_plain_exact"] = rates["bf16_learned"]["value"] / rates["fp64"]["value"]
+    out["physics_rate_bf16_learned_over_plain_exact"] = (
+        rates["bf16_learned"]["particle_gyroperiods_per_s"]
         / rates["fp64"]["particle_gyroperiods_per_s"])
 
     # accuracy: a seeded subsample integrated as far as the time budget allows

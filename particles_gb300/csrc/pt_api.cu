@@ -492,8 +492,6 @@ static int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
     PtRun R;
     int rc = prepare_run(method, np, m, shape_of(f), params, opt, R);
     if (rc != PT_OK) return rc;
-    if (f->precision == PT_PREC_BF16 && (R.mlp || R.rec))
-        return set_err(PT_ERR_UNSUPPORTED, "the learned controller and step records need FP32 or FP64 fields%s");
     attach_fields(f, R);
     R.time = d_time;
     R.state = d_state;
@@ -529,8 +527,6 @@ extern "C" int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_field
     PtRun R;
     int rc = prepare_run(method, np, m, shape_of(f), params, opt, R);
     if (rc != PT_OK) return rc;
-    if (f->precision == PT_PREC_BF16 && (R.mlp || R.rec))
-        return set_err(PT_ERR_UNSUPPORTED, "the learned controller and step records need FP32 or FP64 fields%s");
     cudaStream_t s = (cudaStream_t)stream;
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);

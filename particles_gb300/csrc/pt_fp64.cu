@@ -65,9 +65,6 @@ __device__ __forceinline__ void load_rec(const double *__restrict__ fld, int64_t
 template <int NC>
 struct EvalF64 {
     static constexpr bool kDelta = false;
-    using Rec = double;
-    static constexpr int NCR = NC;
-    static __device__ __forceinline__ const double *records(const PtRun &P) { return P.fld; }
     struct Origin {};
     static __device__ __forceinline__ void begin(const PtRun &, const double *, Origin &) {}
     static __device__ __forceinline__ void feature_cell(const PtRun &P, const double si[6],
@@ -75,6 +72,11 @@ struct EvalF64 {
                                                         float xd[3])
     {
         pt_feature_cell(P, si, l, r, xd);
+    }
+    static __device__ __forceinline__ PtRecordCorners<double, NC>
+    feature_loader(const PtRun &P, const int32_t l[3], const int32_t r[3])
+    {
+        return PtRecordCorners<double, NC>(P, P.fld, l, r);
     }
     static __device__ __forceinline__ void f(const PtRun &P, const double s[6], const double *,
                                              const Origin &, double a[6])

@@ -631,8 +631,8 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
                     int32_t fl_[3], fr_[3];
                     float fx_[3];
                     EV::feature_cell(PT_Q, si, O, fl_, fr_, fx_);
-                    pt_field_features<typename EV::Rec, EV::NCR>(PT_Q, EV::records(PT_Q), si, fl_, fr_,
-                                                                 fx_, feat);
+                    const auto ld_ = EV::feature_loader(PT_Q, fl_, fr_);
+                    pt_field_features(PT_Q, ld_, si, fx_, feat);
                     const float om = PT_Q.qomf * __expf(feat[0] - feat[2]);     /* qom |B| / gamma */
                     const float dtf = pt_d2f(dt);
                     feat[5] = __logf(om * dtf + 1e-30f);

@@ -47,7 +47,6 @@ namespace {
 template <int NC>
 struct GatherF32 {
     static constexpr int NV = (NC == 12) ? 9 : 6;
-    static constexpr int NCR = NC;            /* record width for the feature gather */
     static __device__ __forceinline__ void load(const float *__restrict__ fld, int64_t node,
                                                 float v[NC])
     {
@@ -60,6 +59,12 @@ struct GatherF32 {
             v[4 * i + 2] = x.z;
             v[4 * i + 3] = x.w;
         }
+    }
+    using Loader = PtRecordCorners<float, NC>;
+    static __device__ __forceinline__ Loader loader(const PtRun &P, const int32_t l[3],
+                                                    const int32_t r[3])
+    {
+        return Loader(P, P.fld32, l, r);
     }
     static __device__ __forceinline__ void gather(const PtRun &P, const int32_t l[3],
                                                   const int32_t r[3], const float w8[8],
@@ -95,7 +100,6 @@ struct GatherF32 {
 template <int NC16>
 struct GatherBrick {
     static constexpr int NV = (NC16 == 16) ? 9 : 6;
-    static constexpr int NCR = 8;             /* unused: no learned controller on bricks */
     static constexpr int NS = (NC16 == 16) ? 20 : 12;   /* floats per brick: (offset, scale) pairs */
     static __device__ __forceinline__ float lo(uint32_t w) { return __uint_as_float(w << 16); }
     static __device__ __forceinline__ float hi(uint32_t w) { return __uint_as_float(w & 0xffff0000u); }
@@ -110,6 +114,36 @@ struct GatherBrick {
             const uint4 b = __ldg(fld + node * (NC16 / 8) + 1);
             v[8 % NV] = lo(b.x);
         }
+    }
+    /* Corner loader for the learned controller's features: the brick of l
+     * holds every corner (halo), one scale load per call. */
+    struct Loader {
+        static constexpr int NJ = (NV == 9) ? 3 : 0;
+        const uint4 *fld;
+        int64_t base;
+        float os[NS];
+        __device__ __forceinline__ void corner(int bx, int by, int bz, float v[9]) const
+        {
+            float t[NV];
+            load_node(fld, base + bx + 9 * by + 81 * bz, t);
+#pragma unroll
+            for (int c = 0; c < NV; ++c) v[c] = fmaf(os[2 * c + 1], t[c], os[2 * c]);
+        }
+    };
+    static __device__ __forceinline__ Loader loader(const PtRun &P, const int32_t l[3],
+                                                    const int32_t *)
+    {
+        Loader L;
+        const int64_t b = (l[0] >> 3) + (int64_t)P.nb[0] * ((l[1] >> 3) + (int64_t)P.nb[1] * (l[2] >> 3));
+        L.fld = P.fld16;
+        L.base = b * 729 + (l[0] & 7) + 9 * (l[1] & 7) + 81 * (l[2] & 7);
+        const float4 *sp = reinterpret_cast<const float4 *>(P.bscale + b * NS);
+#pragma unroll
+        for (int i = 0; i < NS / 4; ++i) {
+            const float4 x = __ldg(sp + i);
+            L.os[4 * i] = x.x; L.os[4 * i + 1] = x.y; L.os[4 * i + 2] = x.z; L.os[4 * i + 3] = x.w;
+        }
+        return L;
     }
     static __device__ __forceinline__ void gather(const PtRun &P, const int32_t l[3],
                                                   const int32_t *, const float w8[8], float acc[NV])
@@ -143,9 +177,6 @@ struct GatherBrick {
 template <class G>
 struct EvalMixed {
     static constexpr bool kDelta = true;
-    using Rec = float;
-    static constexpr int NCR = G::NCR;
-    static __device__ __forceinline__ const float *records(const PtRun &P) { return P.fld32; }
     /* Cell of si and the offset of si inside it (FP32), fixed for one attempt. */
     struct Origin {
         int32_t cell[3];
@@ -162,6 +193,12 @@ struct EvalMixed {
             O.off[i] = pt_d2f(xn - fl);
             O.cell[i] = (int32_t)fl;          /* beyond 2^31 cells it saturates */
         }
+    }
+
+    static __device__ __forceinline__ typename G::Loader
+    feature_loader(const PtRun &P, const int32_t l[3], const int32_t r[3])
+    {
+        return G::loader(P, l, r);
     }
 
     /* The cell of si for the learned controller's features: the origin. */
@@ -313,8 +350,7 @@ cudaError_t launch_v(const PtRun &P, cudaStream_t s)
     }
 }
 
-/* LEARNABLE: the store supports the learned controller's feature gather
- * (FP32 records); BF16 bricks run the classical controller only. */
+/* LEARNABLE: the learned-controller (and step-record) variants exist. */
 template <int METHOD, class EV, bool LEARNABLE>
 cudaError_t launch(const PtRun &P, cudaStream_t s)
 {
@@ -347,7 +383,7 @@ cudaError_t pt_launch_rk5_ens_mixed(const PtRun *tab, int nmem, int nc, int minb
 
 cudaError_t pt_launch_rk5_bf16(const PtRun &P, int nc, cudaStream_t s)
 {
-    return nc == 16 ? launch<PT_METHOD_RK5, B16_16, false>(P, s) : launch<PT_METHOD_RK5, B16_8, false>(P, s);
+    return nc == 16 ? launch<PT_METHOD_RK5, B16_16, true>(P, s) : launch<PT_METHOD_RK5, B16_8, true>(P, s);
 }
 
 cudaError_t pt_launch_rk5_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
@@ -374,8 +410,8 @@ cudaError_t pt_launch_dp853_ens_mixed(const PtRun *tab, int nmem, int nc, int mi
 
 cudaError_t pt_launch_dp853_bf16(const PtRun &P, int nc, cudaStream_t s)
 {
-    return nc == 16 ? launch<PT_METHOD_DOP853, B16_16, false>(P, s)
-                    : launch<PT_METHOD_DOP853, B16_8, false>(P, s);
+    return nc == 16 ? launch<PT_METHOD_DOP853, B16_16, true>(P, s)
+                    : launch<PT_METHOD_DOP853, B16_8, true>(P, s);
 }
 
 cudaError_t pt_launch_dp853_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,

@@ -121,11 +121,12 @@ static __device__ __noinline__ float pt_mlp_warp(const PtMlpSmem &M, const float
     for (int i = 0; i < 4; ++i)
         xp[i] = pt_pack_h2((x[2 * i] - M.mu[2 * i]) * M.isd[2 * i],
                            (x[2 * i + 1] - M.mu[2 * i + 1]) * M.isd[2 * i + 1]);
-    float out = 0.0f;
+    /* the warp's 32 rows are two m16 tiles; every weight fragment and bias is
+     * loaded once and applied to both */
+    uint32_t a1[2][4];
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt) {
         /* layer-1 A fragment: rows g and g + 8 of this m tile, columns 2q, 2q+1 */
-        uint32_t a1[4];
         const int r0 = 16 * mt + g, r1 = r0 + 8;
         uint32_t v0 = 0, v1 = 0;
 #pragma unroll
@@ -134,45 +135,62 @@ static __device__ __noinline__ float pt_mlp_warp(const PtMlpSmem &M, const float
             const uint32_t s1 = __shfl_sync(0xffffffffu, xp[i], r1);
             if (q == i) { v0 = s0; v1 = s1; }
         }
-        a1[0] = v0; a1[1] = v1; a1[2] = 0u; a1[3] = 0u;
-        /* layer 1 -> SiLU -> layer-2 A fragments */
-        uint32_t a2[4][4];
+        a1[mt][0] = v0; a1[mt][1] = v1; a1[mt][2] = 0u; a1[mt][3] = 0u;
+    }
+    const float2 *b1 = reinterpret_cast<const float2 *>(M.b1);
+    const float2 *b2 = reinterpret_cast<const float2 *>(M.b2);
+    /* layer 1 -> SiLU -> layer-2 A fragments */
+    uint32_t a2[2][4][4];
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            float c[4];
-            c[0] = c[2] = M.b1[8 * nt + 2 * q];
-            c[1] = c[3] = M.b1[8 * nt + 2 * q + 1];
-            pt_mma16816(c, a1, M.frag[PT_MLP_FRAG_W1 + nt * 32 + lane]);
-            const int kt = nt >> 1, hiw = (nt & 1) * 2;
-            a2[kt][hiw] = pt_silu_h2(c[0], c[1]);
-            a2[kt][hiw + 1] = pt_silu_h2(c[2], c[3]);
+    for (int nt = 0; nt < 8; ++nt) {
+        const float2 bb = b1[4 * nt + q];
+        const uint2 w = M.frag[PT_MLP_FRAG_W1 + nt * 32 + lane];
+        const int kt = nt >> 1, hiw = (nt & 1) * 2;
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            float c[4] = { bb.x, bb.y, bb.x, bb.y };
+            pt_mma16816(c, a1[mt], w);
+            a2[mt][kt][hiw] = pt_silu_h2(c[0], c[1]);
+            a2[mt][kt][hiw + 1] = pt_silu_h2(c[2], c[3]);
         }
-        /* layer 2 -> SiLU -> layer 3, one k16 slice of layer 3 per pair of
-         * layer-2 n tiles (keeps 4 fragment registers live instead of 16);
-         * column 0 of layer 3's n8 tile is the output */
-        float c3[4] = { M.b3[0], 0.0f, M.b3[0], 0.0f };
+    }
+    /* layer 2 -> SiLU -> layer 3, one k16 slice of layer 3 per pair of
+     * layer-2 n tiles; column 0 of layer 3's n8 tile is the output */
+    float c3[2][4];
 #pragma unroll
-        for (int kt3 = 0; kt3 < 4; ++kt3) {
-            uint32_t a3[4];
+    for (int mt = 0; mt < 2; ++mt) { c3[mt][0] = c3[mt][2] = M.b3[0]; c3[mt][1] = c3[mt][3] = 0.0f; }
 #pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int nt = 2 * kt3 + h;
-                float c[4];
-                c[0] = c[2] = M.b2[8 * nt + 2 * q];
-                c[1] = c[3] = M.b2[8 * nt + 2 * q + 1];
+    for (int kt3 = 0; kt3 < 4; ++kt3) {
+        uint32_t a3[2][4];
 #pragma unroll
-                for (int kt = 0; kt < 4; ++kt)
-                    pt_mma16816(c, a2[kt], M.frag[PT_MLP_FRAG_W2 + (kt * 8 + nt) * 32 + lane]);
-                a3[2 * h] = pt_silu_h2(c[0], c[1]);
-                a3[2 * h + 1] = pt_silu_h2(c[2], c[3]);
+        for (int h = 0; h < 2; ++h) {
+            const int nt = 2 * kt3 + h;
+            const float2 bb = b2[4 * nt + q];
+            float c[2][4] = { { bb.x, bb.y, bb.x, bb.y }, { bb.x, bb.y, bb.x, bb.y } };
+#pragma unroll
+            for (int kt = 0; kt < 4; ++kt) {
+                const uint2 w = M.frag[PT_MLP_FRAG_W2 + (kt * 8 + nt) * 32 + lane];
+                pt_mma16816(c[0], a2[0][kt], w);
+                pt_mma16816(c[1], a2[1][kt], w);
             }
-            pt_mma16816(c3, a3, M.frag[PT_MLP_FRAG_W3 + kt3 * 32 + lane]);
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+                a3[mt][2 * h] = pt_silu_h2(c[mt][0], c[mt][1]);
+                a3[mt][2 * h + 1] = pt_silu_h2(c[mt][2], c[mt][3]);
+            }
         }
-        /* row r0 sits in c0 of lane 4g, row r1 in c2 of lane 4g (q == 0) */
+        const uint2 w3 = M.frag[PT_MLP_FRAG_W3 + kt3 * 32 + lane];
+        pt_mma16816(c3[0], a3[0], w3);
+        pt_mma16816(c3[1], a3[1], w3);
+    }
+    /* row r0 of tile mt sits in c0 of lane 4g, row r1 in c2 of lane 4g (q == 0) */
+    float out = 0.0f;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt) {
         const int r = lane - 16 * mt;
         const int src = 4 * (r & 7);
-        const float y0 = __shfl_sync(0xffffffffu, c3[0], src);
-        const float y1 = __shfl_sync(0xffffffffu, c3[2], src);
+        const float y0 = __shfl_sync(0xffffffffu, c3[mt][0], src);
+        const float y1 = __shfl_sync(0xffffffffu, c3[mt][2], src);
         if (r >= 0 && r < 16) out = (r < 8) ? y0 : y1;
     }
     return out;
@@ -217,48 +235,67 @@ __device__ __forceinline__ void pt_feature_cell(const PtRun &P, const double s[6
     }
 }
 
-/* One record's U, B (and J) as floats: vector loads of the FP32 or FP64
- * records (16-B aligned). */
-template <int NCR>
-__device__ __forceinline__ void pt_feature_rec(const float *fld, int64_t node, float v[NCR])
-{
-    const float4 *q = reinterpret_cast<const float4 *>(fld + node * NCR);
-#pragma unroll
-    for (int i = 0; i < NCR / 4; ++i) {
-        const float4 x = __ldg(q + i);
-        v[4 * i] = x.x; v[4 * i + 1] = x.y; v[4 * i + 2] = x.z; v[4 * i + 3] = x.w;
+/* Corner loaders of the feature gather: corner (bx, by, bz) of the cell
+ * (l, r) as floats U[3], B[3] (and J[3] when NJ == 3).  Node records in
+ * x-fastest order, FP64 or FP32, with vector loads. */
+template <class REC, int NCR>
+struct PtRecordCorners {
+    static constexpr int NJ = (NCR >= 9) ? 3 : 0;
+    const REC *fld;
+    int64_t lo[3], hi[3];              /* l and r scaled by the node strides */
+    __device__ __forceinline__ PtRecordCorners(const PtRun &P, const REC *f, const int32_t l[3],
+                                               const int32_t r[3])
+        : fld(f)
+    {
+        const int64_t d1 = P.dm[0], d12 = (int64_t)P.dm[0] * P.dm[1];
+        lo[0] = l[0]; hi[0] = r[0];
+        lo[1] = d1 * l[1]; hi[1] = d1 * r[1];
+        lo[2] = d12 * l[2]; hi[2] = d12 * r[2];
     }
-}
-template <int NCR>
-__device__ __forceinline__ void pt_feature_rec(const double *fld, int64_t node, float v[NCR])
-{
-    const double2 *q = reinterpret_cast<const double2 *>(fld + node * NCR);
-#pragma unroll
-    for (int i = 0; i < NCR / 2; ++i) {
-        const double2 x = __ldg(q + i);
-        v[2 * i] = pt_to_f(x.x); v[2 * i + 1] = pt_to_f(x.y);
+    __device__ __forceinline__ void corner(int bx, int by, int bz, float v[9]) const
+    {
+        const int64_t node = (bx ? hi[0] : lo[0]) + (by ? hi[1] : lo[1]) + (bz ? hi[2] : lo[2]);
+        load(node, v);
     }
-}
+    __device__ __forceinline__ void load(int64_t node, float v[9]) const
+    {
+        float t[NCR];
+        if (sizeof(REC) == 4) {
+            const float4 *q = reinterpret_cast<const float4 *>(fld + node * NCR);
+#pragma unroll
+            for (int i = 0; i < NCR / 4; ++i) {
+                const float4 x = __ldg(q + i);
+                t[4 * i] = x.x; t[4 * i + 1] = x.y; t[4 * i + 2] = x.z; t[4 * i + 3] = x.w;
+            }
+        } else {
+            const double2 *q = reinterpret_cast<const double2 *>(fld + node * NCR);
+#pragma unroll
+            for (int i = 0; i < NCR / 2; ++i) {
+                const double2 x = __ldg(q + i);
+                t[2 * i] = pt_to_f(x.x); t[2 * i + 1] = pt_to_f(x.y);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 6 + NJ; ++c) v[c] = t[c];
+    }
+};
 
 /* The five field invariants of the learned controller at the particle state
  * s, in FP32: log|B|, log|E|, log gamma, pitch cosine u.B/(|u||B|) and
  * log(|grad B|/|B|), with E = -U x B + eta J and grad B the analytic
  * derivative of the trilinear interpolant (the derivatives of the same eight
- * corner weights).  REC/NCR: record type and width of the field records;
- * (l, r, xd): the cell of s (pt_feature_cell, or the attempt origin of the
- * mixed evaluation). */
-template <class REC, int NCR>
-__device__ __forceinline__ void pt_field_features(const PtRun &P, const REC *fld, const double s[6],
-                                                  const int32_t l[3], const int32_t r[3],
+ * corner weights).  xd: the offset of s in its cell; LD: a corner loader
+ * (PtRecordCorners, or the brick loader of the BF16 store). */
+template <class LD>
+__device__ __forceinline__ void pt_field_features(const PtRun &P, const LD &ld, const double s[6],
                                                   const float xd[3], float out[5])
 {
     float xu[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) xu[i] = 1.0f - xd[i];
-    const int64_t d1 = P.dm[0], d12 = (int64_t)P.dm[0] * P.dm[1];
     float U[3] = { 0, 0, 0 }, B[3] = { 0, 0, 0 }, J[3] = { 0, 0, 0 };
     float G[3][3] = { { 0, 0, 0 }, { 0, 0, 0 }, { 0, 0, 0 } };
-    constexpr bool HJ = (NCR >= 9);
+    constexpr bool HJ = (LD::NJ == 3);
 #pragma unroll
     for (int qd = 0; qd < 8; ++qd) {
         const int bx = (qd >> 2) & 1, by = (qd >> 1) & 1, bz = qd & 1;
@@ -267,15 +304,14 @@ __device__ __forceinline__ void pt_field_features(const PtRun &P, const REC *fld
         const float gx = (bx ? 1.0f : -1.0f) * wy * wz * P.gsxf[0];
         const float gy = (by ? 1.0f : -1.0f) * wx * wz * P.gsxf[1];
         const float gz = (bz ? 1.0f : -1.0f) * wx * wy * P.gsxf[2];
-        const int64_t node = (bx ? r[0] : l[0]) + d1 * (by ? r[1] : l[1]) + d12 * (bz ? r[2] : l[2]);
-        float v[NCR];
-        pt_feature_rec<NCR>(fld, node, v);
+        float v[9];
+        ld.corner(bx, by, bz, v);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const float vu = v[c], vb = v[3 + c];
             U[c] = fmaf(w, vu, U[c]);
             B[c] = fmaf(w, vb, B[c]);
-            if (HJ) J[c] = fmaf(w, v[(6 + c) % NCR], J[c]);
+            if (HJ) J[c] = fmaf(w, v[6 + c], J[c]);
             G[c][0] = fmaf(gx, vb, G[c][0]);
             G[c][1] = fmaf(gy, vb, G[c][1]);
             G[c][2] = fmaf(gz, vb, G[c][2]);

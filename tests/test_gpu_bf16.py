@@ -92,20 +92,37 @@ def test_bf16_turbulent_statistics(cuda, oracle_lib, method):
     assert 0.7 < cg[:, 1].sum() / co[:, 1].sum() < 1.4
 
 
-def test_bf16_learned_controller_refused(cuda):
-    from particles_gb300 import Fields, learned
-    from particles_gb300 import _native as N
+def test_bf16_learned_controller_runs(cuda, oracle_lib):
+    """The learned controller on BF16 bricks (features gathered from the
+    brick records): every particle finishes, the energy statistics agree with
+    the FP64 oracle, and records written on bricks train a model."""
     torch = cuda
-    prob = small_problem("rk5", n=16, npart=32, periods=0.2, seed=3)
+    import oracle
+    from particles_gb300 import Fields, learned
+    prob = small_problem("rk5", n=16, npart=256, periods=1.0, seed=3)
     uu, bb = prob["fields"]
     f = Fields(uu, bb, precision="bf16")
-    norm = np.concatenate([np.zeros(8), np.ones(8), [-7.0, 1.0]]).astype(np.float32)
-    model = learned.Model(learned.init_params(1), norm)
+    npart = prob["state"].shape[0]
+    d_time = torch.tensor(prob["time"], device="cuda")
     s = torch.tensor(prob["state"], device="cuda")
-    c = torch.zeros((32, 3), dtype=torch.int64, device="cuda")
-    with pytest.raises(N.PtError) as e:
-        f.run_device("rk5", prob["params"], torch.tensor(prob["time"], device="cuda"), s, c,
-                     model=model)
-    assert e.value.code == N.PT_ERR_UNSUPPORTED
+    c = torch.zeros((npart, 3), dtype=torch.int64, device="cuda")
+    rec = learned.record_buffer(torch, 200000)
+    f.run_device("rk5", prob["params"], d_time, s, c, records=rec)
+    torch.cuda.synchronize()
+    assert f.run_check() == 0
+    X, T = learned.dataset(learned.records_from_buffer(rec), "rk5")
+    assert X.shape[0] > 1000 and np.isfinite(X).all()
+    norm = learned.normalisation(X, T)
+    pm, _ = learned.train(torch, X, T, norm, epochs=2, batch=4096, lr=2e-3)
+    model = learned.Model(pm, norm, safety=0.9)
+    s = torch.tensor(prob["state"], device="cuda")
+    c = torch.zeros((npart, 3), dtype=torch.int64, device="cuda")
+    st = torch.zeros(npart, dtype=torch.int32, device="cuda")
+    f.run_device("rk5", prob["params"], d_time, s, c, st, model=model)
+    torch.cuda.synchronize()
+    assert f.run_check() == 0 and (st.cpu().numpy() == 0).all()
+    so, _, _ = oracle.integrate("rk5", prob["params"], prob["time"], uu, bb, prob["state"].copy())
+    g = s.cpu().numpy()[:, -1, 6]
+    assert abs(g.mean() / so[:, -1, 6].mean() - 1.0) < 2e-3
     model.close()
     f.close()
