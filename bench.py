@@ -72,6 +72,14 @@ WORKLOADS = {
 }
 
 
+# Safety factor of the learned controller's proposal.  Smaller factors trade
+# rejections for shorter steps: at 0.6 the mixed RK5 kernel accepts 79 % of its
+# attempts (classical 46 %) and makes 29 % more accepted steps per second, but
+# simulates 9 % less particle time per second; 0.75 keeps the simulated time
+# per second of the classical controller.  The benchmark uses 0.75 so that
+# accepted steps per second are not bought with shorter steps.
+LEARNED_SAFETY = 0.75
+
 # dram__bytes_read.sum + dram__bytes_write.sum of one timed full-size window,
 # from a single-pass ncu capture of the same command
 # (profiles/k_integrate_full_size_single_pass.md)
@@ -443,7 +451,7 @@ def mixed_leg(args, dev, stream):
             X, T = LRN.dataset(LRN.records_from_buffer(rec), "rk5")
             norm = LRN.normalisation(X, T)
             params_mlp, hist = LRN.train(torch, X, T, norm, epochs=2, batch=16384, lr=2e-3)
-            model = LRN.Model(params_mlp, norm, safety=0.9)
+            model = LRN.Model(params_mlp, norm, safety=LEARNED_SAFETY)
             out["learned_training"] = {"records": int(X.shape[0]), "mse_per_epoch": hist}
             del rec
         del st, cnt, status, carry
@@ -639,11 +647,11 @@ def learned_leg(args, dev, stream):
     t_tr = time.perf_counter()
     p, hist = learned.train(torch, X, T, norm, epochs=2, batch=16384, lr=2e-3)
     t_tr = time.perf_counter() - t_tr
-    model = learned.Model(p, norm, safety=0.9)
+    model = learned.Model(p, norm, safety=LEARNED_SAFETY)
     out = {"workload": "dop853-256, field seed 11 (trained on seed 10)",
            "records": int(X.shape[0]), "record_seconds": t_rec, "train_seconds": t_tr,
            "mse_per_epoch": hist, "target": "accepted log dt + at most log 2 of error headroom",
-           "safety": 0.9}
+           "safety": LEARNED_SAFETY}
     f, st, cnt, status, carry = setup(11)
     snap = (st.clone(), cnt.clone(), carry.clone())
     for name, mdl in (("classical", None), ("learned", model)):
@@ -751,7 +759,7 @@ def main():
         X, T = LRN.dataset(LRN.records_from_buffer(rec), cfg["method"])
         norm = LRN.normalisation(X, T)
         pm, hist = LRN.train(torch, X, T, norm, epochs=2, batch=16384, lr=2e-3)
-        model = LRN.Model(pm, norm, safety=0.9)
+        model = LRN.Model(pm, norm, safety=LEARNED_SAFETY)
         training = {"records": int(X.shape[0]), "mse_per_epoch": hist,
                     "recorded_in": "the first warm-up window (classical controller)"}
         del rec
