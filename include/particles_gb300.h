@@ -318,6 +318,10 @@ int pt_debug_pow(int64_t n, const double *d_x, const double *d_y, double *d_out,
  * roots for the exponents -1/5, -1/4, -1/8; the deterministic pow otherwise). */
 int pt_debug_ctl_pow(int64_t n, const double *d_x, const double *d_y, double *d_out,
                      void *stream);
+/* The integer-pipe floor, node index and double -> int32 conversion next to
+ * the FP64 instructions they replace (4 doubles and 2 ints per input). */
+int pt_debug_intpipe(int64_t n, const double *d_x, int32_t d, double *d_out, int32_t *d_idx,
+                     void *stream);
 int pt_debug_accel(const pt_fields *f, int64_t n, const double params[17],
                    const double *d_vec, double *d_acc, void *stream);
 

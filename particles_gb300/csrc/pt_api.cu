@@ -908,6 +908,14 @@ extern "C" int pt_debug_pow(int64_t n, const double *d_x, const double *d_y, dou
     return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_pow");
 }
 
+extern "C" int pt_debug_intpipe(int64_t n, const double *d_x, int32_t d, double *d_out,
+                                int32_t *d_idx, void *stream)
+{
+    if (n < 0 || (n > 0 && (!d_x || !d_out || !d_idx))) return set_err(PT_ERR_ARG, "bad argument%s");
+    const cudaError_t e = pt_launch_intpipe(n, d_x, d, d_out, d_idx, (cudaStream_t)stream);
+    return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_intpipe");
+}
+
 extern "C" int pt_debug_ctl_pow(int64_t n, const double *d_x, const double *d_y, double *d_out,
                                 void *stream)
 {

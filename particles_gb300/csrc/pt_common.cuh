@@ -112,12 +112,49 @@ __device__ __forceinline__ double pt_max(double a, double b) { return (b > a) ? 
 __device__ __forceinline__ double pt_min(double a, double b) { return (b < a) ? b : a; }
 __device__ __forceinline__ double pt_nanmax(double m, double q) { return (q > m || q != q) ? q : m; }
 
+/* floor(x) for doubles on the integer pipe.  GB300 runs 2 FP64 operations
+ * per cycle per SM and the FP64 rounding and conversion instructions share
+ * that pipe, while integer operations run at 64 per cycle; floor is exact, so
+ * clearing the fraction bits (after a carry into the integer bits for a
+ * negative non-integer) gives the same value as the FP64 instruction,
+ * including -0.0, +-inf and NaN. */
+__device__ __forceinline__ double pt_floor(double x)
+{
+    const long long b = __double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    if (e >= 52) return x;                                  /* integral, inf or NaN */
+    if (e < 0)                                              /* |x| < 1 */
+        return (b < 0) ? ((b & 0x7fffffffffffffffLL) ? -1.0 : x) : __longlong_as_double(0LL);
+    const long long frac = 0x000fffffffffffffLL >> e;
+    if ((b & frac) == 0) return x;
+    return __longlong_as_double(((b < 0) ? b + frac : b) & ~frac);
+}
+
+/* (int32_t)q for an integral double q on the integer pipe, saturating at
+ * the int32 range like the hardware conversion (NaN -> 0). */
+__device__ __forceinline__ int32_t pt_i32(double q)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(q);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    const bool neg = (b >> 63) != 0;
+    if (e == 1024 && (b & 0x000fffffffffffffULL)) return 0;            /* NaN */
+    if (e < 0) return 0;
+    if (e > 30) return neg ? (int32_t)0x80000000u : 0x7fffffff;
+    const int32_t v = (int32_t)(((b & 0x000fffffffffffffULL) | (1ULL << 52)) >> (52 - e));
+    return neg ? -v : v;
+}
+
 /* floor(xp) as a 0-based node index; dm (only reachable when x - floor(x)
  * rounds up to 1 for a tiny negative x, where the reference indexes past the
- * array) wraps to 0, NaN maps to 0.  Identical rule in the oracle. */
+ * array) wraps to 0, NaN maps to 0.  Identical rule in the oracle.  q is an
+ * integral double (a floor), read off its bits on the integer pipe. */
 __device__ __forceinline__ int32_t pt_node_index(double q, int32_t d)
 {
-    return (q >= 0.0 && q < (double)d) ? (int32_t)q : 0;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(q);
+    const int e = (int)((b >> 52) & 0x7ff) - 1023;
+    if ((b >> 63) || e < 0 || e > 30) return 0;            /* negative, < 1, huge, inf, NaN */
+    const int32_t v = (int32_t)(((b & 0x000fffffffffffffULL) | (1ULL << 52)) >> (52 - e));
+    return v < d ? v : 0;
 }
 
 __device__ __forceinline__ uint64_t pt_globaltimer()
@@ -179,6 +216,8 @@ cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int brick, int64_t n, 
 cudaError_t pt_launch_debug_pow(int64_t n, const double *x, const double *y, double *out,
                                 cudaStream_t s);
 cudaError_t pt_launch_ctl_pow(int64_t n, const double *x, const double *y, double *out,
+                              cudaStream_t s);
+cudaError_t pt_launch_intpipe(int64_t n, const double *x, int32_t d, double *out, int32_t *idx,
                               cudaStream_t s);
 
 #endif /* PT_COMMON_CUH */

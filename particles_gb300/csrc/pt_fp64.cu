@@ -88,10 +88,10 @@ struct EvalF64 {
         for (int i = 0; i < 3; ++i) {                            /* :140-149 */
             const double x = P.unit_map ? s[i] : (s[i] - P.xl[i]) / P.xs[i];
             const double xr = x + P.inv_dm[i];
-            double xp = P.dmr[i] * (xr - floor(xr));
-            r[i] = pt_node_index(floor(xp), P.dm[i]);
-            xp = P.dmr[i] * (x - floor(x));
-            const double pl = floor(xp);
+            double xp = P.dmr[i] * (xr - pt_floor(xr));
+            r[i] = pt_node_index(pt_floor(xp), P.dm[i]);
+            xp = P.dmr[i] * (x - pt_floor(x));
+            const double pl = pt_floor(xp);
             l[i] = pt_node_index(pl, P.dm[i]);
             xd[i] = xp - pl;
             xu[i] = 1.0 - xd[i];

@@ -189,9 +189,9 @@ struct EvalMixed {
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             const double xn = fma(si[i], P.gsx[i], P.gox[i]);
-            const double fl = floor(xn);
+            const double fl = pt_floor(xn);
             O.off[i] = pt_d2f(xn - fl);
-            O.cell[i] = (int32_t)fl;          /* beyond 2^31 cells it saturates */
+            O.cell[i] = pt_i32(fl);           /* beyond 2^31 cells it saturates */
         }
     }
 

@@ -220,9 +220,9 @@ __device__ __forceinline__ void pt_feature_cell(const PtRun &P, const double s[6
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         const double xn = fma(s[i], P.gsx[i], P.gox[i]);
-        const double fl = floor(xn);
+        const double fl = pt_floor(xn);
         xd[i] = pt_d2f(xn - fl);
-        const int32_t ci = (int32_t)fl;
+        const int32_t ci = pt_i32(fl);
         int32_t li;
         if (P.dm_mask[i]) {
             li = ci & P.dm_mask[i];

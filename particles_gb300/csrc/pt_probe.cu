@@ -14,6 +14,24 @@
 
 namespace {
 
+/* Integer-pipe floor / index / conversion against the FP64 instructions:
+ * out[4i..4i+3] = { pt_floor(x), floor(x), pt_i32(floor(x)),
+ * (int32_t)floor(x) } and idx[2i..2i+1] = { pt_node_index(floor(x), d), the
+ * FP64-comparison version }. */
+__global__ void k_intpipe(int64_t n, const double *x, int32_t d, double *out, int32_t *idx)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double v = x[i], f = floor(v);
+        out[4 * i] = pt_floor(v);
+        out[4 * i + 1] = f;
+        out[4 * i + 2] = (double)pt_i32(f);
+        out[4 * i + 3] = (f != f) ? 0.0 : (double)(int32_t)f;
+        idx[2 * i] = pt_node_index(f, d);
+        idx[2 * i + 1] = (f >= 0.0 && f < (double)d) ? (int32_t)f : 0;
+    }
+}
+
 /* The non-exact builds' controller power, for its accuracy test. */
 __global__ void k_ctl_pow(int64_t n, const double *x, const double *y, double *o)
 {
@@ -83,5 +101,14 @@ cudaError_t pt_launch_ctl_pow(int64_t n, const double *x, const double *y, doubl
     if (n <= 0) return cudaSuccess;
     const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
     k_ctl_pow<<<grid, 256, 0, s>>>(n, x, y, out);
+    return cudaGetLastError();
+}
+
+cudaError_t pt_launch_intpipe(int64_t n, const double *x, int32_t d, double *out, int32_t *idx,
+                              cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    k_intpipe<<<grid, 256, 0, s>>>(n, x, d, out, idx);
     return cudaGetLastError();
 }

@@ -204,3 +204,31 @@ def test_host_buffer_calls_move_only_the_rows_they_write(cuda, oracle_lib):
     so, co, _ = oracle.integrate("dop853", prob["params"], prob["time"], uu, bb,
                                  prob["state"].copy())
     assert np.array_equal(c, co) and np.array_equal(s, so)
+
+
+def test_integer_pipe_floor_and_indices(cuda):
+    """pt_floor / pt_i32 / pt_node_index (integer pipe) equal the FP64
+    instructions bit for bit, special values included."""
+    torch = cuda
+    from particles_gb300 import _native as N
+    rng = np.random.default_rng(9)
+    x = np.concatenate([
+        rng.uniform(-300, 300, 20000), rng.uniform(-1, 1, 5000) * 10.0 ** rng.uniform(-300, 0, 5000),
+        rng.integers(-1000, 1000, 3000).astype(np.float64),
+        [0.0, -0.0, 0.5, -0.5, 1.0, -1.0, 2.0 ** 52, -(2.0 ** 52) - 0.5, 2.0 ** 31, -(2.0 ** 31),
+         2.0 ** 31 - 0.5, 1e300, -1e300, np.inf, -np.inf, np.nan, 255.99999999999997, 256.0,
+         -1e-320, 5e-324, 4503599627370495.5, -4503599627370495.5]])
+    dx = torch.tensor(x, device="cuda")
+    out = torch.empty(4 * x.size, dtype=torch.float64, device="cuda")
+    idx = torch.empty(2 * x.size, dtype=torch.int32, device="cuda")
+    N.check(N.load().pt_debug_intpipe(x.size, C.c_void_p(dx.data_ptr()), 256,
+                                      C.c_void_p(out.data_ptr()), C.c_void_p(idx.data_ptr()), None),
+            "pt_debug_intpipe")
+    torch.cuda.synchronize()
+    o = out.cpu().numpy().reshape(-1, 4)
+    i = idx.cpu().numpy().reshape(-1, 2)
+    nan = np.isnan(o[:, 1])
+    assert np.array_equal(np.isnan(o[:, 0]), nan)                            # NaN stays NaN
+    assert np.array_equal(o[~nan, 0].view(np.int64), o[~nan, 1].view(np.int64))  # floor, -0.0 too
+    assert np.array_equal(o[:, 2], o[:, 3])                                   # int32 conversion
+    assert np.array_equal(i[:, 0], i[:, 1])                                   # node index
