@@ -280,7 +280,7 @@ def run_reference(args, cfg, rank, world):
     acc = float(cnt[:, 1].sum() - acc0)
     v = acc / el
     line = {
-        "impl": "reference", "metric": "accepted particle-steps/s", "value": v,
+        "impl": "reference", "metric": "accepted particle-steps/s (plain FP64 kernel)", "value": v,
         "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
