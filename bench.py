@@ -140,7 +140,8 @@ def build_inputs(cfg, npart, rank, backend="numpy"):
     out = fields.snapshot(cfg["n"], db_rms=cfg["db_rms"], v_rms=cfg["v_rms"], vunit=VUN,
                           spectrum=cfg["spectrum"], nmin=1.0, nmax=cfg["nmax"],
                           seed=cfg["seed"], with_j=cfg["eta"] != 0.0, backend=backend)
-    idx = np.arange(rank * npart, (rank + 1) * npart, dtype=np.uint64)
+    from particles_gb300.shard import particle_indices
+    idx = particle_indices(rank, npart)
     s0 = initial.isotropic_state(npart, cfg["seed"], speed=cfg["speed"],
                                  gamma_range=cfg["gamma"], index=idx)
     return prm, tg, out, s0
@@ -796,12 +797,8 @@ def main():
     accepted = float(dcnt_tot[1])
     elapsed = dev_s
     if world > 1:
-        t = torch.tensor([elapsed, accepted], dtype=torch.float64, device=dev)
-        mx = t[:1].clone()
-        torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
-        sm = t[1:].clone()
-        torch.distributed.all_reduce(sm, op=torch.distributed.ReduceOp.SUM)
-        elapsed, accepted = float(mx.item()), float(sm.item())
+        from particles_gb300.shard import combine
+        elapsed, accepted = combine(torch, elapsed, accepted, device=dev)
     value = accepted / elapsed
 
     # roofline of the dominant (only) kernel: algorithmic FP64 flops / event time
