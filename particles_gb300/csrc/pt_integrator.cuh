@@ -374,7 +374,13 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
             e = e + CK_D4 * K(3, c); e = e + CK_D5 * K(4, c); e = e + CK_D6 * K(5, c);
             dsf[c] = a;
             sf[c] = si[c] + a;
+#ifdef PT_EXACT
             const double sr = fabs(si[c]) + fabs(K(0, c)) + 2.2250738585072014e-308;
+#else
+            /* + DBL_MIN only changes a zero sum: test the bits instead (integer pipe) */
+            double sr = fabs(si[c]) + fabs(K(0, c));
+            if (__double_as_longlong(sr) == 0) sr = 2.2250738585072014e-308;
+#endif
             const double q = fabs(PT_DIV(e, sr));
             del = (c == 0) ? q : pt_nanmax(del, q);
         }

@@ -8,7 +8,7 @@
  * FMA/clk/SM on GB300 against 2 DP ops/clk/SM).
  *
  * f(s) in FP32 (same physics as accelerations.F90:59-96 with
- * interpolations.F90:104-226):
+ * interpolations.F90:104-226), from si and the FP64 increment d = s - si:
  *   - once per attempt, the cell of si and the offset of si in it are found
  *     in FP64 ((x - xl) / xs * dm, periodic floor), so they stay exact far
  *     from the origin;
@@ -181,6 +181,7 @@ struct EvalMixed {
     struct Origin {
         int32_t cell[3];
         float off[3];
+        float u[3];       /* the momentum of si in FP32 */
     };
 
     /* Once per attempt, in FP64: node coordinate (x - xl) / xs * dm of si. */
@@ -192,6 +193,7 @@ struct EvalMixed {
             const double fl = pt_floor(xn);
             O.off[i] = pt_d2f(xn - fl);
             O.cell[i] = pt_i32(fl);           /* beyond 2^31 cells it saturates */
+            O.u[i] = pt_d2f(si[3 + i]);
         }
     }
 
@@ -222,8 +224,9 @@ struct EvalMixed {
     }
 
     /* f(s) with s = si + d: the stage position relative to the origin cell is
-     * off + d * dm / xs in FP32 (d is at most a few cells); momenta, gather and
-     * force in FP32; every FP64 <-> FP32 conversion on the integer pipe. */
+     * off + d * dm / xs in FP32 (d is at most a few cells), the momentum
+     * u(si) + d in FP32; gather and force in FP32; every FP64 <-> FP32
+     * conversion on the integer pipe. */
     static __device__ __forceinline__ void f(const PtRun &P, const double s[6], const double d[6],
                                              const Origin &O, double a[6])
     {
@@ -253,7 +256,10 @@ struct EvalMixed {
                               pdu * xu[2], pdu * xd[2], pdd * xu[2], pdd * xd[2] };
         float acc[NV];
         G::gather(P, l, r, w8, acc);
-        const float ux = pt_d2f(s[3]), uy = pt_d2f(s[4]), uz = pt_d2f(s[5]);
+        /* the stage momentum in FP32: u(si) + the FP64 increment, both
+         * rounded to FP32 (the FP64 stage state s is not needed) */
+        const float ux = O.u[0] + pt_d2f(d[3]), uy = O.u[1] + pt_d2f(d[4]), uz = O.u[2] + pt_d2f(d[5]);
+        (void)s;
         const float g = sqrtf(fmaf(ux, ux, fmaf(uy, uy, fmaf(uz, uz, 1.0f))));
         const float ig = 1.0f / g;
         const float v0 = ux * ig, v1 = uy * ig, v2 = uz * ig;
