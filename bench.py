@@ -50,22 +50,22 @@ QOM, VUN = 200.0, 1.0 / 20.0
 T0 = 2.0 * math.pi / QOM
 
 WORKLOADS = {
-    # the benchmark spec's metric's FP64 configuration
+    # the headline FP64 workload (DOP853, 256^3, eta J, 2^20 particles)
     "dop853-256": dict(method="dop853", n=256, spectrum="kolmogorov", nmax=32, db_rms=1.0,
                        v_rms=0.2, eta=1e-3, npart=1 << 20, gamma=(1.001, 1e3), speed=None,
                        tol=1e-10, periods=100, seed=1, window=0.05),
-    # the mixed-precision configuration (configuration 3)
+    # the mixed-precision workload: RK5 rtol 1e-8, 512^3, 2^22 particles
     # windows of 0.1 gyro-periods: the slowest particles need ~100x the mean
     # attempts of a window, so shorter windows are set by their duration
     "rk5-512": dict(method="rk5", n=512, spectrum="kolmogorov", nmax=32, db_rms=1.0, v_rms=0.2,
                     eta=0.0, npart=1 << 22, gamma=(1.001, 1e2), speed=None, tol=1e-8,
                     periods=50, seed=2, window=0.1),
-    # uneven batch in one persistent launch (configuration 4): three snapshots
+    # uneven batch in one persistent launch: three snapshots
     "ensemble-3": dict(method="dop853", n=(128, 192, 256), spectrum="kolmogorov", nmax=32,
                        db_rms=(0.5, 1.0, 2.0), v_rms=0.2, eta=0.0, npart=1 << 21,
                        split=(1, 2, 4), gamma=(1.0001, 1e4), speed=None,
                        tol=(1e-6, 1e-8, 1e-10), periods=10, seed=(1, 2, 3), window=0.02),
-    # the CPU-runnable configuration (reference RK5, 64^3, 1024 particles)
+    # the CPU-runnable workload (reference RK5, 64^3, 1024 particles)
     "rk5-64": dict(method="rk5", n=64, spectrum="flat", nmax=4, db_rms=0.5, v_rms=0.1,
                    eta=0.0, npart=1024, gamma=None, speed=0.5, tol=1e-8, periods=10, seed=0,
                    window=1.0),
@@ -370,7 +370,7 @@ def tune(args, f, method, prm, d_time, d_state, stream, t_stop, **kw):
 
 
 def mixed_leg(args, dev, stream):
-    """Configuration 3 (RK5, rtol 1e-8, 512^3, 2^22 particles): accepted
+    """The mixed-precision workload (RK5, rtol 1e-8, 512^3, 2^22 particles): accepted
     particle-steps/s of the exact FP64, FMA FP64 and mixed FP32 kernels on the
     same windows, and the mixed kernel's per-particle energy / position error
     against the exact kernel (bit-identical to the CPU oracle) at a common
@@ -504,7 +504,7 @@ def mixed_leg(args, dev, stream):
 
 
 def ensemble_leg(args, dev, stream):
-    """Configuration 4: three snapshots (128^3, 192^3, 256^3; dB_rms 0.5, 1, 2;
+    """The ensemble workload: three snapshots (128^3, 192^3, 256^3; dB_rms 0.5, 1, 2;
     seeds 1-3) with 2^21 particles split 1:2:4, gamma log-uniform in
     [1.0001, 1e4], DOP853 at rtol 1e-6, 1e-8, 1e-10 and an open x boundary, in
     ONE persistent launch per window; finished and escaped particles are
@@ -593,8 +593,8 @@ def ensemble_leg(args, dev, stream):
 
 
 def learned_leg(args, dev, stream):
-    """Configuration 5: a controller trained on accepted-step records of the
-    plain integrator on the configuration-2 shape with field seed 10, then
+    """The learned-controller workload: a controller trained on accepted-step records of the
+    plain integrator on the headline shape (DOP853, 256^3, eta J) with field seed 10, then
     evaluated with field seed 11, 2^20 particles, DOP853 rtol 1e-10 (exact
     FP64): rejected fraction, attempts/s, accepted steps/s and simulated
     particle-time per second against the classical controller."""
