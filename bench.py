@@ -580,6 +580,32 @@ def ensemble_leg(args, dev, stream):
         res[mode] = {"accepted_steps_per_s": (accepted() - a0) / sec,
                      "ms_per_step": 1e3 * sec / args.steps,
                      "live": live.tolist(), "escaped": esc.tolist()}
+    # short windows (checkpoint-sized steps): here the host work per window --
+    # seven launches and the Python call -- competes with the GPU time, and the
+    # captured graph replays the same windows with one launch
+    sw, k_short = win / 50.0, 50
+    short = {}
+    for mode in ("launches", "graph"):
+        a0 = accepted()
+        if mode == "graph":
+            ens.capture(k_short, sw, stream=stream.cuda_stream)
+        stream.synchronize()
+        w0 = time.perf_counter()
+        if mode == "graph":
+            ens.replay(stream=stream.cuda_stream)
+            t += k_short * sw
+        else:
+            for _ in range(k_short):
+                t += sw
+                ens.run(t, stream=stream.cuda_stream)
+        stream.synchronize()
+        wall = time.perf_counter() - w0
+        short[mode] = {"windows": k_short, "window_gyroperiods": cfg["window"] / 50.0,
+                       "wall_ms_per_window": 1e3 * wall / k_short,
+                       "accepted_steps_per_s": (accepted() - a0) / wall}
+    short["graph_speedup"] = (short["launches"]["wall_ms_per_window"]
+                              / short["graph"]["wall_ms_per_window"])
+    res["short_windows"] = short
     rc = ens.check()
     live, esc = ens.counts()
     out.update(res)
