@@ -77,6 +77,8 @@ struct pt_fields {
     size_t ws_bytes;
     unsigned char *pack;        /* host-buffer runs: the output rows a call wrote, packed */
     size_t pack_bytes;
+    unsigned char *hst;         /* host-buffer runs: pinned host staging, reused across calls */
+    size_t hst_bytes;
 };
 
 /* Bytes the last host-buffer run moved between host and device. */
@@ -316,6 +318,7 @@ extern "C" int pt_fields_destroy(pt_fields *f)
     cudaFree(f->scratch);
     cudaFree(f->ws);
     cudaFree(f->pack);
+    cudaFreeHost(f->hst);
     delete f;
     return PT_OK;
 }
@@ -691,6 +694,17 @@ __global__ void k_rows_written(int64_t np, const int32_t *__restrict__ nf0,
     }
 }
 
+/* The first row of every particle from a packed copy into state(8,m,np). */
+__global__ void k_unpack_row0(int64_t np, int32_t m, const double2 *__restrict__ rows,
+                              double2 *__restrict__ state)
+{
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+         p += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) state[4 * (int64_t)m * p + i] = rows[4 * p + i];
+    }
+}
+
 /* Packs the written rows of every particle at its offset (64-B rows). */
 __global__ void k_pack_rows(int64_t np, int32_t m, const int32_t *__restrict__ nf0,
                             const int64_t *__restrict__ off, const int64_t *__restrict__ count,
@@ -736,9 +750,12 @@ extern "C" int pt_integrate_fields(int32_t method, int64_t np, int32_t m, const 
     const size_t o_count = up256(o_nf0 + (size_t)np * 8), o_off = up256(o_count + (size_t)np * 8);
     const size_t need = up256(o_off + (size_t)np * 8);
     cudaStream_t s = nullptr;
-    std::vector<int64_t> hcount, hoff;
     int64_t rows = 0;
     const int grid = (int)((np + 255) / 256 < 4096 ? (np + 255) / 256 : 4096);
+    /* pinned host staging: [row 0 of every particle | counts | offsets |
+     * start rows and flags | the packed rows written]; grown when needed */
+    const size_t h_row0 = 0, h_count = up256((size_t)np * 64), h_off = up256(h_count + (size_t)np * 8);
+    const size_t h_nf0 = up256(h_off + (size_t)(np + 1) * 8), h_rows = up256(h_nf0 + (size_t)np * 8);
     PT_CU(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     if (f->ws_bytes < need) {
         cudaFree(f->ws);
@@ -746,6 +763,13 @@ extern "C" int pt_integrate_fields(int32_t method, int64_t np, int32_t m, const 
         f->ws_bytes = 0;
         PT_CU(cudaMalloc(&f->ws, need));
         f->ws_bytes = need;
+    }
+    if (f->hst_bytes < h_rows) {
+        cudaFreeHost(f->hst);
+        f->hst = nullptr;
+        f->hst_bytes = 0;
+        PT_CU(cudaMallocHost(&f->hst, h_rows));
+        f->hst_bytes = h_rows;
     }
     {
         unsigned char *w = f->ws;
@@ -758,9 +782,24 @@ extern "C" int pt_integrate_fields(int32_t method, int64_t np, int32_t m, const 
         int64_t *d_count = reinterpret_cast<int64_t *>(w + o_count);
         int64_t *d_off = reinterpret_cast<int64_t *>(w + o_off);
         int32_t *d_n = reinterpret_cast<int32_t *>(d_carry + (size_t)np * 15 * 8);  /* carry n[], flags[] */
+        double *hrow0 = reinterpret_cast<double *>(f->hst + h_row0);
+        int64_t *hcount = reinterpret_cast<int64_t *>(f->hst + h_count);
+        int64_t *hoff = reinterpret_cast<int64_t *>(f->hst + h_off);
+        int32_t *hnf0 = reinterpret_cast<int32_t *>(f->hst + h_nf0);
+        for (int64_t p = 0; p < np; ++p) memcpy(hrow0 + 8 * p, state + 8 * (int64_t)m * p, 64);
         PT_CU(cudaMemcpyAsync(d_time, time, (size_t)m * 8, cudaMemcpyHostToDevice, s));
-        PT_CU(cudaMemcpy2DAsync(d_state, (size_t)m * 64, state, (size_t)m * 64, 64, (size_t)np,
-                                cudaMemcpyHostToDevice, s));
+        /* the packed first rows pass through the (not yet used) pack area */
+        if (f->pack_bytes < (size_t)np * 64) {
+            cudaFree(f->pack);
+            f->pack = nullptr;
+            f->pack_bytes = 0;
+            PT_CU(cudaMalloc(&f->pack, (size_t)np * 64));
+            f->pack_bytes = (size_t)np * 64;
+        }
+        PT_CU(cudaMemcpyAsync(f->pack, hrow0, (size_t)np * 64, cudaMemcpyHostToDevice, s));
+        k_unpack_row0<<<grid, 256, 0, s>>>(np, m, reinterpret_cast<const double2 *>(f->pack),
+                                           reinterpret_cast<double2 *>(d_state));
+        PT_CU(cudaGetLastError());
         g_xfer[0] += (int64_t)m * 8 + np * 64;
         if (h_carry) {
             PT_CU(cudaMemcpyAsync(d_carry, h_carry, crb, cudaMemcpyHostToDevice, s));
@@ -774,31 +813,41 @@ extern "C" int pt_integrate_fields(int32_t method, int64_t np, int32_t m, const 
         if (rc != PT_OK) goto done;
         k_rows_written<<<grid, 256, 0, s>>>(np, d_nf0, d_n, d_count);
         PT_CU(cudaGetLastError());
-        hcount.resize(np);
-        hoff.resize(np + 1);
-        PT_CU(cudaMemcpyAsync(hcount.data(), d_count, (size_t)np * 8, cudaMemcpyDeviceToHost, s));
+        PT_CU(cudaMemcpyAsync(hcount, d_count, (size_t)np * 8, cudaMemcpyDeviceToHost, s));
+        PT_CU(cudaMemcpyAsync(hnf0, d_nf0, (size_t)np * 8, cudaMemcpyDeviceToHost, s));
         PT_CU(cudaStreamSynchronize(s));
         hoff[0] = 0;
         for (int64_t p = 0; p < np; ++p) hoff[p + 1] = hoff[p] + hcount[p];
         rows = hoff[np];
-        PT_CU(cudaMemcpyAsync(d_off, hoff.data(), (size_t)np * 8, cudaMemcpyHostToDevice, s));
+        PT_CU(cudaMemcpyAsync(d_off, hoff, (size_t)np * 8, cudaMemcpyHostToDevice, s));
         if (f->pack_bytes < (size_t)rows * 64) {
+            PT_CU(cudaStreamSynchronize(s));
             cudaFree(f->pack);
             f->pack = nullptr;
             f->pack_bytes = 0;
             PT_CU(cudaMalloc(&f->pack, (size_t)rows * 64));
             f->pack_bytes = (size_t)rows * 64;
         }
+        if (f->hst_bytes < h_rows + (size_t)rows * 64) {          /* grow, keeping the indices */
+            PT_CU(cudaStreamSynchronize(s));
+            unsigned char *nh = nullptr;
+            PT_CU(cudaMallocHost(&nh, h_rows + (size_t)rows * 64));
+            memcpy(nh, f->hst, h_rows);
+            cudaFreeHost(f->hst);
+            f->hst = nh;
+            f->hst_bytes = h_rows + (size_t)rows * 64;
+            hcount = reinterpret_cast<int64_t *>(f->hst + h_count);
+            hoff = reinterpret_cast<int64_t *>(f->hst + h_off);
+            hnf0 = reinterpret_cast<int32_t *>(f->hst + h_nf0);
+        }
+        double *staged = reinterpret_cast<double *>(f->hst + h_rows);
         if (rows > 0) {
             k_pack_rows<<<grid, 256, 0, s>>>(np, m, d_nf0, d_off, d_count,
                                              reinterpret_cast<const double2 *>(d_state),
                                              reinterpret_cast<double2 *>(f->pack));
             PT_CU(cudaGetLastError());
+            PT_CU(cudaMemcpyAsync(staged, f->pack, (size_t)rows * 64, cudaMemcpyDeviceToHost, s));
         }
-        /* the packed rows go to a staging copy, then to their places */
-        std::vector<double> staged((size_t)rows * 8);
-        if (rows > 0)
-            PT_CU(cudaMemcpyAsync(staged.data(), f->pack, (size_t)rows * 64, cudaMemcpyDeviceToHost, s));
         PT_CU(cudaMemcpyAsync(cnt, d_cnt, (size_t)np * 24, cudaMemcpyDeviceToHost, s));
         g_xfer[1] += rows * 64 + np * 24;
         if (h_status) {
@@ -809,16 +858,11 @@ extern "C" int pt_integrate_fields(int32_t method, int64_t np, int32_t m, const 
             PT_CU(cudaMemcpyAsync(h_carry, d_carry, crb, cudaMemcpyDeviceToHost, s));
             g_xfer[1] += (int64_t)crb;
         }
-        std::vector<int32_t> start(np);
-        PT_CU(cudaMemcpyAsync(start.data(), d_nf0, (size_t)np * 4, cudaMemcpyDeviceToHost, s));
-        std::vector<int32_t> flag0(np);
-        PT_CU(cudaMemcpyAsync(flag0.data(), d_nf0 + np, (size_t)np * 4, cudaMemcpyDeviceToHost, s));
         PT_CU(cudaStreamSynchronize(s));
         for (int64_t p = 0; p < np; ++p) {
             if (!hcount[p]) continue;
-            const int64_t r0 = (flag0[p] & 1) ? start[p] : 0;
-            memcpy(state + 8 * (r0 + (int64_t)m * p), staged.data() + 8 * hoff[p],
-                   (size_t)hcount[p] * 64);
+            const int64_t r0 = (hnf0[np + p] & 1) ? hnf0[p] : 0;
+            memcpy(state + 8 * (r0 + (int64_t)m * p), staged + 8 * hoff[p], (size_t)hcount[p] * 64);
         }
     }
     rc = pt_run_check(f);
