@@ -32,6 +32,9 @@ COMMON = [
 # (output object, source, extra flags)
 UNITS = [
     ("pt_api.o", "pt_api.cu", ["--fmad=false"]),
+    ("pt_fields.o", "pt_fields.cu", ["--fmad=false"]),
+    ("pt_hostio.o", "pt_hostio.cu", ["--fmad=false"]),
+    ("pt_ensemble.o", "pt_ensemble.cu", ["--fmad=false"]),
     ("pt_fp64_exact1.o", "pt_fp64.cu", ["--fmad=false", "-DPT_SFX=exact", "-DPT_EXACT", "-DPT_PART=1"]),
     ("pt_fp64_exact2.o", "pt_fp64.cu", ["--fmad=false", "-DPT_SFX=exact", "-DPT_EXACT", "-DPT_PART=2"]),
     ("pt_fp64_fma1.o", "pt_fp64.cu", ["--fmad=true", "-DPT_SFX=fma", "-DPT_PART=1"]),
