@@ -128,3 +128,21 @@ def test_mixed_windowed_resume_matches_single_run(cuda):
     for w in (0.3, 0.8, 0.0):
         f.integrate("rk5", prob["params"], prob["time"], s, c, carry=carry, t_stop=w * T0)
     assert np.array_equal(full[0], s) and np.array_equal(full[1], c)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_near_gather_mixed_statistics(cuda, oracle_lib, precision):
+    """interpolate_near in the mixed-precision evaluations: ensemble energy and
+    step statistics of the FP64 oracle's nearest-node run."""
+    prob = small_problem("rk5", n=24, npart=128, periods=2.0, seed=19)
+    import oracle
+    from particles_gb300 import integrate
+    uu, bb = prob["fields"]
+    so, co, _ = oracle.integrate("rk5", prob["params"], prob["time"], uu, bb, prob["state"].copy(),
+                                 near=True)
+    sg, cg, stg = integrate("rk5", prob["params"], prob["time"], uu, bb, prob["state"].copy(),
+                            precision=precision, interpolation="near")
+    assert (stg == 0).all()
+    g_o, g_g = so[:, -1, 6], sg[:, -1, 6]
+    assert abs(g_g.mean() / g_o.mean() - 1.0) < 2e-3
+    assert 0.7 < cg[:, 1].sum() / co[:, 1].sum() < 1.4
