@@ -834,6 +834,9 @@ def main():
     pk = C.c_double()
     L.pt_probe_peak(0, 16384, C.byref(pk))
     peak = pk.value
+    pk2 = C.c_double()
+    L.pt_probe_peak(2, 16384, C.byref(pk2))
+    peak_split = pk2.value
     traffic = DRAM_BYTES_PER_WINDOW.get((args.workload, args.precision))
     roof = {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,
             "unit": "TFLOP/s", "frac": achieved / peak,
@@ -841,6 +844,11 @@ def main():
             "traffic_source": "profiles/k_integrate_full_size_single_pass.md" if traffic else None,
             "peak_source": "FP64 FMA peak measured live on this GPU (pt_probe_peak); "
                            "the measured-peaks file lists only HBM and bf16",
+            "peak_no_fma": peak_split / 1e12,
+            "frac_of_no_fma_peak": achieved / peak_split,
+            "no_fma_note": "the exact kernel may not contract (bit identity with the CPU "
+                           "restatement), so separate FP64 multiply/add chains measured live "
+                           "bound it",
             "flops_per_step": flops / args.steps,
             "gather_bytes_per_step": roofline.gather_bytes(cfg["method"], np.array([dcnt_tot]),
                                                            record_bytes=rec_bytes) / args.steps}

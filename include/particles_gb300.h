@@ -308,8 +308,9 @@ int pt_debug_echo(int32_t method, int64_t np, int32_t m, const int32_t dm[3],
                   int32_t precision, int32_t has_j, const double params[17],
                   const pt_options *opt, double *d_out, double *host_out);
 
-/* Throughput probe for roofline denominators: kind 0 FP64 FMA, 1 FP32 FMA;
- * writes flop/s (FMA = 2 flops) measured on the current device. */
+/* Throughput probe for roofline denominators: kind 0 FP64 FMA, 1 FP32 FMA,
+ * 2 FP64 multiply + add as separate instructions (no contraction); writes
+ * flop/s (FMA = 2 flops, multiply or add = 1) measured on the current device. */
 int pt_probe_peak(int32_t kind, int32_t iters, double *flops_per_s);
 
 /* Device-side evaluation helpers for the parity tests (device pointers). */

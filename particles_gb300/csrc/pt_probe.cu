@@ -4,8 +4,10 @@
  * The FP64 kernels are bounded by the FP64 pipe, whose rate the measured-peak
  * file of this machine does not list, so the benchmark measures it live on
  * the same GPU: a grid of 8 independent FMA chains per thread, long enough
- * (~50 ms) to reach steady clocks.  kind 0 = FP64 FMA, kind 1 = FP32 FMA.
- * Result in flop/s with an FMA counted as 2 flops.
+ * (~50 ms) to reach steady clocks.  kind 0 = FP64 FMA, kind 1 = FP32 FMA,
+ * kind 2 = FP64 multiply and add as separate instructions (the ceiling of a
+ * kernel that may not contract, such as the exact FP64 integrator).  Result
+ * in flop/s with an FMA counted as 2 flops, a multiply or an add as 1.
  */
 #include <cuda_runtime.h>
 
@@ -40,7 +42,7 @@ __global__ void k_ctl_pow(int64_t n, const double *x, const double *y, double *o
         o[i] = pt_ctl_pow(x[i], y[i]);
 }
 
-template <class T>
+template <class T, bool SPLIT>
 __global__ void k_fma_chains(T *out, int iters, T a, T b)
 {
     T x[8];
@@ -48,7 +50,10 @@ __global__ void k_fma_chains(T *out, int iters, T a, T b)
     for (int j = 0; j < 8; ++j) x[j] = (T)(threadIdx.x + j) * (T)1e-3;
     for (int i = 0; i < iters; ++i) {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) x[j] = fma(x[j], a, b);
+        for (int j = 0; j < 8; ++j) {
+            if (SPLIT) x[j] = __dadd_rn(__dmul_rn((double)x[j], (double)a), (double)b);
+            else x[j] = fma(x[j], a, b);
+        }
     }
     T s = 0;
 #pragma unroll
@@ -56,7 +61,7 @@ __global__ void k_fma_chains(T *out, int iters, T a, T b)
     if (s == (T)12345.678) out[0] = s;   /* keeps the chains alive; practically never true */
 }
 
-template <class T>
+template <class T, bool SPLIT = false>
 double measure(int iters)
 {
     int dev = 0, sms = 1;
@@ -69,9 +74,9 @@ double measure(int iters)
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     const T a = (T)0.999999, b = (T)1e-7;
-    k_fma_chains<T><<<grid, block>>>(out, iters / 8, a, b);   /* warm-up */
+    k_fma_chains<T, SPLIT><<<grid, block>>>(out, iters / 8, a, b);   /* warm-up */
     cudaEventRecord(e0);
-    k_fma_chains<T><<<grid, block>>>(out, iters, a, b);
+    k_fma_chains<T, SPLIT><<<grid, block>>>(out, iters, a, b);
     cudaEventRecord(e1);
     cudaEventSynchronize(e1);
     float ms = 0.f;
@@ -90,7 +95,9 @@ double measure(int iters)
 extern "C" int pt_probe_peak(int32_t kind, int32_t iters, double *flops_per_s)
 {
     if (!flops_per_s || iters <= 0) return PT_ERR_ARG;
-    double r = (kind == 0) ? measure<double>(iters) : measure<float>(iters);
+    if (kind < 0 || kind > 2) return PT_ERR_ARG;
+    const double r = (kind == 0) ? measure<double>(iters)
+                   : (kind == 1) ? measure<float>(iters) : measure<double, true>(iters);
     *flops_per_s = r;
     return r > 0 ? PT_OK : PT_ERR_CUDA;
 }
