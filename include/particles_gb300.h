@@ -57,6 +57,7 @@ extern "C" {
 #define PT_ERR_TIMEOUT     -4  /* the time budget expired; carry and status are consistent */
 #define PT_ERR_UNSUPPORTED -5  /* option combination not built */
 #define PT_ERR_PARTICLE    -6  /* at least one particle ended with a negative status */
+#define PT_ERR_BOUNDS      -7  /* bounds-checked build: a gather indexed outside the field */
 
 /* Per-particle status (pt_options.status / device status arrays). */
 #define PT_ST_DONE          0  /* t reached tmax */

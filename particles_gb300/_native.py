@@ -7,6 +7,7 @@ There is no CPU fallback anywhere in the package.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 from . import build as _build
@@ -14,7 +15,7 @@ from . import build as _build
 PT_METHOD_RK5, PT_METHOD_DOP853 = 1, 2
 PT_PREC_FP64, PT_PREC_FP64_FMA, PT_PREC_FP32, PT_PREC_BF16 = 0, 1, 2, 3
 PT_OK, PT_ERR_ARG, PT_ERR_CUDA, PT_ERR_NOMEM = 0, -1, -2, -3
-PT_ERR_TIMEOUT, PT_ERR_UNSUPPORTED, PT_ERR_PARTICLE = -4, -5, -6
+PT_ERR_TIMEOUT, PT_ERR_UNSUPPORTED, PT_ERR_PARTICLE, PT_ERR_BOUNDS = -4, -5, -6, -7
 PT_ST_DONE, PT_ST_RUNNING, PT_ST_ESCAPED, PT_ST_NOT_RUN = 0, 1, 2, -1
 PT_ST_STEP_LIMIT, PT_ST_DT_UNDERFLOW, PT_ST_NONFINITE, PT_ST_TIMEOUT = -2, -3, -4, -5
 
@@ -64,8 +65,13 @@ class PtError(RuntimeError):
 _lib = None
 
 
+def checked() -> bool:
+    """PT_CHECKED=1 in the environment selects the bounds-checked library."""
+    return os.environ.get("PT_CHECKED", "0") not in ("", "0")
+
+
 def lib_path() -> Path:
-    return _build.LIB
+    return _build.LIB_CHECKED if checked() else _build.LIB
 
 
 def load():
@@ -73,7 +79,7 @@ def load():
     global _lib
     if _lib is not None:
         return _lib
-    path = _build.build()
+    path = _build.build(checked=checked())
     L = C.CDLL(str(path))
     vp, i32, i64, d = C.c_void_p, C.c_int32, C.c_int64, C.c_double
     L.pt_integrate.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp]

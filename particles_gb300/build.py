@@ -21,6 +21,10 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libparticles_gb300.so"
+# the bounds-checked variant (-DPT_CHECKED): every gather index is tested
+# against the field store and counted when out of range (PT_ERR_BOUNDS)
+OUT_CHECKED = OUT / "checked"
+LIB_CHECKED = OUT_CHECKED / "libparticles_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = [
@@ -62,17 +66,21 @@ def _sources_newer_than(target: Path) -> bool:
     return any(d.stat().st_mtime > t for d in deps if d.is_file())
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile and link the library if any source is newer; return its path."""
-    if not force and not _sources_newer_than(LIB):
-        return LIB
-    OUT.mkdir(parents=True, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> Path:
+    """Compile and link the library (or its bounds-checked variant) if any
+    source is newer; return its path."""
+    lib, out = (LIB_CHECKED, OUT_CHECKED) if checked else (LIB, OUT)
+    if not force and not _sources_newer_than(lib):
+        return lib
+    out.mkdir(parents=True, exist_ok=True)
     exe = nvcc()
     ptx_v = ["-Xptxas", "-v"] if verbose else []
+    defs = ["-DPT_CHECKED"] if checked else []
 
     def compile_unit(u):
         obj, src, extra = u
-        cmd = [exe, *ARCH, *COMMON, *extra, *ptx_v, "-c", str(CSRC / src), "-o", str(OUT / obj)]
+        cmd = [exe, *ARCH, *COMMON, *extra, *defs, *ptx_v, "-c", str(CSRC / src), "-o",
+               str(out / obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         return obj, cmd, r
 
@@ -83,17 +91,18 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         log.append(f"$ {' '.join(cmd)}\n{r.stdout}{r.stderr}")
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {obj}:\n{r.stdout}\n{r.stderr}")
-    tmp = LIB.with_suffix(".so.tmp")
-    link = [exe, *ARCH, "-shared", "-o", str(tmp), *[str(OUT / u[0]) for u in UNITS]]
+    tmp = lib.with_suffix(".so.tmp")
+    link = [exe, *ARCH, "-shared", "-o", str(tmp), *[str(out / u[0]) for u in UNITS]]
     r = subprocess.run(link, capture_output=True, text=True)
     log.append(f"$ {' '.join(link)}\n{r.stdout}{r.stderr}")
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    (OUT / "build.log").write_text("\n".join(log))
-    return LIB
+    os.replace(tmp, lib)
+    (out / "build.log").write_text("\n".join(log))
+    return lib
 
 
 if __name__ == "__main__":
-    p = build(force="--force" in sys.argv, verbose="-v" in sys.argv)
+    p = build(force="--force" in sys.argv, verbose="-v" in sys.argv,
+              checked="--checked" in sys.argv)
     print(p)

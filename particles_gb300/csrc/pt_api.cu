@@ -203,6 +203,8 @@ void attach_fields(const pt_fields *f, PtRun &R)
     R.fld16 = f->rec16;
     R.bscale = f->bscale;
     for (int i = 0; i < 3; ++i) R.nb[i] = f->nb[i];
+    R.nrec = f->precision == PT_PREC_BF16 ? (int64_t)f->nb[0] * f->nb[1] * f->nb[2] * 729 : f->nodes;
+    R.oob = f->scratch + 2;
 }
 
 int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
@@ -232,7 +234,7 @@ int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
         e = cudaMemsetAsync(d_status, 0xff, (size_t)np * sizeof(int32_t), s);
         if (e != cudaSuccess) return cuda_err(e, "status reset");
     }
-    e = cudaMemsetAsync(f->scratch, 0, 2 * sizeof(unsigned long long), s);
+    e = cudaMemsetAsync(f->scratch, 0, 3 * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return cuda_err(e, "scratch reset");
     e = launch_run(method, f, R, s);
     if (e != cudaSuccess) return cuda_err(e, "kernel launch");
@@ -294,7 +296,7 @@ extern "C" int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_field
             R.minb = 2 + v;
             e = cudaMemcpy2DAsync(t_state, (size_t)mt * 64, d_state, (size_t)m * 64, 64, (size_t)ns,
                                   cudaMemcpyDeviceToDevice, s);
-            if (e == cudaSuccess) e = cudaMemsetAsync(f->scratch, 0, 2 * sizeof(unsigned long long), s);
+            if (e == cudaSuccess) e = cudaMemsetAsync(f->scratch, 0, 3 * sizeof(unsigned long long), s);
             if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
             if (e == cudaSuccess) e = launch_run(method, f, R, s);
             if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
@@ -390,9 +392,15 @@ extern "C" int pt_run_device(int32_t method, int64_t np, int32_t m, const pt_fie
 extern "C" int pt_run_check(const pt_fields *f)
 {
     if (!f) return set_err(PT_ERR_ARG, "fields handle is NULL%s");
-    int32_t flags[2] = { 0, 0 };
-    cudaError_t e = cudaMemcpy(flags, f->scratch + 1, sizeof flags, cudaMemcpyDeviceToHost);
+    unsigned long long w[2] = { 0, 0 };             /* flags (2 x int32), out-of-range count */
+    cudaError_t e = cudaMemcpy(w, f->scratch + 1, sizeof w, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_err(e, "pt_run_check");
+    int32_t flags[2];
+    memcpy(flags, &w[0], sizeof flags);
+    if (w[1]) {
+        snprintf(g_err, sizeof g_err, "%llu gather index(es) outside the field records", w[1]);
+        return PT_ERR_BOUNDS;
+    }
     if (flags[0]) return set_err(PT_ERR_TIMEOUT, "time budget expired%s");
     if (flags[1]) {
         snprintf(g_err, sizeof g_err, "%d particle(s) ended with a negative status", flags[1]);

@@ -62,6 +62,8 @@ struct PtRun {
     unsigned long long *queue;  /* work-queue head */
     int32_t *flags;        /* [0] time budget hit, [1] particles with negative status */
     int32_t minb;          /* launch variant: resident blocks per SM (2, 3 or 4) */
+    unsigned long long *oob;  /* checked builds: count of out-of-range record indices */
+    int64_t nrec;          /* records of the field store (index bound of the gathers) */
     int32_t *work;         /* per particle: attempts made in this run, or NULL */
     const int64_t *qlen;   /* ensembles: device queue length (else np) */
     const double *tstop;   /* ensembles: device window end (else tend) */
@@ -163,6 +165,25 @@ __device__ __forceinline__ uint64_t pt_globaltimer()
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
+
+/* Checked builds (PT_CHECKED, the bounds-checking variant of the library):
+ * every record index of a gather is tested against the store; an index out
+ * of range is counted in P.oob and replaced by record 0, so the access stays
+ * inside the allocation and the host reports the count (PT_ERR_BOUNDS).
+ * Other builds compile the test away. */
+#ifdef PT_CHECKED
+__device__ __forceinline__ int64_t pt_chk(unsigned long long *oob, int64_t i, int64_t n)
+{
+    if (i < 0 || i >= n) {
+        atomicAdd(oob, 1ULL);
+        return 0;
+    }
+    return i;
+}
+#define PT_CHK(P, i, n) pt_chk((P).oob, (i), (n))
+#else
+#define PT_CHK(P, i, n) (i)
+#endif
 
 /* Internal "keep integrating" word of the step loops; distinct from every
  * PT_ST_* status (PT_ST_RUNNING is 1). */

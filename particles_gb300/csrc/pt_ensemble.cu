@@ -287,7 +287,7 @@ extern "C" int pt_ensemble_create(int32_t method, int32_t nmembers, const pt_mem
     cudaGetDevice(&e->device);
     cudaError_t err = cudaMalloc(&e->d_tab, sizeof(PtRun) * nmembers);
     if (err == cudaSuccess) err = cudaMalloc(&e->d_tstop, sizeof(double));
-    if (err == cudaSuccess) err = cudaMalloc(&e->d_flags, 2 * sizeof(int32_t));
+    if (err == cudaSuccess) err = cudaMalloc(&e->d_flags, 16);   /* flags, out-of-range count */
     if (err == cudaSuccess) err = cudaMalloc(&e->B.ctl, sizeof(unsigned long long) * PT_ENS_CTL * nmembers);
     if (err == cudaSuccess) err = cudaMalloc(&e->B.idx, sizeof(int32_t) * (idx_elems > 0 ? idx_elems : 1));
     if (err != cudaSuccess) {
@@ -318,12 +318,13 @@ extern "C" int pt_ensemble_create(int32_t method, int32_t nmembers, const pt_mem
         R.work = e->B.idx + off + 3 * M.np;
         R.tstop = e->d_tstop;
         R.flags = e->d_flags;
+        R.oob = reinterpret_cast<unsigned long long *>(e->d_flags + 2);
         R.minb = e->minb;
         off += 4 * M.np;
     }
     err = cudaMemcpy(e->d_tab, tab, sizeof(PtRun) * nmembers, cudaMemcpyHostToDevice);
     if (err == cudaSuccess) err = cudaMemset(e->d_tstop, 0, sizeof(double));
-    if (err == cudaSuccess) err = cudaMemset(e->d_flags, 0, 2 * sizeof(int32_t));
+    if (err == cudaSuccess) err = cudaMemset(e->d_flags, 0, 16);
     if (err == cudaSuccess) {
         k_ens_init<<<dim3(ens_grid(npmax), nmembers), 256>>>(e->B);
         err = cudaDeviceSynchronize();
@@ -423,9 +424,15 @@ extern "C" int pt_ensemble_escaped(const pt_ensemble *e, int32_t member, int32_t
 extern "C" int pt_ensemble_check(const pt_ensemble *e)
 {
     if (!e) return set_err(PT_ERR_ARG, "ensemble is NULL%s");
-    int32_t flags[2] = { 0, 0 };
-    const cudaError_t err = cudaMemcpy(flags, e->d_flags, sizeof flags, cudaMemcpyDeviceToHost);
+    unsigned long long w[2] = { 0, 0 };             /* flags (2 x int32), out-of-range count */
+    const cudaError_t err = cudaMemcpy(w, e->d_flags, sizeof w, cudaMemcpyDeviceToHost);
     if (err != cudaSuccess) return cuda_err(err, "pt_ensemble_check");
+    int32_t flags[2];
+    memcpy(flags, &w[0], sizeof flags);
+    if (w[1]) {
+        snprintf(g_err, sizeof g_err, "%llu gather index(es) outside the field records", w[1]);
+        return PT_ERR_BOUNDS;
+    }
     if (flags[0]) return set_err(PT_ERR_TIMEOUT, "time budget expired%s");
     if (flags[1]) {
         snprintf(g_err, sizeof g_err, "%d particle(s) ended with a negative status", flags[1]);

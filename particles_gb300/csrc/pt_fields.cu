@@ -163,6 +163,7 @@ static int fields_create_impl(const int32_t dm[3], const double *uu, const doubl
     f->nodes = nn;
     PT_CU(cudaGetDevice(&f->device));
     PT_CU(cudaMalloc(&f->scratch, 256));
+    PT_CU(cudaMemset(f->scratch, 0, 256));
     if (precision == PT_PREC_BF16) {
         const int64_t nbk = (int64_t)f->nb[0] * f->nb[1] * f->nb[2];
         const int ns = f->has_j ? 20 : 12;

@@ -108,14 +108,14 @@ struct EvalF64 {
         double acc[NV];
         if (P.near) {                          /* interpolate_near (:76-80): the node l */
             double v[NC];
-            load_rec<NC>(P.fld, node[0], v);
+            load_rec<NC>(P.fld, PT_CHK(P, node[0], P.nrec), v);
 #pragma unroll
             for (int cc = 0; cc < NV; ++cc) acc[cc] = v[cc];
         } else {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {                         /* :212-220 in order */
                 double v[NC];
-                load_rec<NC>(P.fld, node[q], v);
+                load_rec<NC>(P.fld, PT_CHK(P, node[q], P.nrec), v);
 #pragma unroll
                 for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * v[cc] : acc[cc] + w8[q] * v[cc];
             }

@@ -76,7 +76,7 @@ struct GatherF32 {
                                   r[0] + yl + zl, r[0] + yl + zr, r[0] + yr + zl, r[0] + yr + zr };
         if (P.near) {                          /* interpolate_near: the node l */
             float v[NC];
-            load(P.fld32, node[0], v);
+            load(P.fld32, PT_CHK(P, node[0], P.nrec), v);
 #pragma unroll
             for (int cc = 0; cc < NV; ++cc) acc[cc] = v[cc];
             return;
@@ -84,7 +84,7 @@ struct GatherF32 {
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             float v[NC];
-            load(P.fld32, node[q], v);
+            load(P.fld32, PT_CHK(P, node[q], P.nrec), v);
 #pragma unroll
             for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * v[cc] : fmaf(w8[q], v[cc], acc[cc]);
         }
@@ -134,7 +134,8 @@ struct GatherBrick {
                                                     const int32_t *)
     {
         Loader L;
-        const int64_t b = (l[0] >> 3) + (int64_t)P.nb[0] * ((l[1] >> 3) + (int64_t)P.nb[1] * (l[2] >> 3));
+        const int64_t b = PT_CHK(P, (l[0] >> 3) + (int64_t)P.nb[0] * ((l[1] >> 3) + (int64_t)P.nb[1] * (l[2] >> 3)),
+                                 P.nrec / 729);
         L.fld = P.fld16;
         L.base = b * 729 + (l[0] & 7) + 9 * (l[1] & 7) + 81 * (l[2] & 7);
         const float4 *sp = reinterpret_cast<const float4 *>(P.bscale + b * NS);
@@ -148,16 +149,18 @@ struct GatherBrick {
     static __device__ __forceinline__ void gather(const PtRun &P, const int32_t l[3],
                                                   const int32_t *, const float w8[8], float acc[NV])
     {
-        const int64_t b = (l[0] >> 3) + (int64_t)P.nb[0] * ((l[1] >> 3) + (int64_t)P.nb[1] * (l[2] >> 3));
+        const int64_t b = PT_CHK(P, (l[0] >> 3) + (int64_t)P.nb[0] * ((l[1] >> 3) + (int64_t)P.nb[1] * (l[2] >> 3)),
+                                 P.nrec / 729);
         const int64_t base = b * 729 + (l[0] & 7) + 9 * (l[1] & 7) + 81 * (l[2] & 7);
         float sum[NV];
         if (P.near) {                          /* interpolate_near: the node l */
-            load_node(P.fld16, base, sum);
+            load_node(P.fld16, PT_CHK(P, base, P.nrec), sum);
         } else {
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
                 float v[NV];
-                load_node(P.fld16, base + ((q & 4) ? 1 : 0) + ((q & 2) ? 9 : 0) + ((q & 1) ? 81 : 0), v);
+                load_node(P.fld16, PT_CHK(P, base + ((q & 4) ? 1 : 0) + ((q & 2) ? 9 : 0) + ((q & 1) ? 81 : 0),
+                                          P.nrec), v);
 #pragma unroll
                 for (int c = 0; c < NV; ++c) sum[c] = (q == 0) ? w8[0] * v[c] : fmaf(w8[q], v[c], sum[c]);
             }

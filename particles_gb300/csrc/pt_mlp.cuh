@@ -245,17 +245,19 @@ struct PtRecordCorners {
     int64_t lo[3], hi[3];              /* l and r scaled by the node strides */
     __device__ __forceinline__ PtRecordCorners(const PtRun &P, const REC *f, const int32_t l[3],
                                                const int32_t r[3])
-        : fld(f)
+        : fld(f), oob(P.oob), nrec(P.nrec)
     {
         const int64_t d1 = P.dm[0], d12 = (int64_t)P.dm[0] * P.dm[1];
         lo[0] = l[0]; hi[0] = r[0];
         lo[1] = d1 * l[1]; hi[1] = d1 * r[1];
         lo[2] = d12 * l[2]; hi[2] = d12 * r[2];
     }
+    unsigned long long *oob;           /* bounds-checked builds */
+    int64_t nrec;
     __device__ __forceinline__ void corner(int bx, int by, int bz, float v[9]) const
     {
         const int64_t node = (bx ? hi[0] : lo[0]) + (by ? hi[1] : lo[1]) + (bz ? hi[2] : lo[2]);
-        load(node, v);
+        load(PT_CHK(*this, node, nrec), v);
     }
     __device__ __forceinline__ void load(int64_t node, float v[9]) const
     {

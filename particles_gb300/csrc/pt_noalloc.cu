@@ -147,6 +147,8 @@ extern "C" int pt_integrate_device_noalloc(int32_t method, int64_t np, int32_t m
         R.carry = nullptr;
         R.queue = reinterpret_cast<unsigned long long *>(base);
         R.flags = reinterpret_cast<int32_t *>(base + sizeof(unsigned long long));
+        R.oob = reinterpret_cast<unsigned long long *>(base + 2 * sizeof(unsigned long long));
+        R.nrec = nn;
         e = (method == PT_METHOD_RK5) ? pt_launch_rk5_exact(R, PT_NOALLOC_NC, s)
                                       : pt_launch_dp853_exact(R, PT_NOALLOC_NC, s);
     }

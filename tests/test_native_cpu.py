@@ -125,3 +125,14 @@ def test_interpolation_option_checked_on_host(native):
         o.interpolation = v
         o.controller = ctl
         assert native.pt_debug_unpack(1, 4, 2, ptr(dm), 0, 0, ptr(p), C.byref(o), ptr(out)) == rc
+
+
+def test_checked_variant_exports_the_same_symbols(native):
+    """The bounds-checked variant is built next to the library and exports
+    every symbol of the header."""
+    import ctypes as C2
+    from particles_gb300 import _native as N
+    from particles_gb300 import build as B
+    lib = C2.CDLL(str(B.build(checked=True)))
+    for name in N.EXPORTS:
+        assert hasattr(lib, name), name
