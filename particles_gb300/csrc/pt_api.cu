@@ -203,7 +203,8 @@ void attach_fields(const pt_fields *f, PtRun &R)
     R.fld16 = f->rec16;
     R.bscale = f->bscale;
     for (int i = 0; i < 3; ++i) R.nb[i] = f->nb[i];
-    R.nrec = f->precision == PT_PREC_BF16 ? (int64_t)f->nb[0] * f->nb[1] * f->nb[2] * 729 : f->nodes;
+    R.nrec = (f->precision == PT_PREC_BF16 || f->precision == PT_PREC_FP32)
+                 ? (int64_t)f->nb[0] * f->nb[1] * f->nb[2] * 729 : f->nodes;
     R.oob = f->scratch + 2;
 }
 

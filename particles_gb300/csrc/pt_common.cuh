@@ -46,7 +46,7 @@ struct PtRun {
     int64_t np;
     /* device pointers */
     const double *fld;     /* FP64 records */
-    const float *fld32;    /* FP32 records (mixed precision) */
+    const float *fld32;    /* FP32 brick records (mixed precision) */
     const uint4 *fld16;    /* BF16 brick records (PT_PREC_BF16) */
     const float *bscale;   /* per brick: FP32 offsets then scales of each component */
     int32_t nb[3];         /* bricks per axis, ceil(dm / 8) */

@@ -33,20 +33,32 @@ __global__ void k_pack_records64(int64_t nn, const double *__restrict__ uu,
     }
 }
 
-/* Planar reference layout -> FP32 node records { U, B, 0, 0 } or { U, B, J, 0, 0, 0 }. */
-__global__ void k_pack_records32(int64_t nn, const double *__restrict__ uu,
-                                 const double *__restrict__ bb, const double *__restrict__ jj,
-                                 int nc, float *__restrict__ rec)
+/* Planar reference layout -> FP32 8^3 bricks with a one-node halo on the
+ * high faces (9^3 records per brick, record (lx, ly, lz) of brick (bx, by,
+ * bz) holding node ((8 bx + lx) mod d0, ...)), so every trilinear stencil
+ * reads one brick.  A record is 8 floats {U, B, 0, 0} (32 B, one 256-bit
+ * load) or 16 floats {U, B, J, 0...} (64 B, two).  One thread per record. */
+__global__ void k_pack_bricks32(int32_t d0, int32_t d1, int32_t d2, int32_t nbx, int32_t nby,
+                                int64_t nrec, const double *__restrict__ uu,
+                                const double *__restrict__ bb, const double *__restrict__ jj,
+                                int nc, float *__restrict__ rec)
 {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        float4 *o = reinterpret_cast<float4 *>(rec + i * nc);
-        o[0] = make_float4((float)uu[i], (float)uu[i + nn], (float)uu[i + 2 * nn], (float)bb[i]);
-        if (nc == 12) {
-            o[1] = make_float4((float)bb[i + nn], (float)bb[i + 2 * nn], (float)jj[i], (float)jj[i + nn]);
-            o[2] = make_float4((float)jj[i + 2 * nn], 0.f, 0.f, 0.f);
+    const int64_t nn = (int64_t)d0 * d1 * d2;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrec;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = r / 729;
+        const int t = (int)(r - b * 729);
+        const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((int64_t)nbx * nby));
+        const int i = (bx * 8 + t % 9) % d0, j = (by * 8 + (t / 9) % 9) % d1, k = (bz * 8 + t / 81) % d2;
+        const int64_t g = i + (int64_t)d0 * (j + (int64_t)d1 * k);
+        float4 *o = reinterpret_cast<float4 *>(rec + r * nc);
+        o[0] = make_float4((float)uu[g], (float)uu[g + nn], (float)uu[g + 2 * nn], (float)bb[g]);
+        if (nc == 16) {
+            o[1] = make_float4((float)bb[g + nn], (float)bb[g + 2 * nn], (float)jj[g], (float)jj[g + nn]);
+            o[2] = make_float4((float)jj[g + 2 * nn], 0.f, 0.f, 0.f);
+            o[3] = make_float4(0.f, 0.f, 0.f, 0.f);
         } else {
-            o[1] = make_float4((float)bb[i + nn], (float)bb[i + 2 * nn], 0.f, 0.f);
+            o[1] = make_float4((float)bb[g + nn], (float)bb[g + 2 * nn], 0.f, 0.f);
         }
     }
 }
@@ -157,7 +169,7 @@ static int fields_create_impl(const int32_t dm[3], const double *uu, const doubl
     f->precision = precision;
     f->has_j = jj != nullptr;
     f->nc = f->has_j ? 10 : 6;
-    f->nc32 = f->has_j ? 12 : 8;
+    f->nc32 = f->has_j ? 16 : 8;
     f->nc16 = f->has_j ? 16 : 8;
     for (int i = 0; i < 3; ++i) f->nb[i] = (dm[i] + 7) / 8;
     f->nodes = nn;
@@ -171,8 +183,9 @@ static int fields_create_impl(const int32_t dm[3], const double *uu, const doubl
         PT_CU(cudaMalloc(&f->bscale, (size_t)nbk * ns * sizeof(float)));
         f->bytes = nbk * 729 * f->nc16 * 2 + nbk * ns * 4 + 256;
     } else if (precision == PT_PREC_FP32) {
-        PT_CU(cudaMalloc(&f->rec32, (size_t)nn * f->nc32 * sizeof(float)));
-        f->bytes = (int64_t)nn * f->nc32 * sizeof(float) + 256;
+        const int64_t nbk = (int64_t)f->nb[0] * f->nb[1] * f->nb[2];
+        PT_CU(cudaMalloc(&f->rec32, (size_t)nbk * 729 * f->nc32 * sizeof(float)));
+        f->bytes = nbk * 729 * f->nc32 * (int64_t)sizeof(float) + 256;
     } else {
         PT_CU(cudaMalloc(&f->rec64, (size_t)nn * f->nc * sizeof(double)));
         f->bytes = (int64_t)nn * f->nc * sizeof(double) + 256;
@@ -202,7 +215,9 @@ static int fields_create_impl(const int32_t dm[3], const double *uu, const doubl
             k_pack_bricks16<6><<<(unsigned)nbk, 768, 0, stream>>>(dm[0], dm[1], dm[2], f->nb[0], f->nb[1],
                                                                   d_uu, d_bb, d_jj, f->rec16, f->bscale);
         else if (precision == PT_PREC_FP32)
-            k_pack_records32<<<(int)blocks, 256, 0, stream>>>(nn, d_uu, d_bb, d_jj, f->nc32, f->rec32);
+            k_pack_bricks32<<<(int)((nbk * 729 + 255) / 256 < 65536 ? (nbk * 729 + 255) / 256 : 65536), 256, 0,
+                              stream>>>(dm[0], dm[1], dm[2], f->nb[0], f->nb[1], nbk * 729, d_uu, d_bb,
+                                        d_jj, f->nc32, f->rec32);
         else
             k_pack_records64<<<(int)blocks, 256, 0, stream>>>(nn, d_uu, d_bb, d_jj, f->nc, f->rec64);
         PT_CU(cudaGetLastError());

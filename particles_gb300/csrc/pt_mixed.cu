@@ -21,13 +21,14 @@
  *     instruction at all (the exact FP64 evaluation issues ~290).
  *
  * Field stores (HBM), chosen by the gather policy:
- *   GatherF32:   8 floats {Ux,Uy,Uz,Bx,By,Bz,0,0} = one 32-B sector per node,
- *                or 12 floats {U,B,J,0,0,0} = 48 B with eta J; x-fastest.
- *   GatherBrick: 8^3-node bricks stored with a one-node halo on their high
- *                faces (9^3 records, bricks x-fastest, records x-fastest),
- *                one record of 8 BF16 {U,B,0,0} = 16 B per node, or 16 BF16
- *                {U,B,J,0...} = 32 B with J; per brick and component an FP32
- *                offset and scale, value = offset + scale * q.
+ *   Both stores are 8^3-node bricks with a one-node halo on their high
+ *   faces (9^3 records, bricks x-fastest, records x-fastest), so the eight
+ *   corners of a stencil lie in one brick.
+ *   GatherF32:   records of 8 floats {U,B,0,0} = 32 B (one 256-bit load), or
+ *                16 floats {U,B,J,0...} = 64 B with eta J.
+ *   GatherBrick: records of 8 BF16 {U,B,0,0} = 16 B, or 16 BF16 {U,B,J,0...}
+ *                = 32 B with J; per brick and component an FP32 offset and
+ *                scale, value = offset + scale * q.
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -43,50 +44,80 @@
 
 namespace {
 
-/* Trilinear sums of FP32 node records: acc[c] = sum_q w8[q] rec(node q)[c]. */
+/* One 256-bit read-only load of 8 floats (32-B aligned; sm_100 and later). */
+__device__ __forceinline__ void pt_ld8(const float *p, float v[8])
+{
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+        : "l"(p));
+}
+
+/* Brick index of the stencil with left corner l and the record of l in it. */
+__device__ __forceinline__ int64_t pt_brick_base(const PtRun &P, const int32_t l[3], int64_t &b)
+{
+    b = PT_CHK(P, (l[0] >> 3) + (int64_t)P.nb[0] * ((l[1] >> 3) + (int64_t)P.nb[1] * (l[2] >> 3)),
+               P.nrec / 729);
+    return b * 729 + (l[0] & 7) + 9 * (l[1] & 7) + 81 * (l[2] & 7);
+}
+
+/* Trilinear sums over FP32 bricks: the brick layout of the BF16 store (8^3
+ * owned nodes + a one-node halo on the high faces, 9^3 records), records of
+ * 8 floats {U, B, 0, 0} (32 B, one 256-bit load) or 16 floats {U, B, J, 0...}
+ * (64 B, two), values stored as they are (no offset/scale). */
 template <int NC>
 struct GatherF32 {
-    static constexpr int NV = (NC == 12) ? 9 : 6;
-    static __device__ __forceinline__ void load(const float *__restrict__ fld, int64_t node,
-                                                float v[NC])
+    static constexpr int NV = (NC == 16) ? 9 : 6;
+    static __device__ __forceinline__ void load_node(const float *__restrict__ fld, int64_t node,
+                                                     float v[NV])
     {
-        const float4 *q = reinterpret_cast<const float4 *>(fld + node * NC);
+        float t[8];
+        pt_ld8(fld + node * NC, t);
 #pragma unroll
-        for (int i = 0; i < NC / 4; ++i) {
-            const float4 x = __ldg(q + i);
-            v[4 * i] = x.x;
-            v[4 * i + 1] = x.y;
-            v[4 * i + 2] = x.z;
-            v[4 * i + 3] = x.w;
+        for (int c = 0; c < 6; ++c) v[c] = t[c];
+        if (NV == 9) {
+            v[6 % NV] = t[6];
+            v[7 % NV] = t[7];
+            float u[8];
+            pt_ld8(fld + node * NC + 8, u);
+            v[8 % NV] = u[0];
         }
     }
-    using Loader = PtRecordCorners<float, NC>;
+    /* Corner loader for the learned controller's features (the brick of l
+     * holds every corner). */
+    struct Loader {
+        static constexpr int NJ = (NV == 9) ? 3 : 0;
+        const float *fld;
+        int64_t base;
+        __device__ __forceinline__ void corner(int bx, int by, int bz, float v[9]) const
+        {
+            load_node(fld, base + bx + 9 * by + 81 * bz, v);
+        }
+    };
     static __device__ __forceinline__ Loader loader(const PtRun &P, const int32_t l[3],
-                                                    const int32_t r[3])
+                                                    const int32_t *)
     {
-        return Loader(P, P.fld32, l, r);
+        Loader L;
+        int64_t b;
+        L.fld = P.fld32;
+        L.base = pt_brick_base(P, l, b);
+        return L;
     }
     static __device__ __forceinline__ void gather(const PtRun &P, const int32_t l[3],
-                                                  const int32_t r[3], const float w8[8],
-                                                  float acc[NV])
+                                                  const int32_t *, const float w8[8], float acc[NV])
     {
-        const int64_t d1 = P.dm[0], d12 = (int64_t)P.dm[0] * P.dm[1];
-        const int64_t yl = d1 * l[1], yr = d1 * r[1], zl = d12 * l[2], zr = d12 * r[2];
-        const int64_t node[8] = { l[0] + yl + zl, l[0] + yl + zr, l[0] + yr + zl, l[0] + yr + zr,
-                                  r[0] + yl + zl, r[0] + yl + zr, r[0] + yr + zl, r[0] + yr + zr };
+        int64_t b;
+        const int64_t base = pt_brick_base(P, l, b);
         if (P.near) {                          /* interpolate_near: the node l */
-            float v[NC];
-            load(P.fld32, PT_CHK(P, node[0], P.nrec), v);
-#pragma unroll
-            for (int cc = 0; cc < NV; ++cc) acc[cc] = v[cc];
+            load_node(P.fld32, PT_CHK(P, base, P.nrec), acc);
             return;
         }
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-            float v[NC];
-            load(P.fld32, PT_CHK(P, node[q], P.nrec), v);
+            float v[NV];
+            load_node(P.fld32, PT_CHK(P, base + ((q & 4) ? 1 : 0) + ((q & 2) ? 9 : 0) + ((q & 1) ? 81 : 0),
+                                      P.nrec), v);
 #pragma unroll
-            for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * v[cc] : fmaf(w8[q], v[cc], acc[cc]);
+            for (int c = 0; c < NV; ++c) acc[c] = (q == 0) ? w8[0] * v[c] : fmaf(w8[q], v[c], acc[c]);
         }
     }
 };
@@ -134,10 +165,9 @@ struct GatherBrick {
                                                     const int32_t *)
     {
         Loader L;
-        const int64_t b = PT_CHK(P, (l[0] >> 3) + (int64_t)P.nb[0] * ((l[1] >> 3) + (int64_t)P.nb[1] * (l[2] >> 3)),
-                                 P.nrec / 729);
+        int64_t b;
         L.fld = P.fld16;
-        L.base = b * 729 + (l[0] & 7) + 9 * (l[1] & 7) + 81 * (l[2] & 7);
+        L.base = pt_brick_base(P, l, b);
         const float4 *sp = reinterpret_cast<const float4 *>(P.bscale + b * NS);
 #pragma unroll
         for (int i = 0; i < NS / 4; ++i) {
@@ -149,9 +179,8 @@ struct GatherBrick {
     static __device__ __forceinline__ void gather(const PtRun &P, const int32_t l[3],
                                                   const int32_t *, const float w8[8], float acc[NV])
     {
-        const int64_t b = PT_CHK(P, (l[0] >> 3) + (int64_t)P.nb[0] * ((l[1] >> 3) + (int64_t)P.nb[1] * (l[2] >> 3)),
-                                 P.nrec / 729);
-        const int64_t base = b * 729 + (l[0] & 7) + 9 * (l[1] & 7) + 81 * (l[2] & 7);
+        int64_t b;
+        const int64_t base = pt_brick_base(P, l, b);
         float sum[NV];
         if (P.near) {                          /* interpolate_near: the node l */
             load_node(P.fld16, PT_CHK(P, base, P.nrec), sum);
@@ -369,7 +398,7 @@ cudaError_t launch(const PtRun &P, cudaStream_t s)
 }
 
 using F32_8 = EvalMixed<GatherF32<8>>;
-using F32_12 = EvalMixed<GatherF32<12>>;
+using F32_16 = EvalMixed<GatherF32<16>>;
 using B16_8 = EvalMixed<GatherBrick<8>>;
 using B16_16 = EvalMixed<GatherBrick<16>>;
 
@@ -380,13 +409,13 @@ using B16_16 = EvalMixed<GatherBrick<16>>;
 #if PT_PART != 2
 cudaError_t pt_launch_rk5_mixed(const PtRun &P, int nc, cudaStream_t s)
 {
-    return nc == 12 ? launch<PT_METHOD_RK5, F32_12, true>(P, s) : launch<PT_METHOD_RK5, F32_8, true>(P, s);
+    return nc == 16 ? launch<PT_METHOD_RK5, F32_16, true>(P, s) : launch<PT_METHOD_RK5, F32_8, true>(P, s);
 }
 
 cudaError_t pt_launch_rk5_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
                                     cudaStream_t s)
 {
-    return nc == 12 ? launch_ens<PT_METHOD_RK5, F32_12>(tab, nmem, minb, ntot, s)
+    return nc == 16 ? launch_ens<PT_METHOD_RK5, F32_16>(tab, nmem, minb, ntot, s)
                     : launch_ens<PT_METHOD_RK5, F32_8>(tab, nmem, minb, ntot, s);
 }
 
@@ -406,14 +435,14 @@ cudaError_t pt_launch_rk5_ens_bf16(const PtRun *tab, int nmem, int nc, int minb,
 #if PT_PART != 1
 cudaError_t pt_launch_dp853_mixed(const PtRun &P, int nc, cudaStream_t s)
 {
-    return nc == 12 ? launch<PT_METHOD_DOP853, F32_12, true>(P, s)
+    return nc == 16 ? launch<PT_METHOD_DOP853, F32_16, true>(P, s)
                     : launch<PT_METHOD_DOP853, F32_8, true>(P, s);
 }
 
 cudaError_t pt_launch_dp853_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
                                       cudaStream_t s)
 {
-    return nc == 12 ? launch_ens<PT_METHOD_DOP853, F32_12>(tab, nmem, minb, ntot, s)
+    return nc == 16 ? launch_ens<PT_METHOD_DOP853, F32_16>(tab, nmem, minb, ntot, s)
                     : launch_ens<PT_METHOD_DOP853, F32_8>(tab, nmem, minb, ntot, s);
 }
 
@@ -434,7 +463,7 @@ cudaError_t pt_launch_dp853_ens_bf16(const PtRun *tab, int nmem, int nc, int min
 #if PT_PART != 2
 
 /* f(vec) of the mixed-precision evaluation: nc = record width of the store
- * (8 / 12 FP32 records, or 8 / 16 BF16 brick records when brick != 0). */
+ * (8 / 16 FP32 or BF16 brick records; brick != 0 selects BF16). */
 cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int brick, int64_t n, const double *vec,
                                   double *acc, cudaStream_t s)
 {
@@ -444,7 +473,7 @@ cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int brick, int64_t n, 
         if (nc == 16) k_accel_mixed<B16_16><<<grid, 128, 0, s>>>(P, n, vec, acc);
         else k_accel_mixed<B16_8><<<grid, 128, 0, s>>>(P, n, vec, acc);
     } else {
-        if (nc == 12) k_accel_mixed<F32_12><<<grid, 128, 0, s>>>(P, n, vec, acc);
+        if (nc == 16) k_accel_mixed<F32_16><<<grid, 128, 0, s>>>(P, n, vec, acc);
         else k_accel_mixed<F32_8><<<grid, 128, 0, s>>>(P, n, vec, acc);
     }
     return cudaGetLastError();
