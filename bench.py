@@ -23,6 +23,8 @@ Reported (one JSON line, rank 0):
              CUDA-event time, against the FP64 FMA peak measured live
   cpu_baseline  the CPU oracle (OpenMP, all host threads) on a seeded
              particle subsample of the same windows
+  plain_fma  the same workload with the FMA build of the FP64 kernel (leg
+             `fma`), with its roofline against the FMA-counted FP64 peak
 
 `--impl reference` times the reference algorithm on the host cores (the CPU
 oracle, the restatement of sources/integrations.F90) on the same workload,
@@ -114,7 +116,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true",
                     help="launch every kernel in its default variant (3 blocks per SM)")
     ap.add_argument("--records", type=int, default=10_000_000)
-    ap.add_argument("--legs", default="headline,mixed,learned,ensemble",
+    ap.add_argument("--legs", default="headline,fma,mixed,learned,ensemble",
                     help="comma list of legs to run (headline always prints the line)")
     ap.add_argument("--mixed-steps", type=int, default=5)
     ap.add_argument("--accuracy-particles", type=int, default=32768)
@@ -367,6 +369,68 @@ def tune(args, f, method, prm, d_time, d_state, stream, t_stop, **kw):
                        sample=-1, **kw)
     return {"blocks_per_sm": v, "trial": "first window, all particles",
             "trial_ms": {str(k): round(t, 3) for k, t in ms.items()}}
+
+
+def plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev, stream, peak, rec_bytes):
+    """The headline workload again with the FMA build of the FP64 kernel (same
+    algorithm and operand order, multiplies and adds contracted to FMAs):
+    results within the FP64 tolerance of the CPU oracle instead of bit-identical,
+    and its roofline against the FMA-counted FP64 peak."""
+    import torch
+    from particles_gb300 import Fields, roofline
+    from particles_gb300 import _native as N
+    L = N.load()
+    m = tg.size
+    f = Fields(out[0], out[1], out[2] if len(out) > 2 else None, precision="fp64_fma")
+    with torch.cuda.stream(stream):
+        d_time = torch.tensor(tg, device=dev)
+        d_state = torch.zeros((npart, m, 8), dtype=torch.float64, device=dev)
+        d_state[:, 0, :6] = torch.tensor(s0, device=dev)
+        d_cnt = torch.zeros((npart, 3), dtype=torch.int64, device=dev)
+        d_status = torch.zeros(npart, dtype=torch.int32, device=dev)
+        d_carry = torch.zeros(int(L.pt_carry_bytes(npart)), dtype=torch.uint8, device=dev)
+    stream.synchronize()
+    ordq = QueueOrder(torch, d_cnt, enabled=not args.no_order)
+
+    def run(w):
+        order = ordq.before()
+        f.run_device(cfg["method"], prm, d_time, d_state, d_cnt, d_status, d_carry,
+                     eta=cfg["eta"], t_stop=w * window * T0, time_budget_s=900.0,
+                     stream=stream.cuda_stream, order=order)
+        ordq.after()
+
+    launch = tune(args, f, cfg["method"], prm, d_time, d_state, stream, window * T0, eta=cfg["eta"])
+    w = 0
+    for _ in range(args.warmup):
+        w += 1
+        run(w)
+    stream.synchronize()
+    acc0 = d_cnt.sum(0).cpu().numpy()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        w += 1
+        ev[k][0].record(stream)
+        run(w)
+        ev[k][1].record(stream)
+    stream.synchronize()
+    dev_s = sum(a.elapsed_time(b) for a, b in ev) * 1e-3
+    dcnt = d_cnt.cpu().numpy().sum(0) - acc0
+    flops = roofline.run_flops(cfg["method"], np.array([dcnt]), with_eta=cfg["eta"] != 0.0,
+                               fresh=False)
+    res = {"value": float(dcnt[1]) / dev_s, "unit": "particle-steps/s", "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
+           "rejected_fraction": float(dcnt[2] / max(dcnt[0], 1)),
+           "roofline": {"bound": "fp64", "achieved": flops / dev_s / 1e12, "peak": peak / 1e12,
+                        "unit": "TFLOP/s", "frac": flops / dev_s / peak,
+                        "peak_source": "FP64 FMA peak measured live on this GPU (pt_probe_peak)"},
+           "launch": launch, "precision": "fp64_fma",
+           "parity": "within the FP64 tolerance of the CPU oracle (not bit-identical)"}
+    f.close()
+    del d_state, d_cnt, d_status, d_carry
+    torch.cuda.empty_cache()
+    return res
 
 
 def mixed_leg(args, dev, stream):
@@ -770,7 +834,7 @@ def main():
     if big:                                   # host copies only for the CPU baseline
         out = tuple(a.cpu().numpy() for a in out) if not args.no_cpu else None
         torch.cuda.empty_cache()
-    rec_bytes = {"fp32": (12 if cfg["eta"] != 0.0 else 8) * 4,
+    rec_bytes = {"fp32": (16 if cfg["eta"] != 0.0 else 8) * 4,
                  "bf16": (16 if cfg["eta"] != 0.0 else 8) * 2}.get(
         args.precision, (10 if cfg["eta"] != 0.0 else 6) * 8)
     stream = torch.cuda.Stream(device=dev)
@@ -928,6 +992,11 @@ def main():
                        "d2h_bytes_per_step": int(xfer_sum[1] // k_e2e),
                        "steps": k_e2e, "api": "pt_integrate_fields (host pinned buffers: "
                        "state(8,m,np), counters, carry, status in and out every step)"}
+
+    if (args.precision == "fp64" and args.controller == "classical" and rank == 0
+            and "fma" in set(args.legs.split(",")) and args.workload == "dop853-256"):
+        line["plain_fma"] = plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev, stream,
+                                          peak, rec_bytes)
 
     if not args.no_cpu and rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline(cfg, prm, tg, out, s0, window, args.warmup,
