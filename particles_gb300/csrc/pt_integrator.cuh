@@ -390,12 +390,14 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
 
 /* ---- the kernel ---------------------------------------------------------- */
 
-/* Dynamic shared memory of one block: the k rows, then (when recording
- * accepted steps) eight pending feature floats per lane. */
+/* Dynamic shared memory of one block: the k rows, then (with a learned
+ * controller) the MLP weight blob, then (when recording accepted steps)
+ * eight pending feature floats per lane. */
 template <int METHOD>
-__host__ __device__ constexpr int smem_bytes(int block, bool record)
+__host__ __device__ constexpr int smem_bytes(int block, bool record, bool mlp = false)
 {
-    return Traits<METHOD>::ROWS * 6 * 8 * block + (record ? 8 * 4 * block : 0);
+    return Traits<METHOD>::ROWS * 6 * 8 * block + (mlp ? PT_MLP_BLOB_BYTES : 0) +
+           (record ? 8 * 4 * block : 0);
 }
 
 /* Persistent launch of one integrator variant: as many blocks as fit on
@@ -483,7 +485,12 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
     bool have_pend = false;
     int mi = 0;                            /* member this lane draws particles from */
 #define PT_Q (MB.q(mi))
-    if (LEARN && PT_Q.rec) pend = reinterpret_cast<float *>(smem_tail) + threadIdx.x;
+    /* the MLP weights are read by every warp at every accepted step: one
+     * copy per block in shared memory (11.9 KB) */
+    PtMlpSmem mlpw{};
+    const int mlp_bytes = (LEARN && PT_Q.mlp) ? PT_MLP_BLOB_BYTES : 0;
+    if (LEARN && PT_Q.mlp) mlpw = pt_mlp_load(PT_Q.mlp, smem_tail);
+    if (LEARN && PT_Q.rec) pend = reinterpret_cast<float *>(smem_tail + mlp_bytes) + threadIdx.x;
     const uint64_t t_start = pt_globaltimer();
     Lane L;
     L.p = 0; L.t = 0.0; L.dt = 0.0; L.errold = 0.0; L.tnext = 0.0; L.n = 0;
@@ -662,7 +669,7 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
                     }
                 }
                 if (PT_Q.mlp && __any_sync(0xffffffffu, want)) {
-                    const float y = pt_mlp_warp(pt_mlp_view(PT_Q.mlp), feat);
+                    const float y = pt_mlp_warp(mlpw, feat);
                     if (want) {
                         const double lo = PT_Q.fcmn * dt;
                         const double hi = (METHOD == PT_METHOD_DOP853 && was_rejected) ? dt : PT_Q.fcmx * dt;

@@ -351,10 +351,10 @@ template <int METHOD, class EV, bool LEARN, int MINB>
 cudaError_t launch1(const PtRun &P, cudaStream_t s)
 {
     static int cache[2][2] = { { -1, 1 }, { -1, 1 } };  /* without / with recording */
-    const bool rec = LEARN && P.rec != nullptr;
+    const bool rec = LEARN && P.rec != nullptr, mlp = LEARN && P.mlp != nullptr;
     return pt_sm::launch_persistent(k_integrate_mixed<METHOD, EV, LEARN, MINB>, PT_BLOCK,
-                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK, rec),
-                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK, true), cache[rec], P.np, s,
+                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK, rec, mlp),
+                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK, true, LEARN), cache[rec], P.np, s,
                                     P);
 }
 

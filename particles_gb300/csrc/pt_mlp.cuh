@@ -78,21 +78,6 @@ __device__ __forceinline__ uint32_t pt_silu_h2(float z0, float z1)
     return *reinterpret_cast<const uint32_t *>(&y);
 }
 
-/* Views of a blob; blob may be shared memory or global memory (the
- * integrator reads it through L1, 11.9 KB, so the k rows keep all of the
- * shared memory and the occupancy of the classical kernel). */
-__device__ __forceinline__ PtMlpSmem pt_mlp_view(const unsigned char *blob)
-{
-    PtMlpSmem m;
-    m.frag = reinterpret_cast<const uint2 *>(blob);
-    m.b1 = reinterpret_cast<const float *>(blob + PT_MLP_NFRAG * 8);
-    m.b2 = m.b1 + 64;
-    m.b3 = m.b2 + 64;
-    m.mu = m.b3 + 4;
-    m.isd = m.mu + 8;
-    return m;
-}
-
 /* Copies the blob into shared memory (whole block, before the main loop). */
 __device__ __forceinline__ PtMlpSmem pt_mlp_load(const unsigned char *blob, unsigned char *smem)
 {
