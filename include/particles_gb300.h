@@ -288,6 +288,37 @@ int pt_integrate_device_noalloc(int32_t method, int64_t np, int32_t m, const int
                                 const double *d_uu, const double *d_bb, double *d_state,
                                 int64_t *d_cnt, int32_t *d_status, void *stream);
 
+/* ---- initial state and its moments (the step before the path) ------------ */
+
+/* Seeded initial states, written on the device into row 0 of
+ * d_state(8, m, np) (columns 0..5; the integrator writes 6..7).  Replaces the
+ * driver's draw (particles.F90:291-296: uniform positions scaled to the domain,
+ * random.F90:104-120; Maxwellian momenta, random.F90:138-179), whose
+ * random_number is unseeded, by a counter-based SplitMix64 stream: particle
+ * index0 + i of seed `seed` always gets the same numbers, so ranks and
+ * subsamples regenerate their particles on their own.
+ *   kind PT_INIT_SPEED:      isotropic directions, |v|/c = p[6]
+ *   kind PT_INIT_GAMMA:      isotropic directions, Lorentz factor log-uniform
+ *                            in [p[6], p[7]]
+ *   kind PT_INIT_MAXWELLIAN: u components normal(0, p[6]) by the Marsaglia
+ *                            polar method (random.F90:152-175)
+ * p[0..2] domain lower corner, p[3..5] upper corner.  Positions, directions'
+ * cosines and the speed kind are bit-identical to the host generator
+ * (particles_gb300.initial); values through log, exp, sin, cos agree to a few
+ * ulps.  Launches on `stream` without synchronising. */
+#define PT_INIT_SPEED      0
+#define PT_INIT_GAMMA      1
+#define PT_INIT_MAXWELLIAN 2
+int pt_initial_state(int32_t kind, int64_t np, int32_t m, uint64_t seed, int64_t index0,
+                     const double p[8], double *d_state, void *stream);
+
+/* Mean, standard deviation, skewness and excess kurtosis of n device values
+ * d_x[0], d_x[stride], ... (random.F90:196-222 with the compensated means of
+ * :318-353), e.g. one component of row 0 of state(8, m, np) with stride 8 m.
+ * Deterministic: fixed-order compensated partial sums per block, combined in
+ * block order.  Synchronises `stream` and writes out[4] on the host. */
+int pt_moments(int64_t n, const double *d_x, int64_t stride, double out[4], void *stream);
+
 /* ---- diagnostics --------------------------------------------------------- */
 
 const char *pt_last_error(void);

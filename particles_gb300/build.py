@@ -47,6 +47,7 @@ UNITS = [
     ("pt_mixed2.o", "pt_mixed.cu", ["--fmad=true", "-DPT_PART=2"]),
     ("pt_probe.o", "pt_probe.cu", ["--fmad=true"]),
     ("pt_noalloc.o", "pt_noalloc.cu", ["--fmad=false"]),
+    ("pt_initial.o", "pt_initial.cu", ["--fmad=false"]),
     ("pt_mlp_train.o", "pt_mlp_train.cu", ["--fmad=true"]),
 ]
 

@@ -126,3 +126,59 @@ def moments(a: np.ndarray) -> np.ndarray:
     mom[2] = neumaier_sum(tmp ** 3) / n
     mom[3] = neumaier_sum(tmp ** 4) / n - 3.0
     return mom
+
+
+# ---- on the device (pt_initial_state / pt_moments) --------------------------
+
+def _stream_ptr(stream):
+    return None if stream is None else int(stream)
+
+
+def state_on_device(state, seed: int, *, kind: str = "gamma", speed: float | None = None,
+                    gamma_range: tuple[float, float] | None = None, vth: float | None = None,
+                    domain_min=(0.0, 0.0, 0.0), domain_max=(1.0, 1.0, 1.0), index0: int = 0,
+                    stream=None):
+    """Fill row 0 (x, u) of a CUDA float64 tensor state of shape (np, m, 8) on
+    the device: the same draws as `isotropic_state` (kind "speed" or "gamma")
+    or `maxwellian_state` (kind "maxwellian"), for particles index0 ..
+    index0 + np - 1 of the seeded set.  Launches on `stream` (a CUDA stream
+    handle; default stream if None) without synchronising."""
+    import ctypes as C
+    from . import _native as N
+    if state.dtype.itemsize != 8 or state.dim() != 3 or state.shape[2] != 8 or not state.is_cuda:
+        raise ValueError("state must be a CUDA float64 tensor of shape (np, m, 8)")
+    if not state.is_contiguous():
+        raise ValueError("state must be contiguous")
+    p = np.zeros(8)
+    p[0:3], p[3:6] = domain_min, domain_max
+    if kind == "speed":
+        k, p[6] = N.PT_INIT_SPEED, speed
+    elif kind == "gamma":
+        k, (p[6], p[7]) = N.PT_INIT_GAMMA, gamma_range
+    elif kind == "maxwellian":
+        k, p[6] = N.PT_INIT_MAXWELLIAN, vth
+    else:
+        raise ValueError(f"unknown kind {kind!r}")
+    L = N.load()
+    N.check(L.pt_initial_state(k, state.shape[0], state.shape[1], C.c_uint64(seed), index0,
+                               p.ctypes.data_as(C.c_void_p), C.c_void_p(state.data_ptr()),
+                               C.c_void_p(_stream_ptr(stream))), "pt_initial_state")
+    return state
+
+
+def moments_on_device(x, stream=None) -> np.ndarray:
+    """`moments` of a 1-D CUDA float64 tensor (any stride, e.g. the view
+    state[:, 0, c] of one initial-state component), computed on the device
+    with deterministic compensated sums.  Synchronises the stream."""
+    import ctypes as C
+    from . import _native as N
+    if x.dtype.itemsize != 8 or not x.is_cuda or x.dim() != 1 or x.numel() < 1:
+        raise ValueError("x must be a non-empty 1-D CUDA float64 tensor")
+    if x.stride(0) < 1:
+        raise ValueError("x must have a positive stride")
+    out = np.zeros(4)
+    L = N.load()
+    N.check(L.pt_moments(x.numel(), C.c_void_p(x.data_ptr()), x.stride(0),
+                         out.ctypes.data_as(C.c_void_p), C.c_void_p(_stream_ptr(stream))),
+            "pt_moments")
+    return out

@@ -136,3 +136,19 @@ def test_checked_variant_exports_the_same_symbols(native):
     lib = C2.CDLL(str(B.build(checked=True)))
     for name in N.EXPORTS:
         assert hasattr(lib, name), name
+
+
+def test_initial_state_argument_errors_need_no_gpu(native):
+    import ctypes as C
+    from particles_gb300 import _native as N
+    p = np.zeros(8)
+    p[3:6] = 1.0
+    vp = C.c_void_p
+    args = lambda kind, npart, m=2: (kind, npart, m, C.c_uint64(1), 0, p.ctypes.data_as(vp), None, None)
+    assert native.pt_initial_state(*args(7, 10)) == N.PT_ERR_ARG        # unknown kind
+    assert native.pt_initial_state(*args(N.PT_INIT_SPEED, -1)) == N.PT_ERR_ARG
+    assert native.pt_initial_state(*args(N.PT_INIT_SPEED, 10, 0)) == N.PT_ERR_ARG   # m < 1
+    assert native.pt_initial_state(*args(N.PT_INIT_SPEED, 0)) == N.PT_OK  # nothing to do
+    assert native.pt_initial_state(*args(N.PT_INIT_SPEED, 10)) == N.PT_ERR_ARG      # NULL state
+    out = np.zeros(4)
+    assert native.pt_moments(0, None, 1, out.ctypes.data_as(vp), None) == N.PT_ERR_ARG
