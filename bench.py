@@ -521,8 +521,6 @@ def mixed_leg(args, dev, stream):
             del rec
         del st, cnt, status, carry
         torch.cuda.empty_cache()
-    if model is not None:
-        model.close()
     out["accepted_steps_per_s"] = {k: v["value"] for k, v in rates.items()}
     out["detail"] = rates
     out["mixed_over_plain_exact"] = rates["fp32"]["value"] / rates["fp64"]["value"]
@@ -538,10 +536,15 @@ def mixed_leg(args, dev, stream):
         rates["bf16_learned"]["particle_gyroperiods_per_s"]
         / rates["fp64"]["particle_gyroperiods_per_s"])
 
-    # accuracy: a seeded subsample integrated as far as the time budget allows
+    # accuracy of every variant: a seeded subsample, the exact kernel integrated
+    # as far as a third of the time budget allows, every other variant to the
+    # same output time
     na = min(args.accuracy_particles, npart)
     res = {}
-    for prec in ("fp64", "fp32", "bf16"):
+    w_ref = cfg["periods"]
+    for name, prec in (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"), ("bf16", "bf16"),
+                       ("fp32_learned", "fp32"), ("bf16_learned", "bf16")):
+        mdl = model if name.endswith("_learned") else None
         st, cnt, status, carry = fresh(na)
         t_start = time.perf_counter()
         w = 0
@@ -549,19 +552,24 @@ def mixed_leg(args, dev, stream):
             w += 1
             handles[prec].run_device("rk5", prm, d_time, st, cnt, status, carry,
                                      t_stop=min(w * T0, tmax), time_budget_s=900.0,
-                                     stream=stream.cuda_stream)
+                                     stream=stream.cuda_stream, model=mdl)
             stream.synchronize()
-            if w >= cfg["periods"] or time.perf_counter() - t_start > args.accuracy_seconds / 3:
+            if w >= w_ref or (name == "fp64" and
+                              time.perf_counter() - t_start > args.accuracy_seconds / 3):
                 break
-        res[prec] = (st.cpu().numpy(), w)
+        if name == "fp64":
+            w_ref = w
+        res[name] = (st.cpu().numpy(), w)
     from particles_gb300 import errors
     out["accuracy"] = {}
-    for prec in ("fp32", "bf16"):
+    for prec in ("fp64_fma", "fp32", "bf16", "fp32_learned", "bf16_learned"):
         nrow = min(res["fp64"][1], res[prec][1])       # sample index reached by both
         rep = errors.report(res["fp64"][0], res[prec][0], rows=(1, nrow), tgrid=tg / T0)
         rep["reference"] = "exact FP64 kernel (bit-identical to the CPU oracle)"
         rep["particles"] = na
         out["accuracy"][prec] = rep
+    if model is not None:
+        model.close()
     for f in handles.values():
         f.close()
     return out
