@@ -82,6 +82,14 @@ WORKLOADS = {
 # accepted steps per second are not bought with shorter steps.
 LEARNED_SAFETY = 0.75
 
+# Variants of the mixed-precision leg: (name, field precision).  "_learned":
+# the learned controller proposes trial steps; "_face": trial steps end just
+# past the next cell face (PT_CTL_FACE).
+MIXED_VARIANTS = (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"), ("bf16", "bf16"),
+                  ("fp32_learned", "fp32"), ("bf16_learned", "bf16"), ("fp32_face", "fp32"),
+                  ("bf16_face", "bf16"), ("fp32_learned_face", "fp32"),
+                  ("bf16_learned_face", "bf16"))
+
 # dram__bytes_read.sum + dram__bytes_write.sum of one timed full-size window,
 # from a single-pass ncu capture of the same command
 # (profiles/k_integrate_full_size_single_pass.md)
@@ -472,19 +480,21 @@ def mixed_leg(args, dev, stream):
     from particles_gb300 import learned as LRN
     rates = {}
     model = None
-    for name, prec in (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"),
-                       ("bf16", "bf16"), ("fp32_learned", "fp32"), ("bf16_learned", "bf16")):
+    for name, prec in MIXED_VARIANTS:
         f = handles[prec]
-        mdl = model if name.endswith("_learned") else None
+        mdl = model if "_learned" in name else None
+        face = name.endswith("_face")
         st, cnt, status, carry = fresh(npart)
-        launch = tune(args, f, "rk5", prm, d_time, st, stream, window * T0, model=mdl)
+        launch = tune(args, f, "rk5", prm, d_time, st, stream, window * T0, model=mdl,
+                      face_steps=face)
         ordq = QueueOrder(torch, cnt, enabled=not args.no_order)
         w = 0
         for _ in range(args.warmup):
             w += 1
             o = ordq.before()
             f.run_device("rk5", prm, d_time, st, cnt, status, carry, t_stop=w * window * T0,
-                         time_budget_s=900.0, stream=stream.cuda_stream, order=o, model=mdl)
+                         time_budget_s=900.0, stream=stream.cuda_stream, order=o, model=mdl,
+                         face_steps=face)
             ordq.after()
         stream.synchronize()
         c0 = cnt.sum(0).cpu().numpy()
@@ -494,7 +504,8 @@ def mixed_leg(args, dev, stream):
             w += 1
             o = ordq.before()
             f.run_device("rk5", prm, d_time, st, cnt, status, carry, t_stop=w * window * T0,
-                         time_budget_s=900.0, stream=stream.cuda_stream, order=o, model=mdl)
+                         time_budget_s=900.0, stream=stream.cuda_stream, order=o, model=mdl,
+                         face_steps=face)
             ordq.after()
         e1.record(stream)
         stream.synchronize()
@@ -531,6 +542,10 @@ def mixed_leg(args, dev, stream):
     out["physics_rate_mixed_learned_over_plain_exact"] = (
         rates["fp32_learned"]["particle_gyroperiods_per_s"]
         / rates["fp64"]["particle_gyroperiods_per_s"])
+    out["over_plain_exact"] = {k: v["value"] / rates["fp64"]["value"] for k, v in rates.items()}
+    out["physics_rate_over_plain_exact"] = {
+        k: v["particle_gyroperiods_per_s"] / rates["fp64"]["particle_gyroperiods_per_s"]
+        for k, v in rates.items()}
     out["bf16_learned_over_plain_exact"] = rates["bf16_learned"]["value"] / rates["fp64"]["value"]
     out["physics_rate_bf16_learned_over_plain_exact"] = (
         rates["bf16_learned"]["particle_gyroperiods_per_s"]
@@ -542,9 +557,9 @@ def mixed_leg(args, dev, stream):
     na = min(args.accuracy_particles, npart)
     res = {}
     w_ref = cfg["periods"]
-    for name, prec in (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"), ("bf16", "bf16"),
-                       ("fp32_learned", "fp32"), ("bf16_learned", "bf16")):
-        mdl = model if name.endswith("_learned") else None
+    for name, prec in MIXED_VARIANTS:
+        mdl = model if "_learned" in name else None
+        face = name.endswith("_face")
         st, cnt, status, carry = fresh(na)
         t_start = time.perf_counter()
         w = 0
@@ -552,7 +567,7 @@ def mixed_leg(args, dev, stream):
             w += 1
             handles[prec].run_device("rk5", prm, d_time, st, cnt, status, carry,
                                      t_stop=min(w * T0, tmax), time_budget_s=900.0,
-                                     stream=stream.cuda_stream, model=mdl)
+                                     stream=stream.cuda_stream, model=mdl, face_steps=face)
             stream.synchronize()
             if w >= w_ref or (name == "fp64" and
                               time.perf_counter() - t_start > args.accuracy_seconds / 3):
@@ -562,7 +577,7 @@ def mixed_leg(args, dev, stream):
         res[name] = (st.cpu().numpy(), w)
     from particles_gb300 import errors
     out["accuracy"] = {}
-    for prec in ("fp64_fma", "fp32", "bf16", "fp32_learned", "bf16_learned"):
+    for prec, _ in MIXED_VARIANTS[1:]:
         nrow = min(res["fp64"][1], res[prec][1])       # sample index reached by both
         rep = errors.report(res["fp64"][0], res[prec][0], rows=(1, nrow), tgrid=tg / T0)
         rep["reference"] = "exact FP64 kernel (bit-identical to the CPU oracle)"
@@ -846,6 +861,12 @@ def main():
                  "bf16": (16 if cfg["eta"] != 0.0 else 8) * 2}.get(
         args.precision, (10 if cfg["eta"] != 0.0 else 6) * 8)
     stream = torch.cuda.Stream(device=dev)
+    # Every torch operation of the run (allocations, queue orders, fresh
+    # states) goes to the stream the kernels run on: the caching allocator
+    # then reuses a freed block only for work ordered after the kernels that
+    # read it (a queue-order array freed while a queued window still reads
+    # it would otherwise be overwritten under that window).
+    torch.cuda.set_stream(stream)
     with torch.cuda.stream(stream):
         d_time = torch.tensor(tg, device=dev)
         d_state = torch.zeros((npart, m, 8), dtype=torch.float64, device=dev)

@@ -49,6 +49,11 @@ extern "C" {
 #define PT_PREC_FP32       2  /* FP32 fields, gather and force; FP64 RK sums, error, controller */
 #define PT_PREC_BF16       3  /* BF16 8^3 bricks with an FP32 scale per brick and component */
 
+/* Step-size controllers (pt_options.controller, bits). */
+#define PT_CTL_CLASSICAL   0  /* pt_options.controller: the reference's controller */
+#define PT_CTL_LEARNED     1  /* bit: the learned MLP proposes the trial step */
+#define PT_CTL_FACE        2  /* bit: trial steps end just past the next cell face */
+
 /* Return codes. */
 #define PT_OK               0
 #define PT_ERR_ARG         -1  /* invalid argument */
@@ -57,7 +62,8 @@ extern "C" {
 #define PT_ERR_TIMEOUT     -4  /* the time budget expired; carry and status are consistent */
 #define PT_ERR_UNSUPPORTED -5  /* option combination not built */
 #define PT_ERR_PARTICLE    -6  /* at least one particle ended with a negative status */
-#define PT_ERR_BOUNDS      -7  /* bounds-checked build: a gather indexed outside the field */
+#define PT_ERR_BOUNDS      -7  /* an index out of range: a queue-order entry outside [0, np), or
+                                  (bounds-checked build) a gather outside the field */
 
 /* Per-particle status (pt_options.status / device status arrays). */
 #define PT_ST_DONE          0  /* t reached tmax */
@@ -75,7 +81,10 @@ typedef struct pt_options {
     int32_t       struct_size;    /* sizeof(pt_options), or 0 */
     int32_t       precision;      /* PT_PREC_* */
     int32_t       open_x;         /* 1: particles escape through x = xmin / xmax of the domain */
-    int32_t       controller;     /* 0 classical; 1 learned trial step (needs a model) */
+    int32_t       controller;     /* PT_CTL_* bits: 0 classical; PT_CTL_LEARNED learned
+                                     trial step (needs a model); PT_CTL_FACE trial step
+                                     capped just past the next cell face (not with
+                                     PT_PREC_FP64, which keeps the reference's controller) */
     int64_t       max_steps;      /* attempt cap per particle; 0 = 1e9 */
     double        eta;            /* resistivity: E = -U x B + eta J; 0 = ideal */
     const double *jj;             /* J = curl B in the layout of bb; required iff eta != 0 */
@@ -85,7 +94,7 @@ typedef struct pt_options {
     void         *carry;          /* host: pt_carry_bytes(np) bytes of controller memory
                                      for resumable windows (zero-filled = fresh), or NULL */
     const void   *model;          /* learned controller (a pt_mlp from pt_mlp_create) used
-                                     when controller == 1 */
+                                     when controller has PT_CTL_LEARNED */
     void         *records;        /* device buffer for accepted-step records (pt_run_device
                                      only): a 16-byte header whose first 8 bytes count the
                                      records, then records of 10 floats each */
@@ -355,6 +364,11 @@ int pt_debug_ctl_pow(int64_t n, const double *d_x, const double *d_y, double *d_
  * the FP64 instructions they replace (4 doubles and 2 ints per input). */
 int pt_debug_intpipe(int64_t n, const double *d_x, int32_t d, double *d_out, int32_t *d_idx,
                      void *stream);
+/* Constants of PT_CTL_FACE for the runs prepared after the call (all
+ * threads): faces within skip x the proposed step are crossed (0 <= skip < 1,
+ * default 0.1) and steps end `over` cells of the fastest axis past the
+ * capping face (0 < over < 1, default 3e-5). */
+int pt_debug_face_params(float skip, float over);
 int pt_debug_accel(const pt_fields *f, int64_t n, const double params[17],
                    const double *d_vec, double *d_acc, void *stream);
 

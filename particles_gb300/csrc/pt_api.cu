@@ -102,6 +102,14 @@ void unpack_params(const double *p, const RunShape &g, PtRun &R)
     R.qomf = (float)R.qom;
 }
 
+/* Face-cap constants (PT_CTL_FACE); pt_debug_face_params sets them.  Tuned
+ * on the mixed-precision workload (RK5, rtol 1e-8, 512^3, FP32): crossing
+ * faces within the first 10 % of the step and ending steps 3e-5 cells past
+ * the capping face gave 1.64x the simulated time per second of the classical
+ * controller (skip 0.05 / 0.15: 1.52x / 1.60x; overshoot 1e-2 / 1e-3 / 1e-4:
+ * 1.09x / 1.46x / 1.62x). */
+static float g_face_skip = 0.1f, g_face_over = 3.0e-5f;
+
 int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
                        const double *params, const pt_options *opt, PtRun &R)
 {
@@ -120,17 +128,20 @@ int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
     if (opt) {
         if (opt->precision != g.precision)
             return set_err(PT_ERR_ARG, "options precision differs from the field handle%s");
-        if (opt->controller != 0 && opt->controller != 1)
+        if (opt->controller < 0 || opt->controller > (PT_CTL_LEARNED | PT_CTL_FACE))
             return set_err(PT_ERR_ARG, "unknown controller%s");
-        if (opt->controller == 1 && !opt->model)
-            return set_err(PT_ERR_ARG, "controller 1 needs opt->model%s");
+        if ((opt->controller & PT_CTL_LEARNED) && !opt->model)
+            return set_err(PT_ERR_ARG, "the learned controller needs opt->model%s");
+        if ((opt->controller & PT_CTL_FACE) && g.precision == PT_PREC_FP64)
+            return set_err(PT_ERR_UNSUPPORTED, "PT_PREC_FP64 keeps the reference's controller; "
+                                               "face-capped steps need another precision%s");
         if (opt->records && opt->record_capacity < 0)
             return set_err(PT_ERR_ARG, "negative record capacity%s");
         if (opt->blocks_per_sm != 0 && (opt->blocks_per_sm < 2 || opt->blocks_per_sm > 4))
             return set_err(PT_ERR_ARG, "blocks_per_sm must be 0, 2, 3 or 4%s");
         if (opt->interpolation != 0 && opt->interpolation != 1)
             return set_err(PT_ERR_ARG, "interpolation must be 0 (trilinear) or 1 (nearest node)%s");
-        if (opt->interpolation == 1 && opt->controller == 1)
+        if (opt->interpolation == 1 && (opt->controller & PT_CTL_LEARNED))
             return set_err(PT_ERR_UNSUPPORTED, "the learned controller's features need the trilinear gather%s");
         eta = opt->eta;
         t_stop = opt->t_stop;
@@ -155,7 +166,11 @@ int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
     R.m = m;
     R.np = np;
     if (opt) {
-        R.mlp = (opt->controller == 1) ? pt_mlp_blob(static_cast<const pt_mlp *>(opt->model)) : nullptr;
+        R.mlp = (opt->controller & PT_CTL_LEARNED)
+                    ? pt_mlp_blob(static_cast<const pt_mlp *>(opt->model)) : nullptr;
+        R.face = (opt->controller & PT_CTL_FACE) ? 1 : 0;
+        R.face_skip = g_face_skip;
+        R.face_over = g_face_over;
         R.rec = static_cast<float *>(opt->records);
         R.rec_cap = opt->record_capacity;
         R.order = opt->order;
@@ -399,7 +414,7 @@ extern "C" int pt_run_check(const pt_fields *f)
     int32_t flags[2];
     memcpy(flags, &w[0], sizeof flags);
     if (w[1]) {
-        snprintf(g_err, sizeof g_err, "%llu gather index(es) outside the field records", w[1]);
+        snprintf(g_err, sizeof g_err, "%llu index(es) out of range (gathers outside the field records or queue-order entries outside [0, np))", w[1]);
         return PT_ERR_BOUNDS;
     }
     if (flags[0]) return set_err(PT_ERR_TIMEOUT, "time budget expired%s");
@@ -498,3 +513,12 @@ extern "C" int pt_debug_accel(const pt_fields *f, int64_t n, const double params
     return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_accel");
 }
 
+
+extern "C" int pt_debug_face_params(float skip, float over)
+{
+    if (!(skip >= 0.0f && skip < 1.0f) || !(over > 0.0f && over < 1.0f))
+        return set_err(PT_ERR_ARG, "pt_debug_face_params: skip in [0, 1), over in (0, 1)%s");
+    g_face_skip = skip;
+    g_face_over = over;
+    return PT_OK;
+}

@@ -34,6 +34,9 @@ struct PtRun {
     int32_t dm_mask[3];     /* dm - 1 when dm is a power of two, else 0 */
     int32_t unit_map;      /* xl == +0 and xs == 1: (pos - xl) / xs == pos exactly */
     int32_t near;          /* 1: interpolate_near (the node at the cell's lower corner) */
+    int32_t face;          /* 1: trial steps capped just past the next cell face */
+    float face_skip;       /* faces within face_skip x the proposed step are crossed */
+    float face_over;       /* overshoot past the capping face, in cells of the fastest axis */
     /* extensions */
     double eta;
     int32_t has_j;

@@ -244,8 +244,9 @@ extern "C" int pt_ensemble_create(int32_t method, int32_t nmembers, const pt_mem
     *out = nullptr;
     if (nmembers < 1 || nmembers > PT_ENSEMBLE_MAX || !members)
         return set_err(PT_ERR_ARG, "need 1..8 members%s");
-    if (opt && opt->controller != 0)
-        return set_err(PT_ERR_UNSUPPORTED, "ensembles run the classical controller%s");
+    if (opt && (opt->controller & PT_CTL_LEARNED))
+        return set_err(PT_ERR_UNSUPPORTED, "ensembles run the classical controller (with or "
+                                           "without PT_CTL_FACE)%s");
     const pt_fields *f0 = members[0].fields;
     if (!f0) return set_err(PT_ERR_ARG, "member 0 has no field handle%s");
     const int32_t prec = opt ? opt->precision : PT_PREC_FP64;
@@ -269,6 +270,7 @@ extern "C" int pt_ensemble_create(int32_t method, int32_t nmembers, const pt_mem
         o.time_budget_s = opt ? opt->time_budget_s : 0.0;
         o.blocks_per_sm = opt ? opt->blocks_per_sm : 0;
         o.interpolation = opt ? opt->interpolation : 0;
+        o.controller = opt ? opt->controller : 0;
         int rc = prepare_run(method, M.np, M.m, shape_of(M.fields), M.params, &o, tab[k]);
         if (rc != PT_OK) return rc;
         ntot += M.np;
@@ -430,7 +432,7 @@ extern "C" int pt_ensemble_check(const pt_ensemble *e)
     int32_t flags[2];
     memcpy(flags, &w[0], sizeof flags);
     if (w[1]) {
-        snprintf(g_err, sizeof g_err, "%llu gather index(es) outside the field records", w[1]);
+        snprintf(g_err, sizeof g_err, "%llu index(es) out of range (gathers outside the field records or queue-order entries outside [0, np))", w[1]);
         return PT_ERR_BOUNDS;
     }
     if (flags[0]) return set_err(PT_ERR_TIMEOUT, "time budget expired%s");

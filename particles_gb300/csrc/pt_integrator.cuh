@@ -388,6 +388,42 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
     }
 }
 
+#ifndef PT_EXACT
+/* Cap of the next trial step h for PT_CTL_FACE.  Trilinear fields are smooth
+ * inside a cell and have a gradient jump at every face; a step that crosses a
+ * face well inside it carries an error set by that jump, while a face crossed
+ * near either end of the step costs little.  Along the straight path from si
+ * (the step is a small fraction of a gyration), the cap is the first face
+ * reached after face_skip x h -- faces before it are crossed near the start
+ * -- plus the time to cross face_over of a cell along the fastest axis, so
+ * the step ends just past that face.  FP32 suffices (an estimate; the error
+ * norm still accepts or rejects the step). */
+__device__ __forceinline__ double pt_face_cap(const PtRun &P, const double si[6], double h)
+{
+    const float ux = pt_d2f(si[3]), uy = pt_d2f(si[4]), uz = pt_d2f(si[5]);
+    const float ig = rsqrtf(fmaf(ux, ux, fmaf(uy, uy, fmaf(uz, uz, 1.0f))));
+    const float u[3] = { ux, uy, uz };
+    const float th = P.face_skip * pt_d2f(h);
+    float tmin = 3.0e38f, wmax = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double xn = fma(si[i], P.gsx[i], P.gox[i]);
+        const float off = pt_d2f(xn - pt_floor(xn));               /* in [0, 1] */
+        const float w = u[i] * ig * P.ivunf * P.gsxf[i];           /* cells per unit time */
+        const float aw = fabsf(w);
+        if (aw > 0.0f) {
+            const float d = (w > 0.0f) ? 1.0f - off : off;          /* cells to the next face */
+            /* first face on this axis at or after time th: d + k cells */
+            const float k = fmaxf(0.0f, ceilf(fmaf(th, aw, -d)));
+            tmin = fminf(tmin, (d + k) / aw);
+        }
+        wmax = fmaxf(wmax, aw);
+    }
+    if (!(wmax > 0.0f)) return h;
+    return pt_min(h, pt_f2d(tmin + P.face_over / wmax));
+}
+#endif
+
 /* ---- the kernel ---------------------------------------------------------- */
 
 /* Dynamic shared memory of one block: the k rows, then (with a learned
@@ -527,7 +563,16 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
                 while (!got && mi < MB.count()) {
                     qi = atomicAdd(PT_Q.queue, 1ULL);
                     got = (int64_t)qi < MB.queue_len(mi);
-                    if (!got) ++mi;
+                    if (!got) {
+                        ++mi;
+                    } else if (PT_Q.order) {
+                        /* a queue-order entry outside [0, np) is skipped and counted */
+                        const int64_t p = (int64_t)PT_Q.order[qi];
+                        if (p < 0 || p >= PT_Q.np) {
+                            if (PT_Q.oob) atomicAdd(PT_Q.oob, 1ULL);
+                            got = false;
+                        }
+                    }
                 }
                 if (ENS && !got) mi = MB.count() - 1;   /* stay on a valid member */
                 if (got) {
@@ -679,6 +724,9 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
                     }
                 }
             }
+#ifndef PT_EXACT
+            if (PT_Q.face && active) L.dt = pt_face_cap(PT_Q, si, L.dt);
+#endif
             /* ---- start of the next attempt ---- */
             if (active) {
                 const int32_t st = lane_check(PT_Q, L, t_start);

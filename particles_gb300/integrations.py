@@ -34,12 +34,13 @@ def _f64(a):
 
 def _options(precision, *, eta=0.0, jj=None, open_x=False, max_steps=0, t_stop=0.0,
              status=None, carry=None, time_budget_s=0.0, model=None, records=None,
-             order=None, blocks_per_sm=0, interpolation=0):
+             order=None, blocks_per_sm=0, interpolation=0, face_steps=False):
     o = N.PtOptions()
     o.struct_size = C.sizeof(N.PtOptions)
     o.precision = N.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     o.open_x = int(bool(open_x))
-    o.controller = 1 if model is not None else 0
+    o.controller = ((N.PT_CTL_LEARNED if model is not None else 0)
+                    | (N.PT_CTL_FACE if face_steps else 0))
     o.model = model.handle if model is not None else None
     if records is not None:                       # device tensor (float32) with header
         o.records = C.c_void_p(records.data_ptr())
@@ -65,7 +66,7 @@ def carry_buffer(npart: int) -> np.ndarray:
 
 def integrate(method, params, time, uu, bb, state, cnt=None, *, precision="fp64", eta=0.0,
               jj=None, open_x=False, max_steps=0, t_stop=0.0, carry=None, status=None,
-              time_budget_s=0.0, check=True, interpolation="linear"):
+              time_budget_s=0.0, check=True, interpolation="linear", face_steps=False):
     """Integrate every particle of ``state`` in place on the GPU.
 
     Returns (state, cnt, status).  With ``check`` a negative return code
@@ -85,7 +86,7 @@ def integrate(method, params, time, uu, bb, state, cnt=None, *, precision="fp64"
     dm = np.array(uu.shape[:0:-1], np.int32)
     opt = _options(precision, eta=eta, jj=jj, open_x=open_x, max_steps=max_steps,
                    t_stop=t_stop, status=status, carry=carry, time_budget_s=time_budget_s,
-                   interpolation=interpolation)
+                   interpolation=interpolation, face_steps=face_steps)
     rc = L.pt_integrate(mid, npart, m, _ptr(dm), _ptr(_f64(params)), _ptr(_f64(time)),
                         _ptr(uu), _ptr(bb), _ptr(state), _ptr(cnt), C.byref(opt))
     if check:
@@ -153,7 +154,7 @@ class Fields:
 
     def integrate(self, method, params, time, state, cnt=None, *, eta=0.0, open_x=False,
                   max_steps=0, t_stop=0.0, carry=None, status=None, time_budget_s=0.0,
-                  check=True, interpolation="linear"):
+                  check=True, interpolation="linear", face_steps=False):
         """Host-buffer run on these fields (pt_integrate_fields)."""
         npart, m, _ = state.shape
         if cnt is None:
@@ -162,7 +163,7 @@ class Fields:
             status = np.zeros(npart, np.int32)
         opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
                        t_stop=t_stop, status=status, carry=carry, time_budget_s=time_budget_s,
-                       interpolation=interpolation)
+                       interpolation=interpolation, face_steps=face_steps)
         rc = self._L.pt_integrate_fields(method_id(method), npart, m, self._h,
                                          _ptr(_f64(params)), _ptr(_f64(time)), _ptr(state),
                                          _ptr(cnt), C.byref(opt))
@@ -173,18 +174,20 @@ class Fields:
     def run_device(self, method, params, d_time, d_state, d_cnt, d_status=None, d_carry=None,
                    *, eta=0.0, open_x=False, max_steps=0, t_stop=0.0, time_budget_s=0.0,
                    stream=0, model=None, records=None, order=None, blocks_per_sm=0,
-                   interpolation="linear"):
+                   interpolation="linear", face_steps=False):
         """Launch on device tensors (torch); returns without synchronising.
 
         model: a learned.Model for the learned controller; records: a device
         record buffer (learned.record_buffer); order: device int32 queue order;
-        blocks_per_sm: launch variant (0 = tuned or default, else 2, 3, 4).
+        blocks_per_sm: launch variant (0 = tuned or default, else 2, 3, 4);
+        face_steps: trial steps end just past the next cell face (PT_CTL_FACE,
+        not with precision "fp64").
         """
         npart, m, _ = d_state.shape
         opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
                        t_stop=t_stop, time_budget_s=time_budget_s, model=model,
                        records=records, order=order, blocks_per_sm=blocks_per_sm,
-                       interpolation=interpolation)
+                       interpolation=interpolation, face_steps=face_steps)
         rc = self._L.pt_run_device(
             method_id(method), npart, m, self._h, _ptr(_f64(params)),
             C.c_void_p(d_time.data_ptr()), C.c_void_p(d_state.data_ptr()),
@@ -196,7 +199,7 @@ class Fields:
 
     def autotune(self, method, params, d_time, d_state, *, eta=0.0, open_x=False, max_steps=0,
                  t_stop=0.0, sample=0, stream=0, model=None, records=None,
-                 interpolation="linear"):
+                 interpolation="linear", face_steps=False):
         """Time the launch variants of the kernel run_device would use with
         these arguments (pt_autotune) and make the fastest its default.
 
@@ -205,7 +208,8 @@ class Fields:
         Returns (blocks_per_sm, {variant: trial ms})."""
         npart, m, _ = d_state.shape
         opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
-                       t_stop=t_stop, model=model, records=records, interpolation=interpolation)
+                       t_stop=t_stop, model=model, records=records, interpolation=interpolation,
+                       face_steps=face_steps)
         chosen = C.c_int32(0)
         ms = np.zeros(3, np.float64)
         rc = self._L.pt_autotune(method_id(method), npart, m, self._h, _ptr(_f64(params)),
@@ -232,7 +236,7 @@ class Ensemble:
     """
 
     def __init__(self, method, members, *, precision="fp64", blocks_per_sm=0,
-                 time_budget_s=0.0, interpolation="linear"):
+                 time_budget_s=0.0, interpolation="linear", face_steps=False):
         self._L = N.load()
         self._h = C.c_void_p()
         self.n = len(members)
@@ -252,7 +256,7 @@ class Ensemble:
             for key in ("time", "state", "cnt", "status", "carry"):
                 setattr(a, key, C.c_void_p(mb[key].data_ptr()))
         opt = _options(precision, time_budget_s=time_budget_s, blocks_per_sm=blocks_per_sm,
-                       interpolation=interpolation)
+                       interpolation=interpolation, face_steps=face_steps)
         N.check(self._L.pt_ensemble_create(method_id(method), self.n, C.byref(arr), C.byref(opt),
                                            C.byref(self._h)), "pt_ensemble_create")
 

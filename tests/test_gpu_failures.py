@@ -107,3 +107,38 @@ def test_checkpoint_file_resume_is_bit_identical(cuda, oracle_lib, tmp_path):
     torch.cuda.synchronize()
     assert f2.run_check() == 0
     assert np.array_equal(cnt.cpu().numpy(), co) and np.array_equal(st.cpu().numpy(), so)
+
+
+def test_bad_queue_order_entries_are_skipped_and_reported(cuda, oracle_lib):
+    """A device queue order holding indices outside [0, np) (a caller's bug,
+    made on the host here) is not followed: those slots are skipped, counted,
+    and pt_run_check returns PT_ERR_BOUNDS; every valid slot still runs and
+    matches the oracle bit for bit."""
+    import oracle
+    torch = cuda
+    from particles_gb300 import Fields
+    from particles_gb300 import _native as N
+    prob = small_problem("rk5", n=16, npart=300, periods=1.0, seed=74)
+    uu, bb = prob["fields"]
+    npart = prob["state"].shape[0]
+    so, co, _ = oracle.integrate("rk5", prob["params"], prob["time"], uu, bb, prob["state"].copy())
+    f = Fields(uu, bb)
+    st = torch.tensor(prob["state"], device="cuda")
+    cnt = torch.zeros((npart, 3), dtype=torch.int64, device="cuda")
+    status = torch.zeros(npart, dtype=torch.int32, device="cuda")
+    d_time = torch.tensor(prob["time"], device="cuda")
+    order = np.arange(npart, dtype=np.int32)[::-1].copy()
+    bad = np.array([3, 50, 299])
+    order[bad] = [npart, -1, 1 << 30]                # particles 296, 249, 0 are never queued
+    d_order = torch.tensor(order, device="cuda")
+    torch.cuda.synchronize()
+    f.run_device("rk5", prob["params"], d_time, st, cnt, status, order=d_order)
+    torch.cuda.synchronize()
+    assert f.run_check() == N.PT_ERR_BOUNDS and b"out of range" in N.load().pt_last_error()
+    skipped = npart - 1 - bad
+    ok = np.setdiff1d(np.arange(npart), skipped)
+    s, c, stt = st.cpu().numpy(), cnt.cpu().numpy(), status.cpu().numpy()
+    assert (stt[skipped] == N.PT_ST_NOT_RUN).all() and (c[skipped] == 0).all()
+    assert (stt[ok] == 0).all()
+    assert np.array_equal(s[ok], so[ok]) and np.array_equal(c[ok], co[ok])
+    f.close()

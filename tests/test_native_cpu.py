@@ -152,3 +152,22 @@ def test_initial_state_argument_errors_need_no_gpu(native):
     assert native.pt_initial_state(*args(N.PT_INIT_SPEED, 10)) == N.PT_ERR_ARG      # NULL state
     out = np.zeros(4)
     assert native.pt_moments(0, None, 1, out.ctypes.data_as(vp), None) == N.PT_ERR_ARG
+
+
+def test_face_controller_checked_on_host(native):
+    """PT_CTL_FACE is a controller bit of the non-exact precisions only."""
+    from particles_gb300 import _native as N
+    from particles_gb300.params import pack_params
+    dm = np.array([8, 8, 8], np.int32)
+    p = pack_params(qom=1.0, vunit=0.1, tmax=1.0)
+    out = np.zeros(8)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)
+    for prec, ctl, rc in ((0, N.PT_CTL_FACE, N.PT_ERR_UNSUPPORTED), (1, N.PT_CTL_FACE, N.PT_OK),
+                          (2, N.PT_CTL_FACE, N.PT_OK), (3, N.PT_CTL_FACE, N.PT_OK),
+                          (2, N.PT_CTL_FACE | N.PT_CTL_LEARNED, N.PT_ERR_ARG),   # no model
+                          (2, 4, N.PT_ERR_ARG), (2, -1, N.PT_ERR_ARG)):
+        o = N.PtOptions()
+        o.struct_size = C.sizeof(o)
+        o.precision = prec
+        o.controller = ctl
+        assert native.pt_debug_unpack(1, 4, 2, ptr(dm), prec, 0, ptr(p), C.byref(o), ptr(out)) == rc, (prec, ctl)
