@@ -86,8 +86,8 @@ LEARNED_SAFETY = 0.75
 # the learned controller proposes trial steps; "_face": trial steps end just
 # past the next cell face (PT_CTL_FACE).
 MIXED_VARIANTS = (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"), ("bf16", "bf16"),
-                  ("fp32_learned", "fp32"), ("bf16_learned", "bf16"), ("fp32_face", "fp32"),
-                  ("bf16_face", "bf16"), ("fp32_learned_face", "fp32"),
+                  ("fp32_learned", "fp32"), ("bf16_learned", "bf16"), ("fp64_fma_face", "fp64_fma"),
+                  ("fp32_face", "fp32"), ("bf16_face", "bf16"), ("fp32_learned_face", "fp32"),
                   ("bf16_learned_face", "bf16"))
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one timed full-size window,

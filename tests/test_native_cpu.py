@@ -171,3 +171,12 @@ def test_face_controller_checked_on_host(native):
         o.precision = prec
         o.controller = ctl
         assert native.pt_debug_unpack(1, 4, 2, ptr(dm), prec, 0, ptr(p), C.byref(o), ptr(out)) == rc, (prec, ctl)
+
+
+def test_face_params_checked_on_host(native):
+    from particles_gb300 import _native as N
+    assert native.pt_debug_face_params(-0.1, 1e-4) == N.PT_ERR_ARG
+    assert native.pt_debug_face_params(1.0, 1e-4) == N.PT_ERR_ARG
+    assert native.pt_debug_face_params(0.1, 0.0) == N.PT_ERR_ARG
+    assert native.pt_debug_face_params(0.1, 1.0) == N.PT_ERR_ARG
+    assert native.pt_debug_face_params(0.1, 3e-5) == N.PT_OK          # the defaults
