@@ -24,7 +24,8 @@ Reported (one JSON line, rank 0):
   cpu_baseline  the CPU oracle (OpenMP, all host threads) on a seeded
              particle subsample of the same windows
   plain_fma  the same workload with the FMA build of the FP64 kernel (leg
-             `fma`), with its roofline against the FMA-counted FP64 peak
+             `fma`), with its roofline against the FMA-counted FP64 peak;
+             plain_fma_face the same with face-capped trial steps
 
 `--impl reference` times the reference algorithm on the host cores (the CPU
 oracle, the restatement of sources/integrations.F90) on the same workload,
@@ -108,6 +109,8 @@ def parse():
     ap.add_argument("--controller", choices=["classical", "learned"], default="classical",
                     help="learned: the first warm-up window records accepted steps, a model "
                          "is trained on them and the later windows use it")
+    ap.add_argument("--face", action="store_true",
+                    help="face-capped trial steps (PT_CTL_FACE; not with --precision fp64)")
     ap.add_argument("--particles", type=int, default=0,
                     help="override the particle count (profiling of small cases only)")
     ap.add_argument("--window", type=float, default=0.0,
@@ -379,11 +382,13 @@ def tune(args, f, method, prm, d_time, d_state, stream, t_stop, **kw):
             "trial_ms": {str(k): round(t, 3) for k, t in ms.items()}}
 
 
-def plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev, stream, peak, rec_bytes):
+def plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev, stream, peak, rec_bytes,
+                  face=False):
     """The headline workload again with the FMA build of the FP64 kernel (same
     algorithm and operand order, multiplies and adds contracted to FMAs):
     results within the FP64 tolerance of the CPU oracle instead of bit-identical,
-    and its roofline against the FMA-counted FP64 peak."""
+    and its roofline against the FMA-counted FP64 peak.  face: with
+    face-capped trial steps (PT_CTL_FACE)."""
     import torch
     from particles_gb300 import Fields, roofline
     from particles_gb300 import _native as N
@@ -404,10 +409,11 @@ def plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev, stream, peak,
         order = ordq.before()
         f.run_device(cfg["method"], prm, d_time, d_state, d_cnt, d_status, d_carry,
                      eta=cfg["eta"], t_stop=w * window * T0, time_budget_s=900.0,
-                     stream=stream.cuda_stream, order=order)
+                     stream=stream.cuda_stream, order=order, face_steps=face)
         ordq.after()
 
-    launch = tune(args, f, cfg["method"], prm, d_time, d_state, stream, window * T0, eta=cfg["eta"])
+    launch = tune(args, f, cfg["method"], prm, d_time, d_state, stream, window * T0, eta=cfg["eta"],
+                  face_steps=face)
     w = 0
     for _ in range(args.warmup):
         w += 1
@@ -430,6 +436,8 @@ def plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev, stream, peak,
     res = {"value": float(dcnt[1]) / dev_s, "unit": "particle-steps/s", "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / args.steps,
            "rejected_fraction": float(dcnt[2] / max(dcnt[0], 1)),
+           "particle_gyroperiods_per_s": npart * window * args.steps / dev_s,
+           "controller": "classical, face-capped steps" if face else "classical",
            "roofline": {"bound": "fp64", "achieved": flops / dev_s / 1e12, "peak": peak / 1e12,
                         "unit": "TFLOP/s", "frac": flops / dev_s / peak,
                         "peak_source": "FP64 FMA peak measured live on this GPU (pt_probe_peak)"},
@@ -884,7 +892,8 @@ def main():
         order = ordq.before()
         f.run_device(cfg["method"], prm, d_time, d_state, d_cnt, d_status, d_carry,
                      eta=cfg["eta"], t_stop=w * window * T0, time_budget_s=900.0,
-                     stream=stream.cuda_stream, order=order, model=model, records=records)
+                     stream=stream.cuda_stream, order=order, model=model, records=records,
+                     face_steps=args.face)
         ordq.after()
 
     w = 0
@@ -902,7 +911,7 @@ def main():
                     "recorded_in": "the first warm-up window (classical controller)"}
         del rec
     launch = tune(args, f, cfg["method"], prm, d_time, d_state, stream, window * T0,
-                  eta=cfg["eta"], model=model)
+                  eta=cfg["eta"], model=model, face_steps=args.face)
     for _ in range(args.warmup - w):
         w += 1
         window_run(w)
@@ -967,7 +976,8 @@ def main():
     line = {
         "metric": ("accepted particle-steps/s (plain FP64 kernel)"
                    if args.precision == "fp64" and args.controller == "classical"
-                   else f"accepted particle-steps/s ({args.precision}, {args.controller} controller)"),
+                   else f"accepted particle-steps/s ({args.precision}, {args.controller} controller"
+                        f"{', face-capped steps' if args.face else ''})"),
         "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -978,8 +988,9 @@ def main():
         "wall_s_timed": wall, "gpu_launches": args.steps, "stopped_particles": stopped,
         "rejected_fraction": float(dcnt_tot[2] / max(dcnt_tot[0], 1)),
         "attempts_per_s": float(dcnt_tot[0]) / elapsed,
+        "particle_gyroperiods_per_s": world * npart * window * args.steps / elapsed,
         "roofline": roof, "clocks": clocks.summary(), "launch": launch,
-        "controller": args.controller,
+        "controller": args.controller + (", face-capped steps" if args.face else ""),
     }
     if training:
         line["learned_training"] = training
@@ -1002,7 +1013,8 @@ def main():
         for _ in range(k_e2e):
             w += 1
             o = _options(args.precision, eta=cfg["eta"], t_stop=w * window * T0,
-                         status=None, carry=None, time_budget_s=900.0, model=model)
+                         status=None, carry=None, time_budget_s=900.0, model=model,
+                         face_steps=args.face)
             o.status = C.c_void_p(h_status.data_ptr())
             o.carry = C.c_void_p(h_carry.data_ptr())
             rc = L.pt_integrate_fields(method_id(cfg["method"]), npart, m, f.handle, prm.ctypes.data_as(C.c_void_p),
@@ -1026,6 +1038,8 @@ def main():
             and "fma" in set(args.legs.split(",")) and args.workload == "dop853-256"):
         line["plain_fma"] = plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev, stream,
                                           peak, rec_bytes)
+        line["plain_fma_face"] = plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev,
+                                               stream, peak, rec_bytes, face=True)
 
     if not args.no_cpu and rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline(cfg, prm, tg, out, s0, window, args.warmup,
