@@ -449,6 +449,43 @@ def plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev, stream, peak,
     return res
 
 
+def headline_accuracy(cfg, prm, tg, out, s0, dev, na=16384):
+    """Energy / position error of the FMA build, classical and with face-capped
+    steps, against the exact kernel (bit-identical to the CPU oracle) on a
+    subsample of the headline workload over one gyro-period."""
+    import torch
+    from particles_gb300 import Fields, errors
+    from particles_gb300 import _native as N
+    L = N.load()
+    m = tg.size
+    na = min(na, s0.shape[0])
+    d_time = torch.tensor(tg, device=dev)
+    res = {}
+    for name, prec, face in (("fp64", "fp64", False), ("fp64_fma", "fp64_fma", False),
+                             ("fp64_fma_face", "fp64_fma", True)):
+        f = Fields(out[0], out[1], out[2] if len(out) > 2 else None, precision=prec)
+        st = torch.zeros((na, m, 8), dtype=torch.float64, device=dev)
+        st[:, 0, :6] = torch.tensor(s0[:na], device=dev)
+        cnt = torch.zeros((na, 3), dtype=torch.int64, device=dev)
+        status = torch.zeros(na, dtype=torch.int32, device=dev)
+        carry = torch.zeros(int(L.pt_carry_bytes(na)), dtype=torch.uint8, device=dev)
+        f.run_device(cfg["method"], prm, d_time, st, cnt, status, carry, eta=cfg["eta"],
+                     t_stop=tg[1] * (1 + 1e-12), time_budget_s=900.0, face_steps=face,
+                     stream=torch.cuda.current_stream().cuda_stream)
+        torch.cuda.current_stream().synchronize()
+        res[name] = st.cpu().numpy()
+        f.close()
+        del st, cnt, status, carry
+    acc = {}
+    for name in ("fp64_fma", "fp64_fma_face"):
+        rep = errors.report(res["fp64"], res[name], rows=(1,), tgrid=tg / T0)
+        rep["reference"] = "exact FP64 kernel (bit-identical to the CPU oracle)"
+        rep["particles"] = na
+        acc[name] = rep
+    torch.cuda.empty_cache()
+    return acc
+
+
 def mixed_leg(args, dev, stream):
     """The mixed-precision workload (RK5, rtol 1e-8, 512^3, 2^22 particles): accepted
     particle-steps/s of the exact FP64, FMA FP64 and mixed FP32 kernels on the
@@ -1040,6 +1077,7 @@ def main():
                                           peak, rec_bytes)
         line["plain_fma_face"] = plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev,
                                                stream, peak, rec_bytes, face=True)
+        line["plain_fma_accuracy"] = headline_accuracy(cfg, prm, tg, out, s0, dev)
 
     if not args.no_cpu and rank == 0 and world == 1:
         line["cpu_baseline"] = cpu_baseline(cfg, prm, tg, out, s0, window, args.warmup,
