@@ -73,10 +73,10 @@ struct EvalF64 {
     {
         pt_feature_cell(P, si, l, r, xd);
     }
-    static __device__ __forceinline__ PtRecordCorners<double, NC>
+    static __device__ __forceinline__ PtRecordCorners<NC>
     feature_loader(const PtRun &P, const int32_t l[3], const int32_t r[3])
     {
-        return PtRecordCorners<double, NC>(P, P.fld, l, r);
+        return PtRecordCorners<NC>(P, P.fld, l, r);
     }
     static __device__ __forceinline__ void f(const PtRun &P, const double s[6], const double *,
                                              const Origin &, double a[6])

@@ -186,7 +186,6 @@ static __device__ __noinline__ float pt_mlp_warp(const PtMlpSmem &M, const float
 #include "pt_common.cuh"
 #include "pt_convert.cuh"
 
-__device__ __forceinline__ float pt_to_f(float v) { return v; }
 /* Features need a few digits: truncate the double's top mantissa bits into a
  * float on the integer pipe (normal range; zero maps to zero). */
 __device__ __forceinline__ float pt_to_f(double v)
@@ -220,15 +219,16 @@ __device__ __forceinline__ void pt_feature_cell(const PtRun &P, const double s[6
     }
 }
 
-/* Corner loaders of the feature gather: corner (bx, by, bz) of the cell
- * (l, r) as floats U[3], B[3] (and J[3] when NJ == 3).  Node records in
- * x-fastest order, FP64 or FP32, with vector loads. */
-template <class REC, int NCR>
+/* Corner loader of the feature gather over FP64 node records (x-fastest,
+ * NCR doubles per node): corner (bx, by, bz) of the cell (l, r) as floats
+ * U[3], B[3] (and J[3] when NJ == 3), with 16-B vector loads.  The FP32 and
+ * BF16 brick stores have their own loaders (pt_mixed.cu). */
+template <int NCR>
 struct PtRecordCorners {
     static constexpr int NJ = (NCR >= 9) ? 3 : 0;
-    const REC *fld;
+    const double *fld;
     int64_t lo[3], hi[3];              /* l and r scaled by the node strides */
-    __device__ __forceinline__ PtRecordCorners(const PtRun &P, const REC *f, const int32_t l[3],
+    __device__ __forceinline__ PtRecordCorners(const PtRun &P, const double *f, const int32_t l[3],
                                                const int32_t r[3])
         : fld(f), oob(P.oob), nrec(P.nrec)
     {
@@ -247,20 +247,11 @@ struct PtRecordCorners {
     __device__ __forceinline__ void load(int64_t node, float v[9]) const
     {
         float t[NCR];
-        if (sizeof(REC) == 4) {
-            const float4 *q = reinterpret_cast<const float4 *>(fld + node * NCR);
+        const double2 *q = reinterpret_cast<const double2 *>(fld + node * NCR);
 #pragma unroll
-            for (int i = 0; i < NCR / 4; ++i) {
-                const float4 x = __ldg(q + i);
-                t[4 * i] = x.x; t[4 * i + 1] = x.y; t[4 * i + 2] = x.z; t[4 * i + 3] = x.w;
-            }
-        } else {
-            const double2 *q = reinterpret_cast<const double2 *>(fld + node * NCR);
-#pragma unroll
-            for (int i = 0; i < NCR / 2; ++i) {
-                const double2 x = __ldg(q + i);
-                t[2 * i] = pt_to_f(x.x); t[2 * i + 1] = pt_to_f(x.y);
-            }
+        for (int i = 0; i < NCR / 2; ++i) {
+            const double2 x = __ldg(q + i);
+            t[2 * i] = pt_to_f(x.x); t[2 * i + 1] = pt_to_f(x.y);
         }
 #pragma unroll
         for (int c = 0; c < 6 + NJ; ++c) v[c] = t[c];
@@ -272,7 +263,7 @@ struct PtRecordCorners {
  * log(|grad B|/|B|), with E = -U x B + eta J and grad B the analytic
  * derivative of the trilinear interpolant (the derivatives of the same eight
  * corner weights).  xd: the offset of s in its cell; LD: a corner loader
- * (PtRecordCorners, or the brick loader of the BF16 store). */
+ * (PtRecordCorners, or the brick loaders of the FP32 and BF16 stores). */
 template <class LD>
 __device__ __forceinline__ void pt_field_features(const PtRun &P, const LD &ld, const double s[6],
                                                   const float xd[3], float out[5])
