@@ -364,11 +364,12 @@ int pt_debug_ctl_pow(int64_t n, const double *d_x, const double *d_y, double *d_
  * the FP64 instructions they replace (4 doubles and 2 ints per input). */
 int pt_debug_intpipe(int64_t n, const double *d_x, int32_t d, double *d_out, int32_t *d_idx,
                      void *stream);
-/* Constants of PT_CTL_FACE for the runs prepared after the call (all
- * threads): faces within skip x the proposed step are crossed (0 <= skip < 1,
- * default 0.1) and steps end `over` cells of the fastest axis past the
- * capping face (0 < over < 1, default 3e-5). */
-int pt_debug_face_params(float skip, float over);
+/* Constants of PT_CTL_FACE of one method for the runs prepared after the
+ * call (all threads): faces within skip x the proposed step are crossed
+ * (0 <= skip < 1; default 0.1 for RK5, 0.01 for DOP853) and steps end `over`
+ * cells of the fastest axis past the capping face (0 < over < 1, default
+ * 3e-5). */
+int pt_debug_face_params(int32_t method, float skip, float over);
 int pt_debug_accel(const pt_fields *f, int64_t n, const double params[17],
                    const double *d_vec, double *d_acc, void *stream);
 

@@ -124,7 +124,7 @@ def load():
     L.pt_integrate_device_noalloc.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.pt_initial_state.argtypes = [i32, i64, i32, C.c_uint64, i64, vp, vp, vp]
     L.pt_moments.argtypes = [i64, vp, i64, vp, vp]
-    L.pt_debug_face_params.argtypes = [C.c_float, C.c_float]
+    L.pt_debug_face_params.argtypes = [i32, C.c_float, C.c_float]
     L.pt_mlp_nparam.restype = i32
     L.pt_mlp_create.argtypes = [vp, vp, C.c_float, C.POINTER(vp)]
     L.pt_mlp_destroy.argtypes = [vp]

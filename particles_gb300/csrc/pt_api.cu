@@ -102,13 +102,17 @@ void unpack_params(const double *p, const RunShape &g, PtRun &R)
     R.qomf = (float)R.qom;
 }
 
-/* Face-cap constants (PT_CTL_FACE); pt_debug_face_params sets them.  Tuned
- * on the mixed-precision workload (RK5, rtol 1e-8, 512^3, FP32): crossing
- * faces within the first 10 % of the step and ending steps 3e-5 cells past
- * the capping face gave 1.64x the simulated time per second of the classical
- * controller (skip 0.05 / 0.15: 1.52x / 1.60x; overshoot 1e-2 / 1e-3 / 1e-4:
- * 1.09x / 1.46x / 1.62x). */
-static float g_face_skip = 0.1f, g_face_over = 3.0e-5f;
+/* Face-cap constants (PT_CTL_FACE) per method [RK5, DOP853]: faces reached
+ * within skip x the proposed step are crossed; steps end `over` cells of the
+ * fastest axis past the capping face.  pt_debug_face_params sets them.
+ * Tuned on the benchmark workloads (FMA / FP32 builds), simulated time per
+ * second relative to the same build without the cap:
+ *   RK5 (rtol 1e-8, 512^3): skip 0.05 / 0.1 / 0.15 -> 1.52x / 1.62x / 1.60x;
+ *     overshoot 1e-2 / 1e-3 / 1e-4 / 3e-5 at skip 0.1 -> 1.09x / 1.46x /
+ *     1.62x / 1.63x;
+ *   DOP853 (rtol 1e-10, 256^3): skip 0 / 0.005 / 0.01 / 0.02 / 0.1 / 0.3
+ *     -> 2.91x / 3.50x / 3.43x / 3.32x / 2.86x / 2.24x at overshoot 3e-5. */
+static float g_face_skip[2] = { 0.1f, 0.01f }, g_face_over[2] = { 3.0e-5f, 3.0e-5f };
 
 int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
                        const double *params, const pt_options *opt, PtRun &R)
@@ -169,8 +173,8 @@ int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
         R.mlp = (opt->controller & PT_CTL_LEARNED)
                     ? pt_mlp_blob(static_cast<const pt_mlp *>(opt->model)) : nullptr;
         R.face = (opt->controller & PT_CTL_FACE) ? 1 : 0;
-        R.face_skip = g_face_skip;
-        R.face_over = g_face_over;
+        R.face_skip = g_face_skip[method == PT_METHOD_DOP853];
+        R.face_over = g_face_over[method == PT_METHOD_DOP853];
         R.rec = static_cast<float *>(opt->records);
         R.rec_cap = opt->record_capacity;
         R.order = opt->order;
@@ -514,11 +518,13 @@ extern "C" int pt_debug_accel(const pt_fields *f, int64_t n, const double params
 }
 
 
-extern "C" int pt_debug_face_params(float skip, float over)
+extern "C" int pt_debug_face_params(int32_t method, float skip, float over)
 {
+    if (method != PT_METHOD_RK5 && method != PT_METHOD_DOP853)
+        return set_err(PT_ERR_ARG, "pt_debug_face_params: unknown method%s");
     if (!(skip >= 0.0f && skip < 1.0f) || !(over > 0.0f && over < 1.0f))
         return set_err(PT_ERR_ARG, "pt_debug_face_params: skip in [0, 1), over in (0, 1)%s");
-    g_face_skip = skip;
-    g_face_over = over;
+    g_face_skip[method == PT_METHOD_DOP853] = skip;
+    g_face_over[method == PT_METHOD_DOP853] = over;
     return PT_OK;
 }

@@ -175,8 +175,10 @@ def test_face_controller_checked_on_host(native):
 
 def test_face_params_checked_on_host(native):
     from particles_gb300 import _native as N
-    assert native.pt_debug_face_params(-0.1, 1e-4) == N.PT_ERR_ARG
-    assert native.pt_debug_face_params(1.0, 1e-4) == N.PT_ERR_ARG
-    assert native.pt_debug_face_params(0.1, 0.0) == N.PT_ERR_ARG
-    assert native.pt_debug_face_params(0.1, 1.0) == N.PT_ERR_ARG
-    assert native.pt_debug_face_params(0.1, 3e-5) == N.PT_OK          # the defaults
+    assert native.pt_debug_face_params(3, 0.1, 1e-4) == N.PT_ERR_ARG
+    assert native.pt_debug_face_params(1, -0.1, 1e-4) == N.PT_ERR_ARG
+    assert native.pt_debug_face_params(1, 1.0, 1e-4) == N.PT_ERR_ARG
+    assert native.pt_debug_face_params(2, 0.1, 0.0) == N.PT_ERR_ARG
+    assert native.pt_debug_face_params(2, 0.1, 1.0) == N.PT_ERR_ARG
+    assert native.pt_debug_face_params(1, 0.1, 3e-5) == N.PT_OK        # the defaults
+    assert native.pt_debug_face_params(2, 0.01, 3e-5) == N.PT_OK
