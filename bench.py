@@ -124,6 +124,8 @@ def parse():
                     help="keep the natural queue order (default: longest first)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble leg")
     ap.add_argument("--ensemble-precision", choices=["fp64", "fp64_fma", "fp32"], default="fp64")
+    ap.add_argument("--no-face-ensemble", action="store_true",
+                    help="skip the ensemble's FMA + face-capped-steps variant")
     ap.add_argument("--no-autotune", action="store_true",
                     help="launch every kernel in its default variant (3 blocks per SM)")
     ap.add_argument("--records", type=int, default=10_000_000)
@@ -652,7 +654,7 @@ def ensemble_leg(args, dev, stream):
     counts[-1] = tot - sum(counts[:-1])
     tmax = cfg["periods"] * T0
     tg = params.time_grid(cfg["periods"], tmax)
-    members, keep = [], []
+    members, keep, fma_fields, s0s = [], [], [], []
     for k in range(3):
         prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=tmax, atol=cfg["tol"][k],
                                  rtol=cfg["tol"][k], facmin=0.333, facmax=6.0, safe=0.9, beta=0.0)
@@ -660,10 +662,13 @@ def ensemble_leg(args, dev, stream):
                                  vunit=VUN, spectrum=cfg["spectrum"], nmin=1.0, nmax=cfg["nmax"],
                                  seed=cfg["seed"][k], backend="torch")
         f = Fields(uu, bb, precision=prec, stream=stream.cuda_stream)
+        if not args.no_face_ensemble:
+            fma_fields.append(Fields(uu, bb, precision="fp64_fma", stream=stream.cuda_stream))
         del uu, bb
         torch.cuda.empty_cache()
         n = counts[k]
         s0 = initial.isotropic_state(n, cfg["seed"][k], gamma_range=cfg["gamma"])
+        s0s.append(s0)
         st = torch.zeros((n, tg.size, 8), dtype=torch.float64, device=dev)
         st[:, 0, :6] = torch.tensor(s0, device=dev)
         members.append(dict(fields=f, params=prm, open_x=True,
@@ -765,6 +770,44 @@ def ensemble_leg(args, dev, stream):
     ens.close()
     for f in keep:
         f.close()
+    if fma_fields:
+        # the same ensemble with the FMA build and face-capped trial steps, from
+        # the same initial states: warm-up and timed windows as launches
+        fm = [dict(mb, fields=fma_fields[k],
+                   state=torch.zeros_like(mb["state"]), cnt=torch.zeros_like(mb["cnt"]),
+                   status=torch.zeros_like(mb["status"]), carry=torch.zeros_like(mb["carry"]))
+              for k, mb in enumerate(members)]
+        for k, mb in enumerate(fm):
+            mb["state"][:, 0, :6] = torch.tensor(s0s[k], device=dev)
+        del members
+        torch.cuda.empty_cache()
+        ef = Ensemble(cfg["method"], fm, precision="fp64_fma", face_steps=True)
+        tf = 0.0
+        for _ in range(args.warmup):
+            tf += win
+            ef.run(tf, stream=stream.cuda_stream)
+        stream.synchronize()
+        a0 = sum(int(m["cnt"][:, 1].sum()) for m in fm)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            tf += win
+            ef.run(tf, stream=stream.cuda_stream)
+        e1.record(stream)
+        stream.synchronize()
+        sec = e0.elapsed_time(e1) * 1e-3
+        c = sum(m["cnt"].sum(0).cpu().numpy() for m in fm)
+        out["fma_face"] = {"accepted_steps_per_s": (int(c[1]) - a0) / sec,
+                           "ms_per_step": 1e3 * sec / args.steps,
+                           "over_exact_launches": (int(c[1]) - a0) / sec
+                           / res["launches"]["accepted_steps_per_s"],
+                           "simulated_time_per_s_over_exact_launches":
+                           res["launches"]["ms_per_step"] / (1e3 * sec / args.steps),
+                           "rejected_fraction": float(c[2] / max(c[0], 1)),
+                           "check": int(ef.check())}
+        ef.close()
+        for f in fma_fields:
+            f.close()
     return out
 
 
