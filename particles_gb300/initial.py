@@ -130,10 +130,6 @@ def moments(a: np.ndarray) -> np.ndarray:
 
 # ---- on the device (pt_initial_state / pt_moments) --------------------------
 
-def _stream_ptr(stream):
-    return None if stream is None else int(stream)
-
-
 def state_on_device(state, seed: int, *, kind: str = "gamma", speed: float | None = None,
                     gamma_range: tuple[float, float] | None = None, vth: float | None = None,
                     domain_min=(0.0, 0.0, 0.0), domain_max=(1.0, 1.0, 1.0), index0: int = 0,
@@ -142,9 +138,10 @@ def state_on_device(state, seed: int, *, kind: str = "gamma", speed: float | Non
     the device: the same draws as `isotropic_state` (kind "speed" or "gamma")
     or `maxwellian_state` (kind "maxwellian"), for particles index0 ..
     index0 + np - 1 of the seeded set.  Launches on `stream` (a CUDA stream
-    handle; default stream if None) without synchronising."""
+    handle; torch's current stream if None) without synchronising."""
     import ctypes as C
     from . import _native as N
+    from .integrations import _stream
     if state.dtype.itemsize != 8 or state.dim() != 3 or state.shape[2] != 8 or not state.is_cuda:
         raise ValueError("state must be a CUDA float64 tensor of shape (np, m, 8)")
     if not state.is_contiguous():
@@ -162,7 +159,7 @@ def state_on_device(state, seed: int, *, kind: str = "gamma", speed: float | Non
     L = N.load()
     N.check(L.pt_initial_state(k, state.shape[0], state.shape[1], C.c_uint64(seed), index0,
                                p.ctypes.data_as(C.c_void_p), C.c_void_p(state.data_ptr()),
-                               C.c_void_p(_stream_ptr(stream))), "pt_initial_state")
+                               _stream(stream, state)), "pt_initial_state")
     return state
 
 
@@ -172,6 +169,7 @@ def moments_on_device(x, stream=None) -> np.ndarray:
     with deterministic compensated sums.  Synchronises the stream."""
     import ctypes as C
     from . import _native as N
+    from .integrations import _stream
     if x.dtype.itemsize != 8 or not x.is_cuda or x.dim() != 1 or x.numel() < 1:
         raise ValueError("x must be a non-empty 1-D CUDA float64 tensor")
     if x.stride(0) < 1:
@@ -179,6 +177,6 @@ def moments_on_device(x, stream=None) -> np.ndarray:
     out = np.zeros(4)
     L = N.load()
     N.check(L.pt_moments(x.numel(), C.c_void_p(x.data_ptr()), x.stride(0),
-                         out.ctypes.data_as(C.c_void_p), C.c_void_p(_stream_ptr(stream))),
+                         out.ctypes.data_as(C.c_void_p), _stream(stream, x)),
             "pt_moments")
     return out

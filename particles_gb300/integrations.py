@@ -28,6 +28,20 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
 
 
+def _stream(stream, tensor=None):
+    """The CUDA stream a launch goes to: `stream` when given (a handle), else
+    torch's current stream on the tensor's device, so that the launch is
+    ordered after the torch work that produced the tensor (and torch's
+    allocator reuses its blocks only after the launch)."""
+    if stream:
+        return C.c_void_p(int(stream))
+    if tensor is not None and getattr(tensor, "is_cuda", False):
+        import torch
+        h = torch.cuda.current_stream(tensor.device).cuda_stream
+        return C.c_void_p(h) if h else None
+    return None
+
+
 def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
@@ -130,7 +144,7 @@ class Fields:
             rc = self._L.pt_fields_create_device(
                 _ptr(dm), C.c_void_p(uu.data_ptr()), C.c_void_p(bb.data_ptr()),
                 C.c_void_p(jj.data_ptr()) if jj is not None else None, prec,
-                C.c_void_p(stream) if stream else None, C.byref(self._h))
+                _stream(stream, uu), C.byref(self._h))
         N.check(rc, "pt_fields_create")
 
     @property
@@ -194,7 +208,7 @@ class Fields:
             C.c_void_p(d_cnt.data_ptr()),
             C.c_void_p(d_status.data_ptr()) if d_status is not None else None,
             C.c_void_p(d_carry.data_ptr()) if d_carry is not None else None,
-            C.byref(opt), C.c_void_p(stream) if stream else None)
+            C.byref(opt), _stream(stream, d_state))
         N.check(rc, "pt_run_device")
 
     def autotune(self, method, params, d_time, d_state, *, eta=0.0, open_x=False, max_steps=0,
@@ -214,7 +228,7 @@ class Fields:
         ms = np.zeros(3, np.float64)
         rc = self._L.pt_autotune(method_id(method), npart, m, self._h, _ptr(_f64(params)),
                                  C.c_void_p(d_time.data_ptr()), C.c_void_p(d_state.data_ptr()),
-                                 C.byref(opt), int(sample), C.c_void_p(stream) if stream else None,
+                                 C.byref(opt), int(sample), _stream(stream, d_state),
                                  C.byref(chosen), _ptr(ms))
         N.check(rc, "pt_autotune")
         return int(chosen.value), {2 + i: float(ms[i]) for i in range(3)}
@@ -241,6 +255,7 @@ class Ensemble:
         self._h = C.c_void_p()
         self.n = len(members)
         self._keep = []
+        self._t0 = members[0]["state"]             # device of the launches' default stream
         arr = (N.PtMember * self.n)()
         for k, mb in enumerate(members):
             prm = _f64(mb["params"])
@@ -262,16 +277,16 @@ class Ensemble:
 
     def run(self, t_stop, stream=0):
         """One window up to t_stop (0 = to each member's tmax); no synchronisation."""
-        N.check(self._L.pt_ensemble_run(self._h, float(t_stop), C.c_void_p(stream) if stream else None),
+        N.check(self._L.pt_ensemble_run(self._h, float(t_stop), _stream(stream, self._t0)),
                 "pt_ensemble_run")
 
     def capture(self, windows, dt_window, stream=0):
         N.check(self._L.pt_ensemble_capture(self._h, int(windows), float(dt_window),
-                                            C.c_void_p(stream) if stream else None),
+                                            _stream(stream, self._t0)),
                 "pt_ensemble_capture")
 
     def replay(self, stream=0):
-        N.check(self._L.pt_ensemble_replay(self._h, C.c_void_p(stream) if stream else None),
+        N.check(self._L.pt_ensemble_replay(self._h, _stream(stream, self._t0)),
                 "pt_ensemble_replay")
 
     def counts(self):

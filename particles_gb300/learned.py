@@ -21,6 +21,7 @@ import ctypes as C
 import numpy as np
 
 from . import _native as N
+from .integrations import _stream
 
 FEATURES = ["log|B|", "log|E|", "log gamma", "pitch cosine", "log(|grad B|/|B|)",
             "log(Omega dt_prev)", "log(err_prev)", "log dt_prev"]
@@ -94,6 +95,7 @@ def train(torch, X: np.ndarray, T: np.ndarray, norm: np.ndarray, *, epochs: int 
     v = torch.zeros_like(p)
     loss = torch.zeros(1, dtype=torch.float32, device=device)
     gen = torch.Generator(device="cpu").manual_seed(seed)
+    st = _stream(None, p)            # the kernels follow the torch work on the same stream
     n = dX.shape[0]
     step, hist = 0, []
     for ep in range(epochs):
@@ -103,10 +105,10 @@ def train(torch, X: np.ndarray, T: np.ndarray, norm: np.ndarray, *, epochs: int 
             idx = perm[s:s + batch]
             xb = dX[idx].contiguous()
             tb = dT[idx].contiguous()
-            N.check(L.pt_mlp_loss_grad(vp(p), vp(xb), vp(tb), batch, vp(g), vp(loss), None),
+            N.check(L.pt_mlp_loss_grad(vp(p), vp(xb), vp(tb), batch, vp(g), vp(loss), st),
                     "pt_mlp_loss_grad")
             step += 1
-            N.check(L.pt_mlp_adam(vp(p), vp(g), vp(m), vp(v), step, lr, 0.9, 0.999, 1e-8, None),
+            N.check(L.pt_mlp_adam(vp(p), vp(g), vp(m), vp(v), step, lr, 0.9, 0.999, 1e-8, st),
                     "pt_mlp_adam")
             tot += float(loss.item())
             nb += 1
@@ -137,7 +139,7 @@ class Model:
         dX = torch.tensor(np.ascontiguousarray(X, np.float32), device="cuda")
         out = torch.empty(dX.shape[0], dtype=torch.float32, device="cuda")
         N.check(self._L.pt_mlp_infer(self._h, C.c_void_p(dX.data_ptr()), dX.shape[0],
-                                     C.c_void_p(out.data_ptr()), None), "pt_mlp_infer")
+                                     C.c_void_p(out.data_ptr()), _stream(None, dX)), "pt_mlp_infer")
         torch.cuda.synchronize()
         return out.cpu().numpy()
 

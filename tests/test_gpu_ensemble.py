@@ -85,6 +85,7 @@ def test_ensemble_graph_replay_equals_stepwise(cuda, precision):
         probs, members = _members(torch, precision, "rk5")
         ens = Ensemble("rk5", members, precision=precision)
         stream = torch.cuda.Stream()
+        stream.wait_stream(torch.cuda.current_stream())   # the members' tensors are ready
         if use_graph:
             ens.capture(4, 0.25 * T0, stream=stream.cuda_stream)
             ens.replay(stream=stream.cuda_stream)
@@ -119,6 +120,7 @@ def test_output_stream_rows_match_final_state(cuda):
     carry = torch.zeros(int(f._L.pt_carry_bytes(npart)), dtype=torch.uint8, device="cuda")
     d_time = torch.tensor(prob["time"], device="cuda")
     stream = torch.cuda.Stream()
+    stream.wait_stream(torch.cuda.current_stream())       # the tensors above are ready
     out = OutputStream(torch, st, prob["time"])
     tmax = prob["time"][-1]
     streamed = 0
