@@ -84,8 +84,9 @@ WORKLOADS = {
 LEARNED_SAFETY = 0.75
 
 # Variants of the mixed-precision leg: (name, field precision).  "_learned":
-# the learned controller proposes trial steps; "_face": trial steps end just
-# past the next cell face (PT_CTL_FACE).
+# the learned controller proposes trial steps (trained on records of the
+# exact classical run; with "_face", on records of the FP32 face-capped run);
+# "_face": trial steps end just past the next cell face (PT_CTL_FACE).
 MIXED_VARIANTS = (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"), ("bf16", "bf16"),
                   ("fp32_learned", "fp32"), ("bf16_learned", "bf16"), ("fp64_fma_face", "fp64_fma"),
                   ("fp32_face", "fp32"), ("bf16_face", "bf16"), ("fp32_learned_face", "fp32"),
@@ -526,11 +527,11 @@ def mixed_leg(args, dev, stream):
 
     from particles_gb300 import learned as LRN
     rates = {}
-    model = None
+    model = model_face = None
     for name, prec in MIXED_VARIANTS:
         f = handles[prec]
-        mdl = model if "_learned" in name else None
         face = name.endswith("_face")
+        mdl = (model_face if face else model) if "_learned" in name else None
         st, cnt, status, carry = fresh(npart)
         launch = tune(args, f, "rk5", prm, d_time, st, stream, window * T0, model=mdl,
                       face_steps=face)
@@ -577,6 +578,22 @@ def mixed_leg(args, dev, stream):
             model = LRN.Model(params_mlp, norm, safety=LEARNED_SAFETY)
             out["learned_training"] = {"records": int(X.shape[0]), "mse_per_epoch": hist}
             del rec
+        if name == "fp32_face":
+            # the face-capped controller's accepted steps train the network the
+            # "_learned_face" variants use (steps that end just past a face)
+            rec = LRN.record_buffer(torch, min(args.records, 4_000_000))
+            w += 1
+            f.run_device("rk5", prm, d_time, st, cnt, status, carry, t_stop=w * window * T0,
+                         time_budget_s=900.0, stream=stream.cuda_stream, records=rec,
+                         face_steps=True)
+            stream.synchronize()
+            X, T = LRN.dataset(LRN.records_from_buffer(rec), "rk5")
+            norm = LRN.normalisation(X, T)
+            params_mlp, hist = LRN.train(torch, X, T, norm, epochs=2, batch=16384, lr=2e-3)
+            model_face = LRN.Model(params_mlp, norm, safety=LEARNED_SAFETY)
+            out["learned_face_training"] = {"records": int(X.shape[0]), "mse_per_epoch": hist,
+                                            "recorded_in": "a window of the FP32 face-capped run"}
+            del rec
         del st, cnt, status, carry
         torch.cuda.empty_cache()
     out["accepted_steps_per_s"] = {k: v["value"] for k, v in rates.items()}
@@ -605,8 +622,8 @@ def mixed_leg(args, dev, stream):
     res = {}
     w_ref = cfg["periods"]
     for name, prec in MIXED_VARIANTS:
-        mdl = model if "_learned" in name else None
         face = name.endswith("_face")
+        mdl = (model_face if face else model) if "_learned" in name else None
         st, cnt, status, carry = fresh(na)
         t_start = time.perf_counter()
         w = 0
@@ -630,8 +647,9 @@ def mixed_leg(args, dev, stream):
         rep["reference"] = "exact FP64 kernel (bit-identical to the CPU oracle)"
         rep["particles"] = na
         out["accuracy"][prec] = rep
-    if model is not None:
-        model.close()
+    for mo in (model, model_face):
+        if mo is not None:
+            mo.close()
     for f in handles.values():
         f.close()
     return out
