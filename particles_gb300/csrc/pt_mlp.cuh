@@ -21,8 +21,9 @@
  * each block): B fragments pre-arranged per (k-tile, n-tile, lane) as uint2,
  * then FP32 b1[64], b2[64], b3[4], the feature means mu[8] and inverse
  * standard deviations isd[8].  Features are standardised in FP32 before the
- * FP16 conversion; the target scaling and the safety factor are folded into
- * W3 and b3 when the blob is built.
+ * FP16 conversion; W1, b1, W2, b2 are stored halved (see pt_silu_h2), and
+ * the target scaling and the safety factor are folded into W3 and b3 when
+ * the blob is built.
  */
 #ifndef PT_MLP_CUH
 #define PT_MLP_CUH
@@ -61,20 +62,18 @@ __device__ __forceinline__ void pt_mma16816(float c[4], const uint32_t a[4], uin
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b.x), "r"(b.y));
 }
 
-__device__ __forceinline__ float pt_silu(float z) { return z / (1.0f + __expf(-z)); }
 
-/* SiLU of two accumulators, packed as the next layer's FP16 pair:
- * silu(z) = z (1/2 + tanh(z/2)/2), with the one-instruction tanh.approx.f16x2
- * (absolute error ~1e-3, below the FP16 operand rounding of the next layer). */
-__device__ __forceinline__ uint32_t pt_silu_h2(float z0, float z1)
+/* SiLU of two accumulators, packed as the next layer's FP16 pair.  The
+ * blob's layers 1 and 2 carry a factor 1/2, so the accumulators hold
+ * h = z / 2 and silu(z) = z (1 + tanh(z/2)) / 2 = h + h tanh(h): a pack,
+ * the one-instruction tanh.approx.f16x2 (absolute error ~1e-3, below the
+ * FP16 operand rounding of the next layer) and one half2 FMA. */
+__device__ __forceinline__ uint32_t pt_silu_h2(float h0, float h1)
 {
-    const __half2 z = __floats2half2_rn(z0, z1);
-    const __half2 half = __float2half2_rn(0.5f);
-    const __half2 h = __hmul2(z, half);
+    const __half2 h = __floats2half2_rn(h0, h1);
     uint32_t t;
     asm("tanh.approx.f16x2 %0, %1;" : "=r"(t) : "r"(*reinterpret_cast<const uint32_t *>(&h)));
-    const __half2 sg = __hfma2(*reinterpret_cast<const __half2 *>(&t), half, half);
-    const __half2 y = __hmul2(z, sg);
+    const __half2 y = __hfma2(h, *reinterpret_cast<const __half2 *>(&t), h);
     return *reinterpret_cast<const uint32_t *>(&y);
 }
 

@@ -240,15 +240,16 @@ extern "C" int pt_mlp_create(const float *params, const float norm[18], float sa
     for (int nt = 0; nt < 8; ++nt)
         for (int lane = 0; lane < 32; ++lane) {
             const int g = lane >> 2, q = lane & 3, nn = 8 * nt + g;
-            frag[2 * (PT_MLP_FRAG_W1 + nt * 32 + lane)] = h2bits(W1[(2 * q) * NH + nn], W1[(2 * q + 1) * NH + nn]);
+            frag[2 * (PT_MLP_FRAG_W1 + nt * 32 + lane)] =
+                h2bits(0.5f * W1[(2 * q) * NH + nn], 0.5f * W1[(2 * q + 1) * NH + nn]);
         }
     for (int kt = 0; kt < 4; ++kt)
         for (int nt = 0; nt < 8; ++nt)
             for (int lane = 0; lane < 32; ++lane) {
                 const int g = lane >> 2, q = lane & 3, nn = 8 * nt + g, k0 = 16 * kt + 2 * q;
                 const int f = PT_MLP_FRAG_W2 + (kt * 8 + nt) * 32 + lane;
-                frag[2 * f] = h2bits(W2[k0 * NH + nn], W2[(k0 + 1) * NH + nn]);
-                frag[2 * f + 1] = h2bits(W2[(k0 + 8) * NH + nn], W2[(k0 + 9) * NH + nn]);
+                frag[2 * f] = h2bits(0.5f * W2[k0 * NH + nn], 0.5f * W2[(k0 + 1) * NH + nn]);
+                frag[2 * f + 1] = h2bits(0.5f * W2[(k0 + 8) * NH + nn], 0.5f * W2[(k0 + 9) * NH + nn]);
             }
     for (int kt = 0; kt < 4; ++kt)
         for (int lane = 0; lane < 32; ++lane) {
@@ -260,7 +261,9 @@ extern "C" int pt_mlp_create(const float *params, const float norm[18], float sa
             }
         }
     std::vector<float> tail(PT_MLP_BLOB_FLOATS, 0.0f);
-    for (int j = 0; j < 64; ++j) { tail[j] = b1[j]; tail[64 + j] = b2[j]; }
+    /* layers 1 and 2 carry a factor 1/2 (exact in FP16/FP32): the inference
+     * takes their accumulators as h = z / 2, and silu(z) = h + h tanh(h) */
+    for (int j = 0; j < 64; ++j) { tail[j] = 0.5f * b1[j]; tail[64 + j] = 0.5f * b2[j]; }
     tail[128] = b3 * ysd + ymu + logf(safety);
     for (int i = 0; i < 8; ++i) {
         tail[132 + i] = mu[i];
