@@ -90,3 +90,13 @@ def test_field_generator_is_solenoidal_and_scaled():
     uu2, bb2, _ = fields.snapshot(n, db_rms=0.5, v_rms=0.1, vunit=0.05, spectrum="kolmogorov",
                                   nmin=1, nmax=8, seed=11, with_j=True)
     assert np.array_equal(bb, bb2) and np.array_equal(uu, uu2)
+
+
+def test_launch_stream_selection():
+    """An explicit stream handle wins; without one, host arrays launch on the
+    default stream (None) and CUDA tensors on torch's current stream."""
+    import ctypes as C
+    from particles_gb300.integrations import _stream
+    assert _stream(None) is None and _stream(0) is None
+    assert _stream(1234).value == 1234
+    assert _stream(None, np.zeros(3)) is None
