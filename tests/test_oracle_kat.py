@@ -328,3 +328,39 @@ def test_near_gather_option(oracle_lib):
     b = oracle.integrate("rk5", prob["params"], prob["time"], uu, bb, prob["state"].copy(), near=True)
     assert not np.array_equal(a[0], b[0])
     assert (b[2] == 0).all() and np.isfinite(b[0]).all()
+
+
+def _gyration_rows(method, nper_step, nrows=5):
+    """Fixed steps (dtmax pins dt) in a uniform field, samples between step
+    ends: the rows come from the dense output.  Returns the largest row error
+    against the analytic helix."""
+    speed = 0.5
+    u = speed / math.sqrt(1.0 - speed ** 2)
+    gam = math.sqrt(1.0 + 0.1 ** 2 + u ** 2)
+    period = 2 * math.pi * gam / QOM
+    dt = period / nper_step
+    prm = params.pack_params(qom=QOM, vunit=VUN, tmax=period, dtmax=dt, atol=1.0, rtol=1.0)
+    tg = params.time_grid(nrows, period)
+    uu, bb = fields.uniform_field(4, b=(1.0, 0.0, 0.0))
+    st = np.zeros((1, tg.size, 8))
+    st[0, 0, :6] = [0.3, 0.4, 0.5, 0.1, u * 0.6, u * 0.8]
+    s, c, status = oracle.integrate(method, prm, tg, uu, bb, st)
+    om, ph0 = QOM / gam, math.atan2(0.8, 0.6)
+    err = 0.0
+    for n in range(1, tg.size - 1):                    # interior rows: between step ends
+        tt = tg[n]
+        uy, uz = u * math.cos(ph0 - om * tt), u * math.sin(ph0 - om * tt)
+        err = max(err, abs(s[0, n, 4] - uy), abs(s[0, n, 5] - uz))
+    return err
+
+
+@pytest.mark.parametrize("method,order", [("rk5", 2), ("dop853", 4)])
+def test_dense_output_order(method, order):
+    """Output rows are cubic Hermite interpolants of the step
+    (integrations.F90:158-168, :447-457).  DOP853 uses f at both step ends,
+    so its rows converge as h^4; RK5 takes the end slope from the stage-6
+    state (f at t + 7h/8, not at t + h), so its rows converge only as h^2 --
+    far below the integrator's own 5th order."""
+    e1, e2 = _gyration_rows(method, 48), _gyration_rows(method, 96)
+    ratio = e1 / e2
+    assert 2 ** (order - 0.5) < ratio < 2 ** (order + 0.7), (e1, e2, ratio)
