@@ -81,6 +81,23 @@ def test_fused_exact_bitwise(cuda, oracle_lib, method):
     assert (sto == 0).all()
 
 
+def test_dop853_pi_controller_bitwise(cuda, oracle_lib):
+    """beta != 0 turns on the PI part of the DOP853 controller
+    (integrations.F90:466-476): expo = 1/8 - 0.75 beta and errold^beta, both
+    through the deterministic pow (no Newton-root shortcut for these
+    exponents), with facmin/facmax/safe away from the defaults."""
+    from particles_gb300 import params
+    prob = small_problem("dop853", n=16, npart=96, periods=2.0, seed=41)
+    T0 = 2.0 * np.pi / 200.0
+    prob["params"] = params.pack_params(qom=200.0, vunit=0.05, tmax=2 * T0, dtmax=2 * T0,
+                                        atol=1e-10, rtol=1e-10, facmin=0.2, facmax=10.0,
+                                        safe=0.85, beta=0.04)
+    (so, co, sto), (sg, cg, stg) = _run_both(prob)
+    assert (sto == 0).all()
+    assert np.array_equal(co, cg) and np.array_equal(sto, stg)
+    assert np.array_equal(so.view(np.int64), sg.view(np.int64))
+
+
 @pytest.mark.parametrize("method", ["rk5", "dop853"])
 def test_fused_fma_uniform_field_close(cuda, oracle_lib, method):
     """FMA contraction changes rounding only.  In a uniform field (gyration
@@ -232,3 +249,22 @@ def test_integer_pipe_floor_and_indices(cuda):
     assert np.array_equal(o[~nan, 0].view(np.int64), o[~nan, 1].view(np.int64))  # floor, -0.0 too
     assert np.array_equal(o[:, 2], o[:, 3])                                   # int32 conversion
     assert np.array_equal(i[:, 0], i[:, 1])                                   # node index
+
+
+@pytest.mark.parametrize("method", ["rk5", "dop853"])
+@pytest.mark.parametrize("npart,nsteps", [(1, 0), (1, 3), (37, 0), (37, 5), (0, 3)])
+def test_tiny_and_ragged_batches_bitwise(cuda, oracle_lib, method, npart, nsteps):
+    """One particle, a batch that is not a multiple of the warp, an empty
+    batch, and m = 1 (only the initial row is an output: the step loop still
+    runs to tmax and counts its steps, integrations.F90:129-197) all match
+    the oracle bit for bit."""
+    prob = small_problem(method, n=16, npart=max(npart, 1), periods=1.0, seed=43, nsteps=nsteps)
+    if nsteps == 0:
+        prob["time"] = prob["time"][:1]
+        prob["state"] = np.ascontiguousarray(prob["state"][:, :1])
+    if npart == 0:
+        prob["state"] = np.ascontiguousarray(prob["state"][:0])
+    (so, co, sto), (sg, cg, stg) = _run_both(prob)
+    assert sg.shape == so.shape
+    assert np.array_equal(co, cg) and np.array_equal(sto, stg)
+    assert np.array_equal(so.view(np.int64), sg.view(np.int64))
