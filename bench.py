@@ -1149,6 +1149,26 @@ def main():
         del d_state, d_cnt, d_status, d_carry
         torch.cuda.empty_cache()
         line["mixed"] = mixed_leg(args, dev, stream)
+    if "mixed" in line:
+        # the headline ratios in one place: mixed precision with the learned
+        # controller against the plain exact kernel, and their accuracy
+        mx = line["mixed"]
+        acc1 = {k: v["rows"]["1"] for k, v in mx.get("accuracy", {}).items() if "1" in v["rows"]}
+        line["targets"] = {
+            "plain_roofline_frac_of_fma_peak": roof["frac"],
+            "plain_roofline_frac_of_no_fma_peak": roof["frac_of_no_fma_peak"],
+            "mixed_learned_accepted_over_plain": {
+                k: mx["over_plain_exact"][k] for k in ("bf16_learned", "bf16_learned_face")},
+            "mixed_learned_simulated_time_over_plain": {
+                k: mx["physics_rate_over_plain_exact"][k]
+                for k in ("bf16_learned", "bf16_learned_face")},
+            "energy_rel_err_median_at_1_gyroperiod": {
+                k: acc1[k]["energy_rel_err_median"] for k in ("bf16_learned", "bf16_learned_face")
+                if k in acc1},
+            "fraction_energy_err_le_1e-6_at_1_gyroperiod": {
+                k: acc1[k]["fraction_energy_err_le_1e-6"]
+                for k in ("bf16_learned", "bf16_learned_face") if k in acc1},
+        }
     if not args.no_learned and "learned" in legs and rank == 0 and args.workload == "dop853-256":
         torch.cuda.empty_cache()
         line["learned"] = learned_leg(args, dev, stream)
