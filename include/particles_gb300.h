@@ -370,6 +370,12 @@ int pt_debug_intpipe(int64_t n, const double *d_x, int32_t d, double *d_out, int
  * cells of the fastest axis past the capping face (0 < over < 1, default
  * 3e-5). */
 int pt_debug_face_params(int32_t method, float skip, float over);
+/* The PT_CTL_FACE cap of `method` for n device states d_si (6 doubles each:
+ * x, u) and proposed steps d_h on the grid and domain of f / params:
+ * d_out[i] = min(h, time to the first cell face after skip x h along the
+ * straight path + overshoot). */
+int pt_debug_face_cap(const pt_fields *f, int32_t method, int64_t n, const double params[17],
+                      const double *d_si, const double *d_h, double *d_out, void *stream);
 int pt_debug_accel(const pt_fields *f, int64_t n, const double params[17],
                    const double *d_vec, double *d_acc, void *stream);
 

@@ -33,7 +33,7 @@ EXPORTS = [
     "pt_ensemble_create", "pt_ensemble_destroy", "pt_ensemble_run", "pt_ensemble_capture",
     "pt_ensemble_replay", "pt_ensemble_counts", "pt_ensemble_escaped", "pt_ensemble_check",
     "pt_copy_rows", "pt_debug_ctl_pow", "pt_last_transfer_bytes", "pt_debug_intpipe",
-    "pt_initial_state", "pt_moments", "pt_debug_face_params",
+    "pt_initial_state", "pt_moments", "pt_debug_face_params", "pt_debug_face_cap",
 ]
 
 PT_INIT_SPEED, PT_INIT_GAMMA, PT_INIT_MAXWELLIAN = 0, 1, 2
@@ -125,6 +125,7 @@ def load():
     L.pt_initial_state.argtypes = [i32, i64, i32, C.c_uint64, i64, vp, vp, vp]
     L.pt_moments.argtypes = [i64, vp, i64, vp, vp]
     L.pt_debug_face_params.argtypes = [i32, C.c_float, C.c_float]
+    L.pt_debug_face_cap.argtypes = [vp, i32, i64, vp, vp, vp, vp, vp]
     L.pt_mlp_nparam.restype = i32
     L.pt_mlp_create.argtypes = [vp, vp, C.c_float, C.POINTER(vp)]
     L.pt_mlp_destroy.argtypes = [vp]

@@ -528,3 +528,23 @@ extern "C" int pt_debug_face_params(int32_t method, float skip, float over)
     g_face_over[method == PT_METHOD_DOP853] = over;
     return PT_OK;
 }
+
+extern "C" int pt_debug_face_cap(const pt_fields *f, int32_t method, int64_t n,
+                                 const double params[17], const double *d_si, const double *d_h,
+                                 double *d_out, void *stream)
+{
+    if (!f || !params) return set_err(PT_ERR_ARG, "NULL argument%s");
+    if (method != PT_METHOD_RK5 && method != PT_METHOD_DOP853)
+        return set_err(PT_ERR_ARG, "pt_debug_face_cap: unknown method%s");
+    if (n <= 0) return PT_OK;
+    if (!d_si || !d_h || !d_out) return set_err(PT_ERR_ARG, "NULL buffer%s");
+    PtRun R;
+    RunShape g = shape_of(f);
+    unpack_params(params, g, R);
+    attach_fields(f, R);
+    R.face = 1;
+    R.face_skip = g_face_skip[method == PT_METHOD_DOP853];
+    R.face_over = g_face_over[method == PT_METHOD_DOP853];
+    const cudaError_t e = pt_launch_face_cap(R, n, d_si, d_h, d_out, (cudaStream_t)stream);
+    return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_face_cap");
+}

@@ -241,6 +241,8 @@ cudaError_t pt_launch_debug_pow(int64_t n, const double *x, const double *y, dou
                                 cudaStream_t s);
 cudaError_t pt_launch_ctl_pow(int64_t n, const double *x, const double *y, double *out,
                               cudaStream_t s);
+cudaError_t pt_launch_face_cap(const PtRun &P, int64_t n, const double *si, const double *h,
+                               double *out, cudaStream_t s);
 cudaError_t pt_launch_intpipe(int64_t n, const double *x, int32_t d, double *out, int32_t *idx,
                               cudaStream_t s);
 

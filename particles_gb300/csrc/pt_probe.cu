@@ -13,6 +13,7 @@
 
 #include "pt_common.cuh"
 #include "pt_ctlpow.cuh"
+#include "pt_integrator.cuh"
 
 namespace {
 
@@ -31,6 +32,19 @@ __global__ void k_intpipe(int64_t n, const double *x, int32_t d, double *out, in
         out[4 * i + 3] = (f != f) ? 0.0 : (double)(int32_t)f;
         idx[2 * i] = pt_node_index(f, d);
         idx[2 * i + 1] = (f >= 0.0 && f < (double)d) ? (int32_t)f : 0;
+    }
+}
+
+/* The face cap of PT_CTL_FACE for given states si (6 per row) and proposed
+ * steps h, for its geometry test. */
+__global__ void k_face_cap(const PtRun P, int64_t n, const double *si, const double *h, double *out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        double s[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) s[c] = si[6 * i + c];
+        out[i] = pt_sm::pt_face_cap(P, s, h[i]);
     }
 }
 
@@ -117,5 +131,14 @@ cudaError_t pt_launch_intpipe(int64_t n, const double *x, int32_t d, double *out
     if (n <= 0) return cudaSuccess;
     const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
     k_intpipe<<<grid, 256, 0, s>>>(n, x, d, out, idx);
+    return cudaGetLastError();
+}
+
+cudaError_t pt_launch_face_cap(const PtRun &P, int64_t n, const double *si, const double *h,
+                               double *out, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    k_face_cap<<<grid, 256, 0, s>>>(P, n, si, h, out);
     return cudaGetLastError();
 }

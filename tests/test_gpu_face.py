@@ -101,3 +101,61 @@ def test_exact_precision_rejects_face_steps(cuda):
     with pytest.raises(N.PtError) as ei:
         integrate("rk5", prob["params"], prob["time"], uu, bb, prob["state"].copy(), face_steps=True)
     assert ei.value.code == N.PT_ERR_UNSUPPORTED
+
+
+def _face_cap_np(si, h, dm, lo, hi, vun, skip, over):
+    """The face cap restated in float64: time along the straight path from si
+    to the first cell face reached after skip * h, plus `over` cells of the
+    fastest axis, capped by h.  Also returns skip*h*|w| - d per axis (the
+    argument of the ceiling), to leave out draws that sit on its jumps."""
+    dm, lo, hi = (np.asarray(a, float) for a in (dm, lo, hi))
+    gsx = dm / (hi - lo)
+    xn = (si[:, :3] - lo) * gsx
+    off = xn - np.floor(xn)
+    u = si[:, 3:]
+    w = u / np.sqrt(1.0 + (u * u).sum(1, keepdims=True)) / vun * gsx
+    aw = np.abs(w)
+    d = np.where(w > 0, 1.0 - off, off)
+    arg = (skip * h)[:, None] * aw - d
+    k = np.maximum(0.0, np.ceil(arg))
+    t = np.where(aw > 0, (d + k) / np.where(aw > 0, aw, 1.0), np.inf)
+    cap = t.min(1) + over / aw.max(1)
+    return np.minimum(h, cap), arg, aw.max(1)
+
+
+@pytest.mark.parametrize("method,skip", [("rk5", 0.1), ("dop853", 0.01)])
+def test_face_cap_geometry(cuda, method, skip):
+    """pt_face_cap (FP32 inside) against its float64 restatement on a
+    non-cubic grid with an offset domain, for proposed steps from far below
+    to far above a cell-crossing time."""
+    import ctypes as C
+    torch = cuda
+    from particles_gb300 import Fields, params
+    from particles_gb300 import _native as N
+    from test_gpu_grids import DM, HI, LO, _fields
+    uu, bb, _ = _fields(35)
+    f = Fields(uu, bb, precision="fp32")
+    prm = params.pack_params(qom=200.0, vunit=0.05, tmax=1.0, domain_min=LO, domain_max=HI)
+    rng = np.random.default_rng(6)
+    n = 4096
+    lo, hi = np.array(LO), np.array(HI)
+    si = np.concatenate([lo + (hi - lo) * rng.uniform(0, 1, (n, 3)),
+                         rng.normal(0, 1, (n, 3)) * 10.0 ** rng.uniform(-1, 1, (n, 1))], 1)
+    h = 10.0 ** rng.uniform(-5.5, -1.5, n)
+    d_si, d_h = torch.tensor(si.ravel(), device="cuda"), torch.tensor(h, device="cuda")
+    out = torch.empty_like(d_h)
+    N.check(N.load().pt_debug_face_cap(f.handle, 1 if method == "rk5" else 2, n,
+                                       prm.ctypes.data_as(C.c_void_p), C.c_void_p(d_si.data_ptr()),
+                                       C.c_void_p(d_h.data_ptr()), C.c_void_p(out.data_ptr()), None),
+            "pt_debug_face_cap")
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    ref, arg, wmax = _face_cap_np(si, h, DM, LO, HI, 0.05, skip, 3e-5)
+    clean = (np.abs(arg - np.round(arg)) > 1e-3).all(1)
+    assert clean.mean() > 0.95
+    # FP32 cell offsets resolve ~6e-8 of a cell: allow that much travel time
+    slack = 1e-4 * ref + 2e-7 / wmax
+    assert (np.abs(got - ref)[clean] <= slack[clean]).all(), (np.abs(got - ref) / slack)[clean].max()
+    assert (got <= h).all()
+    assert 0.2 < (got < h).mean() < 0.95            # the cap binds for some draws, not all
+    f.close()
