@@ -364,3 +364,40 @@ def test_dense_output_order(method, order):
     e1, e2 = _gyration_rows(method, 48), _gyration_rows(method, 96)
     ratio = e1 / e2
     assert 2 ** (order - 0.5) < ratio < 2 ** (order + 0.7), (e1, e2, ratio)
+
+
+def test_dti_guess_restated_independently():
+    """dti_guess (integrations.F90:524-589) restated here in plain Python
+    floats, with the force from the oracle: d0, d1 as RMS norms scaled by
+    atol + rtol |si|, dti = 0.1 d0 / d1 (or 1e-6), d2 = max(d1, |sf - si| /
+    dti) with sf = si + dti ki, dtf = (0.01 / d2)^(1/iord) (or the floor),
+    dt = min(100 dti, dtf, dtmax).  Only the power differs in its last bits
+    (libm against the deterministic pow)."""
+    uu, bb = fields.snapshot(8, seed=11)
+    rng = np.random.default_rng(12)
+    for trial in range(40):
+        iord = 5 if trial % 2 else 8
+        tol = 10.0 ** rng.uniform(-12, -4)
+        prm = params.pack_params(qom=QOM, vunit=VUN, tmax=1.0, dtmax=10.0 ** rng.uniform(-5, 0),
+                                 atol=tol, rtol=tol * rng.uniform(0.1, 10))
+        si = np.concatenate([rng.uniform(0, 1, 3), rng.normal(0, 1, 3) * 10.0 ** rng.uniform(-3, 1)])
+        if trial == 0:
+            si[3:] = 0.0                                    # a particle at rest: tiny d1
+        ki = oracle.acceleration(QOM, VUN, uu, bb, si)
+        atol, rtol, dtm = prm[5], prm[6], prm[4]
+        sr = [atol + rtol * abs(float(x)) for x in si]
+        s0 = s1 = s2 = 0.0
+        for i in range(6):
+            s0 = s0 + (float(si[i]) / sr[i]) ** 2
+        for i in range(6):
+            s1 = s1 + (float(ki[i]) / sr[i]) ** 2
+        d0, d1 = math.sqrt(s0 / 6.0), math.sqrt(s1 / 6.0)
+        dti = 1.0e-06 if min(d0, d1) < 1.0e-10 else 1.0e-01 * (d0 / d1)
+        for i in range(6):
+            sf = float(si[i]) + dti * float(ki[i])
+            s2 = s2 + ((sf - float(si[i])) / sr[i]) ** 2
+        d2 = max(d1, math.sqrt(s2 / 6.0) / dti)
+        dtf = max(1.0e-06, 1.0e-03 * dti) if d2 <= 1.0e-15 else (1.0e-02 / d2) ** (1.0 / iord)
+        want = min(min(1.0e+02 * dti, dtf), dtm)
+        got = oracle.dti_guess(iord, prm, uu, bb, si)
+        assert got == pytest.approx(want, rel=4e-16 * 8), (trial, got, want)
