@@ -401,3 +401,103 @@ def test_dti_guess_restated_independently():
         want = min(min(1.0e+02 * dti, dtf), dtm)
         got = oracle.dti_guess(iord, prm, uu, bb, si)
         assert got == pytest.approx(want, rel=4e-16 * 8), (trial, got, want)
+
+
+# Cash-Karp tableau exactly as integrations.F90:86-98 writes it: b(5,5) filled
+# column-major from the literals, every literal divided by the common factor
+_B = np.array([1.10592e+05, 4.14720e+04, 1.65888e+05, -1.12640e+05, 1.63100e+04,
+               0.0, 1.24416e+05, -4.97664e+05, 1.38240e+06, 1.89000e+05,
+               0.0, 0.0, 6.63552e+05, -1.43360e+06, 2.30000e+04,
+               0.0, 0.0, 0.0, 7.16800e+05, 2.21375e+05,
+               0.0, 0.0, 0.0, 0.0, 3.41550e+04]) / 5.5296e+05
+_CKB = _B.reshape(5, 5, order="F")            # _CKB[j-2, i-1] = b(j-1, i)
+_CKC = np.array([9.361e+03, 0.0, 3.85e+04, 2.0125e+04, 0.0, 2.7648e+04]) / 9.5634e+04
+_CKD = np.array([-1.40162e+05, 0.0, 6.094e+05, -1.114925e+06, -6.30729e+05,
+                 1.276416e+06]) / 3.2643072e+07
+
+
+def _rk5_restated(prm, tg, uu, bb, s_init):
+    """integrate_rk5 (integrations.F90:57-200) for one particle, written
+    again from the Fortran text in plain Python floats (the force, the
+    initial step and the power come from the oracle: they have their own
+    tests).  Returns state(8, m) as rows and cnt(3)."""
+    qom, vun, tmx, dtm, atol = prm[0], prm[1], prm[2], prm[4], prm[5]
+    fcmn, fcmx, safe = prm[7], prm[8], prm[9]
+    xl, xs = tuple(prm[11:14]), tuple(prm[14:17])
+    eps = 2.2250738585072014e-308                     # tiny(qom)
+    m = tg.size
+    out = np.zeros((m, 8))
+    cnt = [0, 0, 0]
+    t = 0.0
+    si = [float(v) for v in s_init]
+    dt = oracle.dti_guess(5, prm, uu, bb, np.array(si))
+    n = 1
+    out[0, :6] = si
+    out[0, 6] = math.sqrt((si[3] * si[3] + si[4] * si[4]) + si[5] * si[5] + 1.0)
+    out[0, 7] = dt
+    n = 2
+    while t < tmx:
+        k, s = [], []
+        for j in range(1, 7):
+            sj = list(si)
+            for i in range(1, j):
+                sj = [sj[c] + _CKB[j - 2, i - 1] * k[i - 1][c] for c in range(6)]
+            ac = oracle.acceleration(qom, vun, uu, bb, np.array(sj), xl=xl, xs=xs)
+            s.append(sj)
+            k.append([dt * float(a) for a in ac])
+        sf, er = [], []
+        for i in range(6):
+            a = 0.0
+            e = 0.0
+            for j in range(6):
+                a = a + _CKC[j] * k[j][i]
+                e = e + _CKD[j] * k[j][i]
+            sf.append(si[i] + a)
+            er.append(e)
+        sr = [abs(si[i]) + abs(k[0][i]) + eps for i in range(6)]
+        dl = max(abs(er[i] / sr[i]) for i in range(6)) / atol
+        if dl <= 1.0:
+            t = t + dt
+            ac = oracle.acceleration(qom, vun, uu, bb, np.array(s[5]), xl=xl, xs=xs)
+            k[5] = [dt * float(a) for a in ac]
+            while n <= m and t >= tg[n - 1]:
+                fr = (t - tg[n - 1]) / dt
+                fl = 1.0 - fr
+                row = []
+                for c in range(6):
+                    ds = sf[c] - si[c]
+                    row.append(fr * si[c] + fl * sf[c]
+                               + fl * fr * ((k[0][c] - ds) * fr + (ds - k[5][c]) * fl))
+                out[n - 1, :6] = row
+                out[n - 1, 6] = math.sqrt((row[3] * row[3] + row[4] * row[4]) + row[5] * row[5] + 1.0)
+                out[n - 1, 7] = dt
+                n += 1
+            si = sf
+            cnt[1] += 1
+            dtn = dt * min(fcmx, safe * oracle.det_pow(dl, -0.20))
+        else:
+            cnt[2] += 1
+            dtn = dt * max(fcmn, safe * oracle.det_pow(dl, -0.25))
+        cnt[0] += 1
+        dt = min(dtn, dtm)
+    return out, cnt
+
+
+def test_rk5_restated_from_the_fortran_text_bitwise():
+    """The oracle's RK5 equals, bit for bit, a second restatement written
+    line by line from integrations.F90:57-200 (tableau from the literals,
+    stage sums, error norm, accept/reject factors, dense output rows)."""
+    uu, bb = fields.snapshot(16, db_rms=0.8, seed=21)
+    tmax = 0.6 * T0
+    prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=tmax, atol=1e-8, rtol=1e-8,
+                             domain_min=(-0.25, 0.0, 0.5), domain_max=(0.75, 2.0, 1.5))
+    tg = params.time_grid(5, tmax)
+    st = np.zeros((4, tg.size, 8))
+    st[:, 0, :6] = initial.isotropic_state(4, 22, gamma_range=(1.001, 20.0),
+                                           domain_min=(-0.25, 0.0, 0.5), domain_max=(0.75, 2.0, 1.5))
+    s, c, status = oracle.integrate("rk5", prm, tg, uu, bb, st.copy())
+    assert (status == 0).all()
+    for p in range(4):
+        rows, cnt = _rk5_restated(prm, tg, uu, bb, st[p, 0, :6])
+        assert list(c[p]) == cnt
+        assert np.array_equal(s[p].view(np.int64), rows.view(np.int64)), p
