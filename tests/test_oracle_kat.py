@@ -501,3 +501,218 @@ def test_rk5_restated_from_the_fortran_text_bitwise():
         rows, cnt = _rk5_restated(prm, tg, uu, bb, st[p, 0, :6])
         assert list(c[p]) == cnt
         assert np.array_equal(s[p].view(np.int64), rows.view(np.int64)), p
+
+
+# DOP853 coefficients typed from integrations.F90:255-326 (Fortran d-literals)
+_A = {(2, 1): 5.26001519587677318785587544488e-02,
+      (3, 1): 1.97250569845378994544595329183e-02, (3, 2): 5.91751709536136983633785987549e-02,
+      (4, 1): 2.95875854768068491816892993775e-02, (4, 3): 8.87627564304205475450678981324e-02,
+      (5, 1): 2.41365134159266685502369798665e-01, (5, 3): -8.84549479328286085344864962717e-01,
+      (5, 4): 9.24834003261792003115737966543e-01,
+      (6, 1): 3.70370370370370370370370370370e-02, (6, 4): 1.70828608729473871279604482173e-01,
+      (6, 5): 1.25467687566822425016691814123e-01,
+      (7, 1): 3.71093750000000000000000000000e-02, (7, 4): 1.70252211019544039314978060272e-01,
+      (7, 5): 6.02165389804559606850219397283e-02, (7, 6): -1.75781250000000000000000000000e-02,
+      (8, 1): 3.70920001185047927108779319836e-02, (8, 4): 1.70383925712239993810214054705e-01,
+      (8, 5): 1.07262030446373284651809199168e-01, (8, 6): -1.53194377486244017527936158236e-02,
+      (8, 7): 8.27378916381402288758473766002e-03,
+      (9, 1): 6.24110958716075717114429577812e-01, (9, 4): -3.36089262944694129406857109825e+00,
+      (9, 5): -8.68219346841726006818189891453e-01, (9, 6): 2.75920996994467083049415600797e+01,
+      (9, 7): 2.01540675504778934086186788979e+01, (9, 8): -4.34898841810699588477366255144e+01,
+      (10, 1): 4.77662536438264365890433908527e-01, (10, 4): -2.48811461997166764192642586468e+00,
+      (10, 5): -5.90290826836842996371446475743e-01, (10, 6): 2.12300514481811942347288949897e+01,
+      (10, 7): 1.52792336328824235832596922938e+01, (10, 8): -3.32882109689848629194453265587e+01,
+      (10, 9): -2.03312017085086261358222928593e-02,
+      (11, 1): -9.37142430085987325717040216580e-01, (11, 4): 5.18637242884406370830023853209e+00,
+      (11, 5): 1.09143734899672957818500254654e+00, (11, 6): -8.14978701074692612513997267357e+00,
+      (11, 7): -1.85200656599969598641566180701e+01, (11, 8): 2.27394870993505042818970056734e+01,
+      (11, 9): 2.49360555267965238987089396762e+00, (11, 10): -3.04676447189821950038236690220e+00,
+      (12, 1): 2.27331014751653820792359768449e+00, (12, 4): -1.05344954667372501984066689879e+01,
+      (12, 5): -2.00087205822486249909675718444e+00, (12, 6): -1.79589318631187989172765950534e+01,
+      (12, 7): 2.79488845294199600508499808837e+01, (12, 8): -2.85899827713502369474065508674e+00,
+      (12, 9): -8.87285693353062954433549289258e+00, (12, 10): 1.23605671757943030647266201528e+01,
+      (12, 11): 6.43392746015763530355970484046e-01}
+_BW = [(1, 5.42937341165687622380535766363e-02), (6, 4.45031289275240888144113950566e+00),
+       (7, 1.89151789931450038304281599044e+00), (8, -5.80120396001058478146721142270e+00),
+       (9, 3.11164366957819894408916062370e-01), (10, -1.52160949662516078556178806805e-01),
+       (11, 2.01365400804030348374776537501e-01), (12, 4.47106157277725905176885569043e-02)]
+_BH = (0.244094488188976377952755905512e+00, 0.733846688281611857341361741547e+00,
+       0.220588235294117647058823529412e-01)
+_ER = [(1, 0.1312004499419488073250102996e-01), (6, -0.1225156446376204440720569753e+01),
+       (7, -0.4957589496572501915214079952e+00), (8, 0.1664377182454986536961530415e+01),
+       (9, -0.3503288487499736816886487290e+00), (10, 0.3341791187130174790297318841e+00),
+       (11, 0.8192320648511571246570742613e-01), (12, -0.2235530786388629525884427845e-01)]
+
+
+def _dop853_restated(prm, tg, uu, bb, s_init):
+    """integrate_dp853 (integrations.F90:224-505) for one particle, written
+    again from the Fortran text in plain Python floats; stage j's derivative
+    is kept as stage j (the Fortran reuses rows 2 and 3 of k for stages 11
+    and 12, which changes no value)."""
+    qom, vun, tmx, dtm, atol, rtol = prm[0], prm[1], prm[2], prm[4], prm[5], prm[6]
+    fcmn, fcmx, safe, beta = prm[7], prm[8], prm[9], prm[10]
+    xl, xs = tuple(prm[11:14]), tuple(prm[14:17])
+
+    def f(s):
+        return [float(a) for a in oracle.acceleration(qom, vun, uu, bb, np.array(s), xl=xl, xs=xs)]
+
+    expo = 2.0e-01 * beta - 1.25e-01
+    errold, rejected = 1.0e-04, False
+    m = tg.size
+    out = np.zeros((m, 8))
+    cnt = [0, 0, 0]
+    t = 0.0
+    si = [float(v) for v in s_init]
+    dt = oracle.dti_guess(8, prm, uu, bb, np.array(si))
+    out[0, :6] = si
+    out[0, 6] = math.sqrt((si[3] * si[3] + si[4] * si[4]) + si[5] * si[5] + 1.0)
+    out[0, 7] = dt
+    n = 2
+    while t < tmx:
+        k = {1: f(si)}
+        for j in range(2, 13):
+            terms = [(i, a) for (jj, i), a in sorted(_A.items()) if jj == j]
+            ss = []
+            for c in range(6):
+                if j == 2:
+                    ss.append(si[c] + dt * terms[0][1] * k[1][c])
+                else:
+                    acc = terms[0][1] * k[terms[0][0]][c]
+                    for i, a in terms[1:]:
+                        acc = acc + a * k[i][c]
+                    ss.append(si[c] + dt * acc)
+            k[j] = f(ss)
+        k4, sf, sr = [], [], []
+        for c in range(6):
+            acc = _BW[0][1] * k[1][c]
+            for i, b in _BW[1:]:
+                acc = acc + b * k[i][c]
+            k4.append(acc)
+            sf.append(si[c] + dt * acc)
+            sr.append(atol + rtol * max(abs(si[c]), abs(sf[c])))
+        err3 = err5 = 0.0
+        for c in range(6):
+            e = ((k4[c] - _BH[0] * k[1][c]) - _BH[1] * k[9][c]) - _BH[2] * k[12][c]
+            err3 = err3 + (e / sr[c]) ** 2
+        for c in range(6):
+            e = _ER[0][1] * k[1][c]
+            for i, a in _ER[1:]:
+                e = e + a * k[i][c]
+            err5 = err5 + (e / sr[c]) ** 2
+        deno = err5 + 1.0e-02 * err3
+        err = abs(dt) * err5 / math.sqrt(6.0) if deno <= 0.0 else abs(dt) * err5 / math.sqrt(6.0 * deno)
+        if err <= 1.0:
+            t = t + dt
+            ka, kb = f(si), f(sf)
+            while n <= m and t >= tg[n - 1]:
+                fr = (t - tg[n - 1]) / dt
+                fl = 1.0 - fr
+                row = []
+                for c in range(6):
+                    ds = sf[c] - si[c]
+                    row.append(fr * si[c] + fl * sf[c]
+                               + fl * fr * ((dt * ka[c] - ds) * fr + (ds - dt * kb[c]) * fl))
+                out[n - 1, :6] = row
+                out[n - 1, 6] = math.sqrt((row[3] * row[3] + row[4] * row[4]) + row[5] * row[5] + 1.0)
+                out[n - 1, 7] = dt
+                n += 1
+            si = sf
+            cnt[1] += 1
+            dtn = max(fcmn, safe * oracle.det_pow(err, expo) * oracle.det_pow(errold, beta))
+            dtn = dt * min(dtn, 1.0) if rejected else dt * min(dtn, fcmx)
+            errold = max(err, 1.0e-04)
+            rejected = False
+        else:
+            cnt[2] += 1
+            dtn = dt * max(fcmn, safe * oracle.det_pow(err, expo))
+            rejected = True
+        cnt[0] += 1
+        dt = min(dtn, dtm)
+    return out, cnt
+
+
+@pytest.mark.parametrize("beta", [0.0, 0.04])
+def test_dop853_restated_from_the_fortran_text_bitwise(beta):
+    """The oracle's DOP853 equals, bit for bit, a second restatement written
+    line by line from integrations.F90:224-505 (coefficients from the
+    literals, the 12 stages, both error estimates, the PI controller with
+    and without beta, dense output rows)."""
+    uu, bb = fields.snapshot(16, db_rms=0.8, seed=23)
+    tmax = 0.4 * T0
+    prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=tmax, atol=1e-10, rtol=1e-9,
+                             facmin=0.25, facmax=8.0, safe=0.85, beta=beta)
+    tg = params.time_grid(4, tmax)
+    st = np.zeros((3, tg.size, 8))
+    st[:, 0, :6] = initial.isotropic_state(3, 24, gamma_range=(1.001, 20.0))
+    s, c, status = oracle.integrate("dop853", prm, tg, uu, bb, st.copy())
+    assert (status == 0).all()
+    for p in range(3):
+        rows, cnt = _dop853_restated(prm, tg, uu, bb, st[p, 0, :6])
+        assert list(c[p]) == cnt, (p, c[p], cnt)
+        assert np.array_equal(s[p].view(np.int64), rows.view(np.int64)), p
+
+
+def _accel_restated(qom, vun, uu, bb, vec, xl, xs):
+    """acceleration (accelerations.F90:59-96) with interpolate_lin
+    (interpolations.F90:104-226) written again from the Fortran text in plain
+    Python floats.  uu, bb have numpy shape (3, dm3, dm2, dm1).  A node index
+    equal to dm (a fraction that rounds up to 1.0) wraps to node 0, the
+    periodic image -- the one deviation from the reference, which would
+    index past the array."""
+    dm = [uu.shape[3], uu.shape[2], uu.shape[1]]
+    l, r, xd, xu = [0] * 3, [0] * 3, [0.0] * 3, [0.0] * 3
+    for a in range(3):
+        x = (float(vec[a]) - xl[a]) / xs[a]
+        xr = x + 1.0 / float(dm[a])
+        xp = float(dm[a]) * (xr - math.floor(xr))
+        r[a] = int(math.floor(xp)) % dm[a]
+        xp = float(dm[a]) * (x - math.floor(x))
+        pl = math.floor(xp)
+        l[a] = int(pl) % dm[a]
+        xd[a] = xp - pl
+        xu[a] = 1.0 - xd[a]
+    c = [xu[0] * xu[1] * xu[2], xu[0] * xu[1] * xd[2], xu[0] * xd[1] * xu[2], xu[0] * xd[1] * xd[2],
+         xd[0] * xu[1] * xu[2], xd[0] * xu[1] * xd[2], xd[0] * xd[1] * xu[2], xd[0] * xd[1] * xd[2]]
+    corners = [(l[0], l[1], l[2]), (l[0], l[1], r[2]), (l[0], r[1], l[2]), (l[0], r[1], r[2]),
+               (r[0], l[1], l[2]), (r[0], l[1], r[2]), (r[0], r[1], l[2]), (r[0], r[1], r[2])]
+
+    def gather(f):
+        out = []
+        for comp in range(3):
+            acc = None
+            for q, (i, j, k) in enumerate(corners):
+                term = c[q] * float(f[comp, k, j, i])
+                acc = term if acc is None else acc + term
+            out.append(acc)
+        return out
+
+    u, b = gather(uu), gather(bb)
+    v4, v5, v6 = (float(vec[3]), float(vec[4]), float(vec[5]))
+    g = math.sqrt((v4 * v4 + v5 * v5) + v6 * v6 + 1.0)
+    v = [v4 / g, v5 / g, v6 / g]
+    w = [v[0] - u[0], v[1] - u[1], v[2] - u[2]]
+    return [v[0] / vun, v[1] / vun, v[2] / vun,
+            qom * (w[1] * b[2] - w[2] * b[1]),
+            qom * (w[2] * b[0] - w[0] * b[2]),
+            qom * (w[0] * b[1] - w[1] * b[0])]
+
+
+def test_force_and_gather_restated_from_the_fortran_text_bitwise():
+    """The oracle's force equals, bit for bit, a second restatement of
+    accelerations.F90:59-96 and interpolations.F90:104-226, on a non-cubic
+    grid and an offset domain, at random points, far outside the domain and
+    at the rounding edge of the periodic map."""
+    rng = np.random.default_rng(25)
+    shape = (3, 10, 14, 6)                                  # dm = (6, 14, 10)
+    uu = 0.01 * rng.normal(size=shape)
+    bb = rng.normal(size=shape)
+    xl, xs = (-0.5, 0.25, 1.0), (2.0, 1.0, 0.5)
+    pts = np.concatenate([rng.uniform(-3, 4, (300, 3)),
+                          np.array([[-0.5 - 1e-17, 0.25, 1.0], [1.5 - 1e-16, 1.25 - 1e-16, 1.5 - 1e-16],
+                                    [-0.5, 0.25 - 1e-18, 1.0 - 1e-19]])])
+    mom = rng.normal(0, 2, (pts.shape[0], 3))
+    for p, m in zip(pts, mom):
+        vec = np.concatenate([p, m])
+        got = oracle.acceleration(QOM, VUN, uu, bb, vec, xl=xl, xs=xs)
+        want = _accel_restated(QOM, VUN, uu, bb, vec, xl, xs)
+        assert np.array_equal(np.asarray(got).view(np.int64), np.array(want).view(np.int64)), vec
