@@ -716,3 +716,23 @@ def test_force_and_gather_restated_from_the_fortran_text_bitwise():
         got = oracle.acceleration(QOM, VUN, uu, bb, vec, xl=xl, xs=xs)
         want = _accel_restated(QOM, VUN, uu, bb, vec, xl, xs)
         assert np.array_equal(np.asarray(got).view(np.int64), np.array(want).view(np.int64)), vec
+
+
+def test_interpolate_near_restated_from_the_fortran_text():
+    """interpolate_near (interpolations.F90:55-83): p = floor(dm * (x -
+    floor(x))) + 1 on the normalised position, node values as they are; the
+    oracle's copy at random points of a non-cubic grid, an offset domain and
+    the periodic rounding edge (index dm wraps to node 0)."""
+    rng = np.random.default_rng(26)
+    shape = (3, 7, 5, 9)                                     # dm = (9, 5, 7)
+    uu, bb = rng.normal(size=shape), rng.normal(size=shape)
+    dm = (9, 5, 7)
+    xl, xs = (0.25, -1.0, 2.0), (0.5, 3.0, 1.5)
+    pts = np.concatenate([rng.uniform(-4, 5, (300, 3)), np.array([[0.25 - 1e-17, -1.0, 2.0]])])
+    for pos in pts:
+        p = []
+        for a in range(3):
+            x = (float(pos[a]) - xl[a]) / xs[a]
+            p.append(int(math.floor(float(dm[a]) * (x - math.floor(x)))) % dm[a])
+        u, b = oracle.interpolate_near(uu, bb, pos, xl=xl, xs=xs)
+        assert np.array_equal(u, uu[:, p[2], p[1], p[0]]) and np.array_equal(b, bb[:, p[2], p[1], p[0]])
