@@ -25,7 +25,17 @@ Reported (one JSON line, rank 0):
              particle subsample of the same windows
   plain_fma  the same workload with the FMA build of the FP64 kernel (leg
              `fma`), with its roofline against the FMA-counted FP64 peak;
-             plain_fma_face the same with face-capped trial steps
+             plain_fma_face the same with face-capped trial steps, and
+             plain_fma_accuracy both against the exact kernel
+  mixed      the mixed-precision workload (RK5, 512^3, 2^22 particles) in
+             every precision / controller variant, with per-particle
+             energy and position errors against the exact kernel
+  learned    the learned controller against the classical one (DOP853)
+  ensemble   three snapshots in one persistent launch per window, as
+             launches and as a CUDA graph, and with the FMA build and
+             face-capped steps
+  targets    the plain kernel's roofline fractions and the mixed + learned
+             ratios with their accuracy, gathered from the legs above
 
 `--impl reference` times the reference algorithm on the host cores (the CPU
 oracle, the restatement of sources/integrations.F90) on the same workload,
