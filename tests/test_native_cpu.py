@@ -182,3 +182,57 @@ def test_face_params_checked_on_host(native):
     assert native.pt_debug_face_params(2, 0.1, 1.0) == N.PT_ERR_ARG
     assert native.pt_debug_face_params(1, 0.1, 3e-5) == N.PT_OK        # the defaults
     assert native.pt_debug_face_params(2, 0.01, 3e-5) == N.PT_OK
+
+
+def _header_arities():
+    """{function: number of parameters} of the header's prototypes."""
+    text = (ROOT / "include" / "particles_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(pt_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", text, flags=re.S):
+        args = m.group(2).strip()
+        out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_the_header(native):
+    """Every prototype with declared ctypes argument types has as many of
+    them as the header has parameters (a changed C signature must change
+    the binding too)."""
+    ar = _header_arities()
+    assert len(ar) >= 40
+    checked = 0
+    for name, n in ar.items():
+        fn = getattr(native, name)
+        if fn.argtypes is not None:
+            assert len(fn.argtypes) == n, (name, len(fn.argtypes), n)
+            checked += 1
+    assert checked >= 30
+
+
+def test_header_is_plain_c_and_cxx(tmp_path):
+    """The C ABI header compiles as C99 (the Fortran/C side) and as C++11,
+    without warnings, and a C program can link against the library."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no gcc")
+    hdr = ROOT / "include" / "particles_gb300.h"
+    for lang, std in (("c", "-std=c99"), ("c++", "-std=c++11")):
+        r = subprocess.run([gcc, std, "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-x", lang,
+                            str(hdr)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+    from particles_gb300 import _native as N
+    src = tmp_path / "use.c"
+    src.write_text('#include "particles_gb300.h"\n#include <stdio.h>\n'
+                   'int main(void) { printf("%d %d\\n", (int)pt_abi_version(), '
+                   '(int)pt_method_from_name("dop853")); return 0; }\n')
+    lib = N.lib_path()
+    exe = tmp_path / "use"
+    r = subprocess.run([gcc, "-std=c99", "-I", str(ROOT / "include"), str(src), "-o", str(exe),
+                        "-L", str(lib.parent), "-lparticles_gb300", f"-Wl,-rpath,{lib.parent}"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.split() == ["1", "2"], (r.stdout, r.stderr)
