@@ -56,6 +56,21 @@ def _open(path, mode):
     return gzip.open(path, mode) if path.suffix == ".gz" else open(path, mode)
 
 
+def _header(shape, bitpix, keys=None) -> bytes:
+    """Primary-HDU header of an image of numpy `shape`, padded to a block."""
+    cards = [_card("SIMPLE", True, "conforms to FITS standard"),
+             _card("BITPIX", bitpix, "array data type"),
+             _card("NAXIS", len(shape), "number of array dimensions")]
+    for i, n in enumerate(tuple(shape)[::-1]):
+        cards.append(_card(f"NAXIS{i + 1}", int(n)))
+    for k, v in (keys or {}).items():
+        val, com = v if isinstance(v, tuple) else (v, "")
+        cards.append(_card(k.upper(), val, com))
+    cards.append(b"END".ljust(80))
+    header = b"".join(cards)
+    return header + b" " * (-len(header) % BLOCK)
+
+
 def write_image(path, data, keys: dict | None = None, bitpix: int | None = None):
     """Write `data` as the primary image of a new FITS file (gzip for *.gz).
 
@@ -69,17 +84,7 @@ def write_image(path, data, keys: dict | None = None, bitpix: int | None = None)
         bitpix = _FROM_DTYPE[data.dtype]
     if bitpix not in _BITPIX:
         raise ValueError(f"unsupported BITPIX {bitpix}")
-    cards = [_card("SIMPLE", True, "conforms to FITS standard"),
-             _card("BITPIX", bitpix, "array data type"),
-             _card("NAXIS", data.ndim, "number of array dimensions")]
-    for i, n in enumerate(data.shape[::-1]):
-        cards.append(_card(f"NAXIS{i + 1}", int(n)))
-    for k, v in (keys or {}).items():
-        val, com = v if isinstance(v, tuple) else (v, "")
-        cards.append(_card(k.upper(), val, com))
-    cards.append(b"END".ljust(80))
-    header = b"".join(cards)
-    header += b" " * (-len(header) % BLOCK)
+    header = _header(data.shape, bitpix, keys)
     body = np.ascontiguousarray(data).astype(_BITPIX[bitpix]).tobytes()
     body += b"\0" * (-len(body) % BLOCK)
     with _open(path, "wb") as fh:
@@ -192,6 +197,56 @@ def write_fields(datadir, uu, bb, bitpix=-64, names: dict | None = None):
         write_image(Path(datadir) / f"{names[key]}.fits", bb[i], bitpix=bitpix)
 
 
+def _temp_key(temperature):
+    return ({"TEMP": (float(temperature), "Initial thermal temperature")}
+            if temperature is not None else None)
+
+
+class StateWriter:
+    """state.fits written while a run produces it (the output of
+    particles.F90:371 / fitsio.F90:490-540, streamed): the header and a
+    zero-filled data section are laid down once, then ranges of output rows
+    are stored in place through a memory map of the big-endian data (FITS
+    order: NAXIS1 = 8 fastest, NAXIS2 = m, NAXIS3 = np), so rows reach the
+    file as windows finish instead of at the end.  close() flushes; the
+    finished file is byte-identical to write_outputs' state.fits.  Plain
+    .fits only (a gzip stream cannot be written in place)."""
+
+    def __init__(self, path, npart: int, m: int, temperature=None):
+        self.path = Path(path)
+        if self.path.suffix == ".gz":
+            raise ValueError("StateWriter writes plain .fits files")
+        self.shape = (int(npart), int(m), 8)
+        header = _header(self.shape, -64, _temp_key(temperature))
+        nbytes = int(np.prod(self.shape)) * 8
+        with open(self.path, "wb") as fh:
+            fh.write(header)
+            fh.truncate(len(header) + nbytes + (-nbytes % BLOCK))
+        self._mm = np.memmap(self.path, dtype=">f8", mode="r+", offset=len(header),
+                             shape=self.shape) if nbytes else None
+
+    def write_rows(self, n0: int, n1: int, rows):
+        """Store rows n0..n1-1 of every particle: rows has shape (np, n1-n0, 8)."""
+        if not 0 <= n0 <= n1 <= self.shape[1]:
+            raise ValueError(f"rows {n0}:{n1} outside 0:{self.shape[1]}")
+        rows = np.asarray(rows, np.float64)
+        if rows.shape != (self.shape[0], n1 - n0, 8):
+            raise ValueError(f"rows of shape {rows.shape}, expected {(self.shape[0], n1 - n0, 8)}")
+        if self._mm is not None and n1 > n0:
+            self._mm[:, n0:n1, :] = rows
+
+    def close(self):
+        if self._mm is not None:
+            self._mm.flush()
+            self._mm = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
 def write_outputs(outdir, counter, time, state, tunit=None, temperature=None):
     """counter.fits (int64, NAXIS1 = 3), time.fits (key TUNIT) and state.fits
     (key TEMP, NAXIS1 = 8, NAXIS2 = m) as particles.F90:369-371 writes them."""
@@ -200,6 +255,4 @@ def write_outputs(outdir, counter, time, state, tunit=None, temperature=None):
     write_image(out / "counter.fits", np.asarray(counter, np.int64))
     write_image(out / "time.fits", np.asarray(time, np.float64),
                 {"TUNIT": (float(tunit), "Time unit in seconds")} if tunit is not None else None)
-    write_image(out / "state.fits", np.asarray(state, np.float64),
-                {"TEMP": (float(temperature), "Initial thermal temperature")}
-                if temperature is not None else None)
+    write_image(out / "state.fits", np.asarray(state, np.float64), _temp_key(temperature))

@@ -86,3 +86,37 @@ def test_snapshot_and_outputs(tmp_path):
     t2, h = fitsio.read_image(tmp_path / "out" / "time.fits", with_header=True)
     assert np.array_equal(t2, time) and h["TUNIT"] == 0.25
     assert np.array_equal(fitsio.read_image(tmp_path / "out" / "counter.fits"), cnt)
+
+
+def test_state_writer_streams_rows_into_the_same_file(tmp_path):
+    """Rows written in pieces through the memory map give a state.fits
+    byte-identical to the one written at the end (write_outputs)."""
+    from particles_gb300 import fitsio
+    rng = np.random.default_rng(7)
+    state = rng.normal(size=(37, 11, 8))
+    fitsio.write_outputs(tmp_path / "whole", np.zeros((37, 3), np.int64), np.arange(11.0), state,
+                         temperature=1.5e6)
+    with fitsio.StateWriter(tmp_path / "state.fits", 37, 11, temperature=1.5e6) as w:
+        for n0, n1 in ((0, 1), (1, 5), (5, 5), (5, 11)):
+            w.write_rows(n0, n1, state[:, n0:n1])
+    a = (tmp_path / "state.fits").read_bytes()
+    b = (tmp_path / "whole" / "state.fits").read_bytes()
+    assert a == b
+    got, hdr = fitsio.read_image(tmp_path / "state.fits", with_header=True)
+    assert np.array_equal(got, state) and hdr["TEMP"] == 1.5e6
+
+
+def test_state_writer_checks_its_arguments(tmp_path):
+    import pytest
+    from particles_gb300 import fitsio
+    with pytest.raises(ValueError):
+        fitsio.StateWriter(tmp_path / "s.fits.gz", 2, 2)
+    w = fitsio.StateWriter(tmp_path / "s.fits", 2, 3)
+    with pytest.raises(ValueError):
+        w.write_rows(2, 4, np.zeros((2, 2, 8)))
+    with pytest.raises(ValueError):
+        w.write_rows(0, 1, np.zeros((3, 1, 8)))
+    w.close()
+    empty = fitsio.StateWriter(tmp_path / "e.fits", 0, 3)
+    empty.close()
+    assert fitsio.read_image(tmp_path / "e.fits").shape == (0, 3, 8)
