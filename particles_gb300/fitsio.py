@@ -188,7 +188,12 @@ def read_fields(datadir, uunit=1.0, bunit=1.0, names: dict | None = None):
 
 
 def write_fields(datadir, uu, bb, bitpix=-64, names: dict | None = None):
-    """Write a snapshot as six 3-D images <datadir>/<name>.fits."""
+    """Write a snapshot as six 3-D images <datadir>/<name>.fits.
+
+    BITPIX -64 (the default) keeps every bit and is read back exactly by
+    read_fields.  Files meant for the reference's Fortran driver need
+    bitpix=-32: its read_field reads a -64 image with the single-precision
+    ftgpve into a double buffer (fitsio.F90:258-261) and so misreads it."""
     names = {**FIELD_NAMES, **(names or {})}
     Path(datadir).mkdir(parents=True, exist_ok=True)
     for i, key in enumerate(("ux", "uy", "uz")):
