@@ -145,6 +145,9 @@ def parse():
     ap.add_argument("--mixed-steps", type=int, default=5)
     ap.add_argument("--accuracy-particles", type=int, default=32768)
     ap.add_argument("--accuracy-seconds", type=float, default=40.0)
+    ap.add_argument("--legs-out", default="gpurun_out/bench_legs.json",
+                    help="file that receives the full result with every leg (stdout gets one "
+                         "compact line)")
     return ap.parse_args()
 
 
@@ -252,11 +255,16 @@ def _calibrate(cfg, prm, tg, out, s0_all, window, nthreads, ncal=512):
     return (time.perf_counter() - t) / sample[0].shape[0]
 
 
-def cpu_baseline(cfg, prm, tg, out, s0_all, window, warm, steps, seconds):
+def cpu_baseline(cfg, prm, tg, out, s0_all, window, warm, steps, seconds, gpu=None):
     """The CPU oracle (test infrastructure, here only the timed baseline) with
     all host threads on a seeded particle subsample, over exactly the windows
     the GPU timed (after the same warm-up windows); the subsample is sized so
-    the timed part takes about ``seconds``."""
+    the timed part takes about ``seconds``.
+
+    ``gpu`` (host copies of the GPU's counters, carry and first output rows
+    after the same windows, from ``gpu_snapshot``) turns the same run into a
+    parity check: the subsample's states from the oracle and from the kernel
+    are compared bit for bit.  Returns (baseline, parity or None)."""
     nthreads = os.cpu_count() or 1
     per_particle = _calibrate(cfg, prm, tg, out, s0_all, window, nthreads)
     nsub = int(seconds / max(per_particle * steps, 1e-9))
@@ -274,10 +282,44 @@ def cpu_baseline(cfg, prm, tg, out, s0_all, window, warm, steps, seconds):
         _oracle_window(cfg, prm, tg, out, sample, w * window * T0, nthreads)
     el = time.perf_counter() - t0
     acc = float(cnt[:, 1].sum() - acc0)
-    return {"value": acc / el, "unit": "particle-steps/s", "cores": nthreads, "kind": "port",
-            "sample": f"{nsub} of the workload's {s0_all.shape[0]} particles (seeded choice) over "
-                      f"the same {steps} timed windows of {window} gyro-periods after {warm} "
-                      f"warm-up windows; {int(acc)} accepted steps in {el:.1f} s"}
+    base = {"value": acc / el, "unit": "particle-steps/s", "cores": nthreads, "kind": "port",
+            "sample": f"{nsub} of {s0_all.shape[0]} particles (seeded), the same {steps} timed "
+                      f"windows of {window} gyro-periods after {warm} warm-up; {int(acc)} "
+                      f"accepted steps in {el:.1f} s"}
+    return base, (parity_check(sample, gpu, s0_all.shape[0]) if gpu is not None else None)
+
+
+def gpu_snapshot(torch, d_state, d_cnt, d_carry, npart, rows):
+    """Host copies of what a window leaves behind for every particle: counters,
+    the carry's t, dt, errold and current state si(6), and the first ``rows``
+    output rows (the rows written so far)."""
+    car = d_carry[: 15 * 8 * npart].view(torch.float64).view(15, npart)
+    return {"cnt": d_cnt.cpu().numpy(), "t": car[0].cpu().numpy(), "dt": car[1].cpu().numpy(),
+            "errold": car[2].cpu().numpy(), "si": car[3:9].t().cpu().numpy(),
+            "state": d_state[:, :rows].cpu().numpy(), "rows": rows}
+
+
+def parity_check(sample, gpu, npart, seed=12345):
+    """Bit-for-bit comparison of the oracle's subsample (``_oracle_sample``'s
+    seeded choice) with the GPU's snapshot of the same particles."""
+    state, cnt, carry = sample
+    nsub = state.shape[0]
+    idx = np.random.default_rng(seed).choice(npart, nsub, replace=False)
+    idx.sort()
+    ca = np.ctypeslib.as_array(carry)
+    o_t, o_dt, o_eo, o_si = ca["t"], ca["dt"], ca["errold"], ca["si"]
+    r = gpu["rows"]
+    bad = np.zeros(nsub, bool)
+    bad |= (gpu["cnt"][idx] != cnt).any(1)
+    for a, b in ((gpu["t"][idx], o_t), (gpu["dt"][idx], o_dt), (gpu["errold"][idx], o_eo)):
+        bad |= a.view(np.int64) != np.ascontiguousarray(b, np.float64).view(np.int64)
+    bad |= (gpu["si"][idx].view(np.int64)
+            != np.ascontiguousarray(o_si, np.float64).view(np.int64)).any(1)
+    bad |= (gpu["state"][idx].reshape(nsub, -1).view(np.int64)
+            != np.ascontiguousarray(state[:, :r]).reshape(nsub, -1).view(np.int64)).any(1)
+    return {"bitwise": bool(not bad.any()), "particles": int(nsub), "mismatched": int(bad.sum()),
+            "compared": f"counters, t, dt, errold, x and u of every particle of the CPU sample "
+                        f"and output rows 1..{r}, after the warm-up and timed windows"}
 
 
 def run_reference(args, cfg, rank, world):
@@ -946,6 +988,87 @@ def learned_leg(args, dev, stream):
     return out
 
 
+def _r(x, d=4):
+    """Rounds floats to ``d`` significant digits (compact output)."""
+    if isinstance(x, float):
+        return float(f"{x:.{d}g}")
+    if isinstance(x, dict):
+        return {k: _r(v, d) for k, v in x.items()}
+    if isinstance(x, (list, tuple)):
+        return [_r(v, d) for v in x]
+    return x
+
+
+def targets(line):
+    """At most ten headline figures gathered from the legs: the plain kernel's
+    roofline fractions, the mixed + learned ratios against the plain exact and
+    FMA kernels (accepted steps/s and simulated time per second) and their
+    accuracy."""
+    t = {}
+    roof = line.get("roofline", {})
+    t["plain_exact_frac_of_fp64_fma_peak"] = roof.get("frac")
+    t["plain_exact_frac_of_no_fma_peak"] = roof.get("frac_of_no_fma_peak")
+    if "plain_fma" in line:
+        t["plain_fma_frac_of_fp64_fma_peak"] = line["plain_fma"]["roofline"]["frac"]
+    mx = line.get("mixed")
+    if mx:
+        ov, ph = mx["over_plain_exact"], mx["physics_rate_over_plain_exact"]
+        fma = mx["accepted_steps_per_s"]["fp64_fma"]
+        fma_ph = mx["detail"]["fp64_fma"]["particle_gyroperiods_per_s"]
+        pick = {k: mx["accepted_steps_per_s"][k] for k in ("bf16_learned", "bf16_learned_face",
+                                                          "fp32_learned", "fp32_learned_face")
+                if k in mx["accepted_steps_per_s"]}
+        best = max(pick, key=pick.get)
+        t["mixed_learned_variant"] = best
+        t["mixed_learned_over_plain_exact"] = {"accepted": ov[best], "simulated_time": ph[best]}
+        t["mixed_learned_over_plain_fma"] = {
+            "accepted": pick[best] / fma,
+            "simulated_time": mx["detail"][best]["particle_gyroperiods_per_s"] / fma_ph}
+        nf = best.replace("_face", "")
+        if nf != best and nf in ov:
+            t["mixed_learned_no_face_over_plain_exact"] = {"accepted": ov[nf],
+                                                           "simulated_time": ph[nf]}
+        acc = mx.get("accuracy", {}).get(best)
+        if acc:
+            last = max(acc["rows"], key=int)
+            t["mixed_learned_energy_err"] = {
+                f"t{r}": {"median": acc["rows"][r]["energy_rel_err_median"],
+                          "frac_le_1e-6": acc["rows"][r]["fraction_energy_err_le_1e-6"]}
+                for r in sorted({"1", last}, key=int)}
+    if "learned" in line:
+        t["learned_dop853_simulated_time_ratio"] = line["learned"]["physics_rate_ratio"]
+    return {k: v for k, v in t.items() if v is not None}
+
+
+def compact_line(line, legs_path):
+    """The one JSON line on stdout (under 2 KB): the contract's keys for the
+    headline kernel; every leg in full goes to ``legs_path``."""
+    roof = line["roofline"]
+    out = {k: line[k] for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup",
+                                 "ms_per_step", "higher_is_better", "scaling", "vs_baseline",
+                                 "dtype", "data") if k in line}
+    cfg = dict(line["config"])
+    cfg["l2"] = "inputs larger than L2, no flush"
+    out["config"] = cfg
+    out["roofline"] = {"bound": roof["bound"], "achieved": roof["achieved"],
+                       "peak": roof["peak"], "unit": roof["unit"], "frac": roof["frac"],
+                       "traffic": roof.get("traffic"),
+                       "peak_source": "FP64 FMA peak measured live (pt_probe_peak)",
+                       "frac_of_no_fma_peak": roof.get("frac_of_no_fma_peak")}
+    for k in ("e2e", "cpu_baseline", "parity", "clocks", "gpu_launches", "rejected_fraction",
+              "stopped_particles"):
+        if line.get(k) not in (None, {}):
+            out[k] = line[k]
+    if "e2e" in out:
+        out["e2e"] = {k: out["e2e"][k] for k in ("value", "unit", "h2d_bytes_per_step",
+                                                 "d2h_bytes_per_step")}
+    if "parity" in out:
+        out["parity"] = {k: out["parity"][k] for k in ("bitwise", "particles", "mismatched")}
+    out["targets"] = targets(line)
+    out["legs"] = legs_path
+    return _r(out)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -1044,6 +1167,13 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     stopped = stopped_particles(f, d_status, "timed run")
+    # what the timed windows left behind, for the bitwise comparison with the
+    # CPU oracle's sample over the same windows (rows written so far + 1)
+    snap = None
+    if not args.no_cpu and rank == 0 and world == 1 and args.precision == "fp64" \
+            and args.controller == "classical":
+        rows = min(m, int(w * window + 1e-9) + 2)
+        snap = gpu_snapshot(torch, d_state, d_cnt, d_carry, npart, rows)
     kern_ms = [a.elapsed_time(b) for a, b in ev]
     dev_s = sum(kern_ms) * 1e-3
     c_now = d_cnt.cpu().numpy()
@@ -1151,8 +1281,11 @@ def main():
         line["plain_fma_accuracy"] = headline_accuracy(cfg, prm, tg, out, s0, dev)
 
     if not args.no_cpu and rank == 0 and world == 1:
-        line["cpu_baseline"] = cpu_baseline(cfg, prm, tg, out, s0, window, args.warmup,
-                                            args.steps, args.cpu_seconds)
+        line["cpu_baseline"], par = cpu_baseline(cfg, prm, tg, out, s0, window, args.warmup,
+                                                 args.steps, args.cpu_seconds, gpu=snap)
+        if par is not None:
+            line["parity"] = par
+        snap = None
     legs = set(args.legs.split(","))
     if not args.no_mixed and "mixed" in legs and rank == 0 and args.workload == "dop853-256":
         f.close()
@@ -1186,7 +1319,10 @@ def main():
         torch.cuda.empty_cache()
         line["ensemble"] = ensemble_leg(args, dev, stream)
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        legs_out = Path(args.legs_out)
+        legs_out.parent.mkdir(parents=True, exist_ok=True)
+        legs_out.write_text(json.dumps(line, indent=1))
+        print(json.dumps(compact_line(line, str(legs_out))), flush=True)
     if model is not None:
         model.close()
     if world > 1:
