@@ -278,24 +278,34 @@ int pt_mlp_adam(float *d_params, const float *d_grad, float *d_m, float *d_v, in
 
 /* ---- no device allocation ------------------------------------------------ */
 
-/* For callers that cannot call cudaMalloc (code where the device allocator is
- * off limits: host callbacks, foreign allocators that forbid allocations of
- * their own, real-time loops that must not block).  No counterpart in the
- * reference.  The same exact FP64 integration as pt_run_device with the
+/* For callers that cannot call cudaMalloc: code running under an allocator
+ * owned by another runtime that forbids device allocations of its own, or a
+ * real-time loop where an allocation could block or fail.  No counterpart in
+ * the reference.  The same exact FP64 integration as pt_run_device with the
  * reference's behaviour (no options), but the fields come as DEVICE pointers
  * in the reference layout and every byte of scratch -- the converted field
- * records, the work-queue head, the flags -- lives in a static device array
- * that each GPU loading this library holds until exit.  Nothing is allocated.
- * Capacity: grids of at most 64^3 nodes (ideal MHD); larger ones return
- * PT_ERR_ARG.  The first call on a device looks up the array's address, so
- * make it before any stream capture.  All calls share the array: calls that
- * overlap on the GPU race, so serialise them.  Launches on `stream` and
- * returns without synchronising; d_status (np int32, may be NULL) holds the
- * per-particle outcome once the stream is synchronised. */
+ * records, the work-queue head, the flags, the out-of-range counter -- lives
+ * in a static device array that each GPU loading this library holds until
+ * exit.  Capacity: grids of at most 64^3 nodes (ideal MHD); larger ones
+ * return PT_ERR_ARG.  The first call on a device looks up the array's
+ * address and, under CUDA's lazy module loading, loads the kernels (the
+ * driver allocates memory for them then): make it at set-up time, e.g. with
+ * np = 1 on a small grid, and before any stream capture; later calls
+ * allocate nothing.  The function makes CUDA runtime calls, so it must not
+ * be called from a stream callback or cudaLaunchHostFunc host function.  All
+ * calls share the array: calls that overlap on the GPU race, so serialise
+ * them.  Launches on `stream` and returns without synchronising; d_status
+ * (np int32, may be NULL) holds the per-particle outcome once the stream is
+ * synchronised. */
 int pt_integrate_device_noalloc(int32_t method, int64_t np, int32_t m, const int32_t dm[3],
                                 const double params[17], const double *d_time,
                                 const double *d_uu, const double *d_bb, double *d_state,
                                 int64_t *d_cnt, int32_t *d_status, void *stream);
+/* Outcome of the last pt_integrate_device_noalloc call on the current device
+ * (no counterpart in the reference): synchronises `stream`, then returns
+ * PT_OK, PT_ERR_BOUNDS, PT_ERR_TIMEOUT or PT_ERR_PARTICLE from the flags in
+ * the static array, as pt_run_check does for handle runs.  Allocates nothing. */
+int pt_integrate_device_noalloc_check(void *stream);
 
 /* ---- initial state and its moments (the step before the path) ------------ */
 

@@ -28,7 +28,7 @@ EXPORTS = [
     "pt_fields_destroy", "pt_fields_bytes", "pt_integrate_fields", "pt_carry_bytes",
     "pt_run_device", "pt_run_check", "pt_last_error", "pt_abi_version", "pt_tableau",
     "pt_debug_pow", "pt_debug_accel", "pt_probe_peak", "pt_debug_unpack", "pt_debug_echo",
-    "pt_integrate_device_noalloc", "pt_mlp_nparam", "pt_mlp_create", "pt_mlp_destroy",
+    "pt_integrate_device_noalloc", "pt_integrate_device_noalloc_check", "pt_mlp_nparam", "pt_mlp_create", "pt_mlp_destroy",
     "pt_mlp_infer", "pt_mlp_loss_grad", "pt_mlp_adam", "pt_autotune",
     "pt_ensemble_create", "pt_ensemble_destroy", "pt_ensemble_run", "pt_ensemble_capture",
     "pt_ensemble_replay", "pt_ensemble_counts", "pt_ensemble_escaped", "pt_ensemble_check",
@@ -122,6 +122,7 @@ def load():
     L.pt_debug_unpack.argtypes = [i32, i64, i32, vp, i32, i32, vp, vp, vp]
     L.pt_debug_echo.argtypes = [i32, i64, i32, vp, i32, i32, vp, vp, vp, vp]
     L.pt_integrate_device_noalloc.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.pt_integrate_device_noalloc_check.argtypes = [vp]
     L.pt_initial_state.argtypes = [i32, i64, i32, C.c_uint64, i64, vp, vp, vp]
     L.pt_moments.argtypes = [i64, vp, i64, vp, vp]
     L.pt_debug_face_params.argtypes = [i32, C.c_float, C.c_float]
