@@ -120,12 +120,21 @@ struct EvalF64 {
                 for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * v[cc] : acc[cc] + w8[q] * v[cc];
             }
         }
+#ifdef PT_EXACT
         const double g = sqrt(s[3] * s[3] + s[4] * s[4] + s[5] * s[5] + 1.0);
         const double v0 = s[3] / g, v1 = s[4] / g, v2 = s[5] / g;
-        const double w0 = v0 - acc[0], w1 = v1 - acc[1], w2 = v2 - acc[2];
         a[0] = v0 / P.vun;
         a[1] = v1 / P.vun;
         a[2] = v2 / P.vun;
+#else
+        /* 1/gamma once, then multiplies (within an ulp of the divisions) */
+        const double ig = pt_sm::pt_rsqrt(fma(s[3], s[3], fma(s[4], s[4], fma(s[5], s[5], 1.0))));
+        const double v0 = s[3] * ig, v1 = s[4] * ig, v2 = s[5] * ig;
+        a[0] = v0 * P.inv_vun;
+        a[1] = v1 * P.inv_vun;
+        a[2] = v2 * P.inv_vun;
+#endif
+        const double w0 = v0 - acc[0], w1 = v1 - acc[1], w2 = v2 - acc[2];
         if (NC == 10) {                                           /* resistive extension */
             a[3] = P.qom * ((w1 * acc[5] - w2 * acc[4]) + P.eta * acc[6 % NV]);
             a[4] = P.qom * ((w2 * acc[3] - w0 * acc[5]) + P.eta * acc[7 % NV]);

@@ -71,6 +71,38 @@ def test_accel_bitwise(cuda, oracle_lib, with_j):
     assert np.array_equal(got, ref)
 
 
+def test_accel_fma_within_ulps(cuda, oracle_lib):
+    """The FMA build's force: contracted gather sums, and 1/gamma from a
+    refined reciprocal square root in place of the square root and the six
+    divisions (u / gamma, v / vun).  It stays within a few ulps of the
+    oracle's force scale, momenta up to gamma ~ 1e4 included."""
+    torch = cuda
+    import oracle
+    from particles_gb300 import Fields, fields, params
+    from particles_gb300 import _native as N
+    uu, bb = fields.snapshot(12, seed=3)
+    rng = np.random.default_rng(5)
+    vec = np.concatenate([rng.uniform(-1.5, 2.5, (800, 3)),
+                          rng.normal(0, 1, (800, 3)) * 10.0 ** rng.uniform(-4, 4, (800, 1))], 1)
+    prm = params.pack_params(qom=200.0, vunit=0.05, tmax=1.0)
+    f = Fields(uu, bb, precision="fp64_fma")
+    dv = torch.tensor(vec.ravel(), device="cuda")
+    da = torch.empty_like(dv)
+    N.check(N.load().pt_debug_accel(f.handle, vec.shape[0], prm.ctypes.data_as(C.c_void_p),
+                                    C.c_void_p(dv.data_ptr()), C.c_void_p(da.data_ptr()), None),
+            "pt_debug_accel")
+    torch.cuda.synchronize()
+    f.close()
+    got = da.cpu().numpy().reshape(-1, 6)
+    ref = np.stack([oracle.acceleration(200.0, 0.05, uu, bb, v) for v in vec])
+    eps = np.finfo(np.float64).eps
+    # dx/dt = v / vun: relative to its own scale; du/dt: to qom |w| |B|
+    sx = np.linalg.norm(ref[:, :3], axis=1, keepdims=True)
+    assert (np.abs(got[:, :3] - ref[:, :3]) / sx).max() < 8 * eps
+    su = np.linalg.norm(ref[:, 3:], axis=1, keepdims=True) + 200.0 * 1e-3
+    assert (np.abs(got[:, 3:] - ref[:, 3:]) / su).max() < 64 * eps
+
+
 @pytest.mark.parametrize("method", ["rk5", "dop853"])
 def test_fused_exact_bitwise(cuda, oracle_lib, method):
     prob = small_problem(method, n=16, npart=96, periods=2.0, seed=4)
