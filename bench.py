@@ -133,6 +133,9 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-controller leg")
     ap.add_argument("--no-order", action="store_true",
                     help="keep the natural queue order (default: longest first)")
+    ap.add_argument("--order", choices=["work", "brick"], default="work",
+                    help="queue order: longest first (work), or longest-first classes "
+                         "sorted inside by the Morton index of the particle's cell (brick)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble leg")
     ap.add_argument("--ensemble-precision", choices=["fp64", "fp64_fma", "fp32"], default="fp64")
     ap.add_argument("--no-face-ensemble", action="store_true",
@@ -144,11 +147,22 @@ def parse():
                     help="comma list of legs to run (headline always prints the line)")
     ap.add_argument("--mixed-steps", type=int, default=5)
     ap.add_argument("--accuracy-particles", type=int, default=32768)
-    ap.add_argument("--accuracy-seconds", type=float, default=40.0)
+    ap.add_argument("--accuracy-seconds", type=float, default=60.0,
+                    help="time limit of the exact kernel's accuracy reference run")
     ap.add_argument("--legs-out", default="gpurun_out/bench_legs.json",
                     help="file that receives the full result with every leg (stdout gets one "
                          "compact line)")
     return ap.parse_args()
+
+
+def hbm_peak():
+    """Measured HBM copy bandwidth (B/s) from the measured-peaks file when it
+    is present, else the 6.8 TB/s fallback; returns (B/s, source)."""
+    f = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(f.read_text())["hbm_gbs"]) * 1e9, "measured"
+    except (OSError, ValueError, KeyError):
+        return 6.8e12, "fallback"
 
 
 def dist_env():
@@ -404,13 +418,25 @@ def stopped_particles(f, d_status, where):
 class QueueOrder:
     """Longest-first queue order for the persistent kernel: particles sorted
     by the attempts they needed in the previous window, so the slowest ones
-    start first and the end-of-window tail stays short.  The order changes
-    which lane takes which particle, never a particle's result."""
+    start first and the end-of-window tail stays short.  With ``cells`` (the
+    grid's (dm1, dm2, dm3), unit domain) and the carry, the order is by work
+    class (bit length of the attempts, longest first) and, inside a class, by
+    the Morton index of the particle's cell, so the lanes of a warp start on
+    neighbouring cells and share the 8^3 bricks they gather from.  The order
+    changes which lane takes which particle, never a particle's result."""
 
-    def __init__(self, torch, d_cnt, enabled=True):
+    def __init__(self, torch, d_cnt, enabled=True, cells=None, d_carry=None):
         self.torch, self.cnt, self.enabled = torch, d_cnt, enabled
         self.prev = None
         self.order = None
+        self.cells, self.carry = cells, d_carry
+        if cells is not None:
+            bits = max(int(d - 1).bit_length() for d in cells)
+            v = torch.arange(1 << bits, device=d_cnt.device, dtype=torch.int64)
+            spread = torch.zeros_like(v)
+            for b in range(bits):
+                spread |= ((v >> b) & 1) << (3 * b)
+            self.spread = spread
 
     def before(self):
         if self.enabled:
@@ -418,9 +444,24 @@ class QueueOrder:
         return self.order
 
     def after(self):
-        if self.enabled:
-            work = self.cnt[:, 0] - self.prev
-            self.order = self.torch.argsort(work, descending=True).to(self.torch.int32)
+        if not self.enabled:
+            return
+        torch = self.torch
+        work = self.cnt[:, 0] - self.prev
+        if self.cells is None:
+            self.order = torch.argsort(work, descending=True).to(torch.int32)
+            return
+        n = work.shape[0]
+        x = self.carry[: 9 * 8 * n].view(torch.float64)[3 * n: 6 * n].view(3, n)
+        key = torch.zeros(n, dtype=torch.int64, device=work.device)
+        for i in range(3):
+            d = self.cells[i]
+            c = torch.remainder(torch.floor(x[i] * d), d).to(torch.int64)
+            key |= self.spread[c] << i
+        cls = 63 - torch.bucketize(work, torch.tensor([1 << k for k in range(63)],
+                                                      device=work.device), right=True)
+        key |= cls << 40
+        self.order = torch.argsort(key).to(torch.int32)
 
 
 def tune(args, f, method, prm, d_time, d_state, stream, t_stop, **kw):
@@ -541,14 +582,14 @@ def headline_accuracy(cfg, prm, tg, out, s0, dev, na=16384):
     return acc
 
 
-def mixed_leg(args, dev, stream):
+def mixed_leg(args, dev, stream, peak):
     """The mixed-precision workload (RK5, rtol 1e-8, 512^3, 2^22 particles): accepted
     particle-steps/s of the exact FP64, FMA FP64 and mixed FP32 kernels on the
     same windows, and the mixed kernel's per-particle energy / position error
     against the exact kernel (bit-identical to the CPU oracle) at a common
     output time."""
     import torch
-    from particles_gb300 import Fields, fields, initial, params
+    from particles_gb300 import Fields, fields, initial, params, roofline
     cfg = WORKLOADS["rk5-512"]
     npart, window = cfg["npart"], cfg["window"]
     tmax = cfg["periods"] * T0
@@ -587,7 +628,8 @@ def mixed_leg(args, dev, stream):
         st, cnt, status, carry = fresh(npart)
         launch = tune(args, f, "rk5", prm, d_time, st, stream, window * T0, model=mdl,
                       face_steps=face)
-        ordq = QueueOrder(torch, cnt, enabled=not args.no_order)
+        ordq = QueueOrder(torch, cnt, enabled=not args.no_order,
+                          cells=(cfg["n"],) * 3 if args.order == "brick" else None, d_carry=carry)
         w = 0
         for _ in range(args.warmup):
             w += 1
@@ -616,7 +658,9 @@ def mixed_leg(args, dev, stream):
                        "rejected_fraction": float(d[2] / max(d[0], 1)),
                        "ms_per_step": 1e3 * sec / args.mixed_steps,
                        "particle_gyroperiods_per_s": npart * window * args.mixed_steps / sec,
-                       "stopped_particles": stopped, "launch": launch}
+                       "stopped_particles": stopped, "launch": launch,
+                       "roofline": roofline.mixed_roofline("rk5", prec, d[None], sec,
+                                                           fp64_peak=peak, hbm_peak=hbm_peak()[0])}
         if name == "fp64":
             # the plain integrator writes the learned controller's training records
             rec = LRN.record_buffer(torch, min(args.records, 4_000_000))
@@ -667,13 +711,16 @@ def mixed_leg(args, dev, stream):
         rates["bf16_learned"]["particle_gyroperiods_per_s"]
         / rates["fp64"]["particle_gyroperiods_per_s"])
 
-    # accuracy of every variant: a seeded subsample, the exact kernel integrated
-    # as far as a third of the time budget allows, every other variant to the
-    # same output time
+    # accuracy of every variant on a seeded subsample at 1, 10 and 50
+    # gyro-periods (the configuration's t_end): the exact kernel integrated
+    # as far as the time budget allows (50 gyro-periods take ~25 s), every
+    # other variant to the same output time.  Per-particle errors at late
+    # times measure chaos; the energy histograms are compared by their
+    # two-sample KS distance against the 95 % critical value 1.36 sqrt(2/n).
     na = min(args.accuracy_particles, npart)
     res = {}
     w_ref = cfg["periods"]
-    for name, prec in MIXED_VARIANTS:
+    for name, prec in (MIXED_VARIANTS if na > 0 else ()):
         face = name.endswith("_face")
         mdl = (model_face if face else model) if "_learned" in name else None
         st, cnt, status, carry = fresh(na)
@@ -682,22 +729,26 @@ def mixed_leg(args, dev, stream):
         while True:
             w += 1
             handles[prec].run_device("rk5", prm, d_time, st, cnt, status, carry,
-                                     t_stop=min(w * T0, tmax), time_budget_s=900.0,
+                                     t_stop=tg[min(w, m - 1)] * (1 + 1e-12), time_budget_s=900.0,
                                      stream=stream.cuda_stream, model=mdl, face_steps=face)
             stream.synchronize()
             if w >= w_ref or (name == "fp64" and
-                              time.perf_counter() - t_start > args.accuracy_seconds / 3):
+                              time.perf_counter() - t_start > args.accuracy_seconds):
                 break
         if name == "fp64":
             w_ref = w
         res[name] = (st.cpu().numpy(), w)
     from particles_gb300 import errors
     out["accuracy"] = {}
-    for prec, _ in MIXED_VARIANTS[1:]:
+    ks_bound = 1.36 * math.sqrt(2.0 / max(na, 1))
+    for prec, _ in (MIXED_VARIANTS[1:] if na > 0 else ()):
         nrow = min(res["fp64"][1], res[prec][1])       # sample index reached by both
-        rep = errors.report(res["fp64"][0], res[prec][0], rows=(1, nrow), tgrid=tg / T0)
+        rep = errors.report(res["fp64"][0], res[prec][0], rows=(1, min(10, nrow), nrow),
+                            tgrid=tg / T0)
         rep["reference"] = "exact FP64 kernel (bit-identical to the CPU oracle)"
         rep["particles"] = na
+        rep["ks_bound"] = ks_bound
+        rep["ks_within_bound"] = all(r["ks_energy"] < ks_bound for r in rep["rows"].values())
         out["accuracy"][prec] = rep
     for mo in (model, model_face):
         if mo is not None:
@@ -1031,10 +1082,12 @@ def targets(line):
         acc = mx.get("accuracy", {}).get(best)
         if acc:
             last = max(acc["rows"], key=int)
+            r1, rl = acc["rows"]["1"], acc["rows"][last]
             t["mixed_learned_energy_err"] = {
-                f"t{r}": {"median": acc["rows"][r]["energy_rel_err_median"],
-                          "frac_le_1e-6": acc["rows"][r]["fraction_energy_err_le_1e-6"]}
-                for r in sorted({"1", last}, key=int)}
+                "t1": {"median": r1["energy_rel_err_median"],
+                       "frac_le_1e-6": r1["fraction_energy_err_le_1e-6"]},
+                f"t{last}": {"ks": rl["ks_energy"], "ks_bound": acc.get("ks_bound"),
+                             "mean": rl["mean_energy_rel_err"]}}
     if "learned" in line:
         t["learned_dop853_simulated_time_ratio"] = line["learned"]["physics_rate_ratio"]
     return {k: v for k, v in t.items() if v is not None}
@@ -1117,7 +1170,8 @@ def main():
 
     model = None
     training = None
-    ordq = QueueOrder(torch, d_cnt, enabled=not args.no_order)
+    ordq = QueueOrder(torch, d_cnt, enabled=not args.no_order,
+                      cells=(cfg["n"],) * 3 if args.order == "brick" else None, d_carry=d_carry)
 
     def window_run(w, records=None):
         order = ordq.before()
@@ -1291,7 +1345,7 @@ def main():
         f.close()
         del d_state, d_cnt, d_status, d_carry
         torch.cuda.empty_cache()
-        line["mixed"] = mixed_leg(args, dev, stream)
+        line["mixed"] = mixed_leg(args, dev, stream, peak)
     if "mixed" in line:
         # the headline ratios in one place: mixed precision with the learned
         # controller against the plain exact kernel, and their accuracy

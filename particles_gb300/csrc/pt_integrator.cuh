@@ -377,7 +377,16 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
         }
 #undef PT_OVER_SR
         const double deno = err5 + 1.0e-02 * err3;
+#ifdef PT_EXACT
         return (deno <= 0.0) ? fabs(dt) * err5 / sqrt(6.0) : fabs(dt) * err5 / sqrt(6.0 * deno);
+#else
+        /* 1/sqrt(6) = 0.40824829046386307; the refined reciprocal square
+         * root outside the subnormal range of its hardware approximation */
+        if (!(deno > 1.0e-300))
+            return (deno <= 0.0) ? fabs(dt) * err5 * 0.40824829046386307
+                                 : fabs(dt) * err5 / sqrt(6.0 * deno);
+        return fabs(dt) * err5 * pt_rsqrt(6.0 * deno);
+#endif
     } else {                                                    /* :140-148 */
         double del = 0.0;
 #pragma unroll

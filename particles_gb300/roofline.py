@@ -76,3 +76,46 @@ def gather_bytes(method: str, cnt: np.ndarray, *, record_bytes: int) -> float:
     c = np.asarray(cnt, np.float64).reshape(-1, 3).sum(0)
     evals = (5 * c[0] + c[1]) if method in ("rk5", 1) else (11 * c[0] + c[1])
     return float(evals * 8 * record_bytes)
+
+
+def split_work(method: str, cnt: np.ndarray, *, with_eta: bool = False) -> dict:
+    """Work of a run split by where it executes in the mixed-precision kernels:
+    the step machine (stage sums, error norm, controller: FP64), the
+    evaluations (gather + force: FP64 in the FP64 builds, FP32 in the mixed
+    ones) and their count.  Windows of a continuing run (no initial guess)."""
+    c = np.asarray(cnt, np.float64).reshape(-1, 3).sum(0)
+    if method in ("rk5", 1):
+        evals = 5 * c[0] + c[1]
+        machine = c[0] * FLOPS["rk5_stage"] + c[1] * FLOPS["rk5_accept"] + c[2] * FLOPS["rk5_reject"]
+    else:
+        evals = 11 * c[0] + c[1]
+        machine = (c[0] * FLOPS["dp853_stage"] + c[1] * FLOPS["dp853_accept"]
+                   + c[2] * FLOPS["dp853_reject"])
+    return {"machine_flops": float(machine), "evals": float(evals),
+            "eval_flops": float(evals * FLOPS["eval_j" if with_eta else "eval"])}
+
+
+# bytes one evaluation gathers from each field store: 8 corner records
+# (FP64 records 48 / 80 B; FP32 brick records 32 / 64 B; BF16 brick records
+# 16 / 32 B plus the brick's FP32 offset/scale pairs, 48 / 80 B)
+EVAL_BYTES = {("fp64", False): 8 * 48, ("fp64", True): 8 * 80,
+              ("fp64_fma", False): 8 * 48, ("fp64_fma", True): 8 * 80,
+              ("fp32", False): 8 * 32, ("fp32", True): 8 * 64,
+              ("bf16", False): 8 * 16 + 48, ("bf16", True): 8 * 32 + 80}
+
+
+def mixed_roofline(method: str, precision: str, cnt: np.ndarray, seconds: float, *,
+                   fp64_peak: float, hbm_peak: float, with_eta: bool = False) -> dict:
+    """Roofline figures of one run of any build: FP64 flops per second and
+    their fraction of the FP64 peak (for the mixed builds only the step
+    machine's; their evaluations run in FP32), FP32 flops per second, and the
+    gathered bytes per second against the HBM peak (an upper bound on the
+    field traffic: most gathers hit L1/L2).  Peaks in flop/s and B/s."""
+    w = split_work(method, cnt, with_eta=with_eta)
+    mixed = precision in ("fp32", "bf16")
+    f64 = w["machine_flops"] + (0.0 if mixed else w["eval_flops"])
+    f32 = w["eval_flops"] if mixed else 0.0
+    gb = w["evals"] * EVAL_BYTES[(precision, with_eta)]
+    return {"bound": "fp64", "fp64_tflops": f64 / seconds / 1e12,
+            "fp64_frac": f64 / seconds / fp64_peak, "fp32_tflops": f32 / seconds / 1e12,
+            "gather_gbs": gb / seconds / 1e9, "gather_frac_of_hbm": gb / seconds / hbm_peak}

@@ -38,8 +38,9 @@ def test_reference_arm_other_ranks_exit_quietly():
 def _full_line():
     """A result with every leg, shaped as bench.main() builds it."""
     acc = {"rows": {r: {"energy_rel_err_median": 1.23456789e-8, "energy_rel_err_p90": 4.5e-7,
-                        "fraction_energy_err_le_1e-6": 0.93712345, "ks_energy": 0.0012345}
-                    for r in ("1", "50")}}
+                        "fraction_energy_err_le_1e-6": 0.93712345, "ks_energy": 0.0012345,
+                        "mean_energy_rel_err": 1.234567e-5}
+                    for r in ("1", "10", "50")}, "ks_bound": 0.010625}
     names = ("fp64", "fp64_fma", "fp32", "bf16", "fp32_learned", "bf16_learned",
              "fp64_fma_face", "fp32_face", "bf16_face", "fp32_learned_face", "bf16_learned_face")
     detail = {k: {"value": 1.2345678e8, "particle_gyroperiods_per_s": 12345.678901,
