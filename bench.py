@@ -465,17 +465,17 @@ class QueueOrder:
 
 
 def tune(args, f, method, prm, d_time, d_state, stream, t_stop, **kw):
-    """pt_autotune of the kernel the next runs launch (launch variant = resident
-    blocks per SM); the choice becomes that kernel's default.  The trial is
-    the first window itself, on all particles (scratch copies): per-particle
-    work spreads over ~100x within a window, so short capped trials on a
-    sample mispredict the full launch."""
+    """pt_autotune of the kernel the next runs launch (launch variant =
+    register cap x threads per block); the choice becomes that kernel's
+    default.  The trial is the first window itself, on all particles
+    (scratch copies): per-particle work spreads over ~100x within a window, so
+    short capped trials on a sample mispredict the full launch."""
     if args.no_autotune:
         return None
-    v, ms = f.autotune(method, prm, d_time, d_state, stream=stream.cuda_stream, t_stop=t_stop,
-                       sample=-1, **kw)
-    return {"blocks_per_sm": v, "trial": "first window, all particles",
-            "trial_ms": {str(k): round(t, 3) for k, t in ms.items()}}
+    (v, tpb), ms = f.autotune(method, prm, d_time, d_state, stream=stream.cuda_stream,
+                              t_stop=t_stop, sample=-1, **kw)
+    return {"blocks_per_sm": v, "threads_per_block": tpb, "trial": "first window, all particles",
+            "trial_ms": {f"{b}x{t}": round(ms_, 3) for (b, t), ms_ in ms.items()}}
 
 
 def plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev, stream, peak, rec_bytes,

@@ -107,6 +107,8 @@ typedef struct pt_options {
     int32_t       interpolation;  /* 0: trilinear, interpolate_lin (interpolations.F90:104-226),
                                      the reference's choice; 1: the node at the lower
                                      corner of the cell, interpolate_near (:55-83) */
+    int32_t       threads_per_block; /* 64, 128 or 256 (one particle per lane); 0 = the
+                                     choice of pt_autotune for this kernel, else 128 */
 } pt_options;
 
 /* ---- one-shot, reference-shaped call ----------------------------------- */
@@ -170,19 +172,24 @@ int pt_run_device(int32_t method, int64_t np, int32_t m, const pt_fields *f,
 int pt_run_check(const pt_fields *f);
 
 /* Launch autotuner: times the kernel that pt_run_device would launch with
- * these arguments in each of its launch variants (blocks_per_sm 2, 3, 4) and
- * makes the fastest the default (blocks_per_sm == 0) of that kernel family
- * for the rest of the process.  The trial runs the first `sample` particles
- * (0: min(np, 2 x 4 x 128 per SM); < 0: all np) from state(:,1,:) on
- * scratch copies: up to opt->t_stop when it is > 0 -- a real first window,
- * outliers and tail included -- else max_steps attempts each (opt->max_steps,
- * else 32).  d_state is only read.  Synchronises the stream.  chosen: the
- * variant (2, 3 or 4); ms_out (host, 3 doubles, or NULL): the trial times of
- * variants 2, 3, 4. */
+ * these arguments in its launch variants and makes the fastest the default
+ * (blocks_per_sm == 0, threads_per_block == 0) of that kernel family for the
+ * rest of the process.  Search: the register cap of 2, 3 and 4 resident
+ * 128-thread blocks per SM at 128 threads per block, then 64 and 256
+ * threads per block at the best cap (one particle per lane throughout: the
+ * lanes of a warp walk the stages in lock step).  The trial runs the first
+ * `sample` particles (0: min(np, 2 x 4 x 128 per SM); < 0: all np) from
+ * state(:,1,:) on scratch copies: up to opt->t_stop when it is > 0 -- a real
+ * first window, outliers and tail included -- else max_steps attempts each
+ * (opt->max_steps, else 32).  d_state is only read.  Synchronises the
+ * stream.  chosen (2 int32, or NULL): blocks_per_sm and threads_per_block of
+ * the winner; ms_out (host, 9 doubles, or NULL): the trial time of
+ * (blocks_per_sm b, threads t) at [3 (b - 2) + {64: 0, 128: 1, 256: 2}[t]],
+ * -1 where not tried. */
 int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_fields *f,
                 const double params[17], const double *d_time, const double *d_state,
-                const pt_options *opt, int64_t sample, void *stream, int32_t *chosen,
-                double ms_out[3]);
+                const pt_options *opt, int64_t sample, void *stream, int32_t chosen[2],
+                double ms_out[9]);
 
 /* Streaming output: copies output rows [row0, row1) of every particle of a
  * device state(8,m,np) to host memory laid out (np, row1 - row0, 8), as one

@@ -48,6 +48,7 @@ class PtOptions(C.Structure):
         ("status", C.c_void_p), ("carry", C.c_void_p), ("model", C.c_void_p),
         ("records", C.c_void_p), ("record_capacity", C.c_int64), ("order", C.c_void_p),
         ("blocks_per_sm", C.c_int32), ("interpolation", C.c_int32),
+        ("threads_per_block", C.c_int32),
     ]
 
 
@@ -99,7 +100,7 @@ def load():
     L.pt_carry_bytes.restype = i64
     L.pt_run_device.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     L.pt_run_check.argtypes = [vp]
-    L.pt_autotune.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, i64, vp, C.POINTER(i32), vp]
+    L.pt_autotune.argtypes = [i32, i64, i32, vp, vp, vp, vp, vp, i64, vp, vp, vp]
     L.pt_ensemble_create.argtypes = [i32, i32, vp, vp, C.POINTER(vp)]
     L.pt_ensemble_destroy.argtypes = [vp]
     L.pt_ensemble_run.argtypes = [vp, d, vp]

@@ -114,6 +114,15 @@ void unpack_params(const double *p, const RunShape &g, PtRun &R)
  *     -> 2.91x / 3.50x / 3.43x / 3.32x / 2.86x / 2.24x at overshoot 3e-5. */
 static float g_face_skip[2] = { 0.1f, 0.01f }, g_face_over[2] = { 3.0e-5f, 3.0e-5f };
 
+/* pt_options.threads_per_block, read only from callers whose struct has it
+ * (struct_size 0 means the current layout). */
+int32_t pt_opt_threads_per_block(const pt_options *opt)
+{
+    if (!opt) return 0;
+    const int32_t need = (int32_t)(offsetof(pt_options, threads_per_block) + sizeof(int32_t));
+    return (opt->struct_size == 0 || opt->struct_size >= need) ? opt->threads_per_block : 0;
+}
+
 int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
                        const double *params, const pt_options *opt, PtRun &R)
 {
@@ -143,6 +152,9 @@ int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
             return set_err(PT_ERR_ARG, "negative record capacity%s");
         if (opt->blocks_per_sm != 0 && (opt->blocks_per_sm < 2 || opt->blocks_per_sm > 4))
             return set_err(PT_ERR_ARG, "blocks_per_sm must be 0, 2, 3 or 4%s");
+        const int32_t tpb = pt_opt_threads_per_block(opt);
+        if (tpb != 0 && tpb != 64 && tpb != 128 && tpb != 256)
+            return set_err(PT_ERR_ARG, "threads_per_block must be 0, 64, 128 or 256%s");
         if (opt->interpolation != 0 && opt->interpolation != 1)
             return set_err(PT_ERR_ARG, "interpolation must be 0 (trilinear) or 1 (nearest node)%s");
         if (opt->interpolation == 1 && (opt->controller & PT_CTL_LEARNED))
@@ -179,13 +191,15 @@ int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
         R.rec_cap = opt->record_capacity;
         R.order = opt->order;
         R.minb = opt->blocks_per_sm;
+        R.block = pt_opt_threads_per_block(opt);
         R.near = opt->interpolation;
     }
     return PT_OK;
 }
 
 /* Launch variants chosen by pt_autotune, per kernel family
- * [precision][method - 1][with J][learned]; 0 = not tuned. */
+ * [precision][method - 1][with J][learned]: blocks_per_sm | threads_per_block
+ * << 8; 0 = not tuned. */
 static std::atomic<int> g_tuned[4][2][2][2];
 
 std::atomic<int> &tuned_slot(int32_t method, const pt_fields *f, const PtRun &R)
@@ -244,9 +258,10 @@ int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
     R.carry = static_cast<unsigned char *>(d_carry);
     R.queue = f->scratch;
     R.flags = reinterpret_cast<int32_t *>(f->scratch + 1);
-    if (R.minb == 0) {
+    if (R.minb == 0 || R.block == 0) {
         const int t = tuned_slot(method, f, R).load(std::memory_order_relaxed);
-        R.minb = t ? t : PT_MINB_DEFAULT;
+        if (R.minb == 0) R.minb = (t & 0xff) ? (t & 0xff) : PT_MINB_DEFAULT;
+        if (R.block == 0) R.block = (t >> 8) ? (t >> 8) : PT_BLOCK_DEFAULT;
     }
 
     cudaError_t e;
@@ -265,8 +280,8 @@ int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f,
 
 extern "C" int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_fields *f,
                            const double params[17], const double *d_time, const double *d_state,
-                           const pt_options *opt, int64_t sample, void *stream, int32_t *chosen,
-                           double ms_out[3])
+                           const pt_options *opt, int64_t sample, void *stream, int32_t chosen[2],
+                           double ms_out[9])
 {
     if (!f) return set_err(PT_ERR_ARG, "fields handle is NULL%s");
     if (np < 1 || !d_time || !d_state) return set_err(PT_ERR_ARG, "autotune needs np >= 1 and buffers%s");
@@ -287,8 +302,9 @@ extern "C" int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_field
     int64_t *t_cnt = nullptr;
     float *t_rec = nullptr;            /* a record header with no room: counted, not written */
     cudaEvent_t ev[2] = { nullptr, nullptr };
-    double ms[3] = { 0, 0, 0 };
-    int best = 0;
+    static const int kBlocks[3] = { 64, 128, 256 };
+    double ms[9];
+    for (int v = 0; v < 9; ++v) ms[v] = -1.0;
     e = cudaMalloc(&t_state, (size_t)ns * mt * 8 * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&t_cnt, (size_t)ns * 3 * sizeof(int64_t));
     if (e == cudaSuccess && R.rec) e = cudaMalloc(&t_rec, 16);
@@ -309,25 +325,35 @@ extern "C" int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_field
     R.queue = f->scratch;
     R.flags = reinterpret_cast<int32_t *>(f->scratch + 1);
     if (!windowed && !(opt && opt->max_steps > 0)) R.max_steps = 32;
-    /* short attempt-capped trials get a warm-up round; window trials last
-     * long enough that the first launch's set-up does not matter */
-    for (int round = windowed ? 1 : 0; round < 2 && e == cudaSuccess; ++round) {
-        for (int v = 0; v < 3 && e == cudaSuccess; ++v) {
-            R.minb = 2 + v;
-            e = cudaMemcpy2DAsync(t_state, (size_t)mt * 64, d_state, (size_t)m * 64, 64, (size_t)ns,
-                                  cudaMemcpyDeviceToDevice, s);
-            if (e == cudaSuccess) e = cudaMemsetAsync(f->scratch, 0, 3 * sizeof(unsigned long long), s);
-            if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
-            if (e == cudaSuccess) e = launch_run(method, f, R, s);
-            if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
-            if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
-            float t = 0.0f;
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
-            if (e == cudaSuccess && round == 1) {
-                ms[v] = t;
-                if (ms[v] < ms[best]) best = v;
-            }
-        }
+    /* One trial of variant (minb, block index) on fresh copies of the states. */
+    auto trial = [&](int minb, int bi, bool keep) {
+        R.minb = minb;
+        R.block = kBlocks[bi];
+        e = cudaMemcpy2DAsync(t_state, (size_t)mt * 64, d_state, (size_t)m * 64, 64, (size_t)ns,
+                              cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(f->scratch, 0, 3 * sizeof(unsigned long long), s);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
+        if (e == cudaSuccess) e = launch_run(method, f, R, s);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
+        if (e == cudaSuccess) e = cudaEventSynchronize(ev[1]);
+        float t = 0.0f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev[0], ev[1]);
+        if (e == cudaSuccess && keep) ms[(minb - 2) * 3 + bi] = t;
+    };
+    /* Coordinate search: the register cap (2, 3, 4 resident 128-thread
+     * blocks) at 128 threads per block, then 64 and 256 threads per block at
+     * the best cap.  Short attempt-capped trials get a warm-up round; window
+     * trials last long enough that the first launch's set-up does not
+     * matter. */
+    int best_m = 3, best_b = 1;
+    for (int round = windowed ? 1 : 0; round < 2 && e == cudaSuccess; ++round)
+        for (int v = 0; v < 3 && e == cudaSuccess; ++v) trial(2 + v, 1, round == 1);
+    for (int v = 0; v < 3; ++v)
+        if (ms[v * 3 + 1] >= 0.0 && ms[v * 3 + 1] < ms[(best_m - 2) * 3 + 1]) best_m = 2 + v;
+    for (int bi = 0; bi < 3 && e == cudaSuccess; bi += 2) trial(best_m, bi, true);
+    for (int bi = 0; bi < 3; ++bi) {
+        const double t = ms[(best_m - 2) * 3 + bi];
+        if (t >= 0.0 && t < ms[(best_m - 2) * 3 + best_b]) best_b = bi;
     }
     if (ev[0]) cudaEventDestroy(ev[0]);
     if (ev[1]) cudaEventDestroy(ev[1]);
@@ -336,10 +362,13 @@ extern "C" int pt_autotune(int32_t method, int64_t np, int32_t m, const pt_field
     cudaFree(t_rec);
     if (e != cudaSuccess) return cuda_err(e, "pt_autotune");
     R.minb = 0;
-    tuned_slot(method, f, R).store(2 + best, std::memory_order_relaxed);
-    if (chosen) *chosen = 2 + best;
+    tuned_slot(method, f, R).store(best_m | (kBlocks[best_b] << 8), std::memory_order_relaxed);
+    if (chosen) {
+        chosen[0] = best_m;
+        chosen[1] = kBlocks[best_b];
+    }
     if (ms_out)
-        for (int v = 0; v < 3; ++v) ms_out[v] = ms[v];
+        for (int v = 0; v < 9; ++v) ms_out[v] = ms[v];
     return PT_OK;
 }
 

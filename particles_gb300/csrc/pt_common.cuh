@@ -64,7 +64,9 @@ struct PtRun {
     int64_t rec_cap;       /* record capacity */
     unsigned long long *queue;  /* work-queue head */
     int32_t *flags;        /* [0] time budget hit, [1] particles with negative status */
-    int32_t minb;          /* launch variant: resident blocks per SM (2, 3 or 4) */
+    int32_t minb;          /* launch variant: register cap of 2, 3 or 4 resident 128-thread
+                              blocks per SM (255, 168, 128 registers) */
+    int32_t block;         /* threads per block: 64, 128 or 256 (0 = 128) */
     unsigned long long *oob;  /* checked builds: count of out-of-range record indices */
     int64_t nrec;          /* records of the field store (index bound of the gathers) */
     int32_t *work;         /* per particle: attempts made in this run, or NULL */
@@ -72,11 +74,18 @@ struct PtRun {
     const double *tstop;   /* ensembles: device window end (else tend) */
 };
 
-/* Launch variant of an integrator: the same kernel compiled for 2, 3 or 4
- * resident 128-thread blocks per SM.  The register cap (255 / 168 / 128) is
- * the trade: more blocks hide more latency, fewer avoid spills (the learned
- * controller's MLP, DOP853's k rows in flight).  Results do not depend on it. */
+/* Launch variant of an integrator: the same kernel compiled with the
+ * register cap of 2, 3 or 4 resident 128-thread blocks per SM (255 / 168 /
+ * 128 registers, __maxnreg__), launched with 64, 128 or 256 threads per
+ * block (one particle per lane; the k rows in shared memory scale with the
+ * block).  The register cap is the trade: more resident warps hide more
+ * latency, fewer avoid spills (the learned controller's MLP, DOP853's k rows
+ * in flight); the block size sets how shared memory and the register file
+ * are carved into blocks.  Results do not depend on either. */
 #define PT_MINB_DEFAULT 3
+#define PT_BLOCK_DEFAULT 128
+#define PT_BLOCK_MAX 256
+#define PT_REGS_OF_MINB(b) ((b) == 2 ? 255 : (b) == 3 ? 168 : 128)
 
 /* Carry (controller memory) SoA layout inside one buffer of 128*np bytes:
  *   double t[np], dt[np], errold[np], si[6][np], k1[6][np]; int32 n[np], flags[np]
@@ -215,25 +224,25 @@ struct PtLaunch {
                                       const double *vec, double *acc, cudaStream_t s); \
     cudaError_t pt_launch_echo_##sfx(const PtRun &P, double *out, cudaStream_t s);    \
     cudaError_t pt_launch_rk5_ens_##sfx(const PtRun *tab, int nmem, int nc, int minb, \
-                                        int64_t ntot, cudaStream_t s);              \
+                                        int block, int64_t ntot, cudaStream_t s);   \
     cudaError_t pt_launch_dp853_ens_##sfx(const PtRun *tab, int nmem, int nc, int minb, \
-                                          int64_t ntot, cudaStream_t s);
+                                          int block, int64_t ntot, cudaStream_t s);
 
 PT_DECLARE_FP64_LAUNCHERS(exact)
 PT_DECLARE_FP64_LAUNCHERS(fma)
 
 cudaError_t pt_launch_rk5_mixed(const PtRun &P, int nc, cudaStream_t s);
-cudaError_t pt_launch_rk5_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
-                                    cudaStream_t s);
-cudaError_t pt_launch_dp853_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
-                                      cudaStream_t s);
+cudaError_t pt_launch_rk5_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int block,
+                                    int64_t ntot, cudaStream_t s);
+cudaError_t pt_launch_dp853_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int block,
+                                      int64_t ntot, cudaStream_t s);
 cudaError_t pt_launch_dp853_mixed(const PtRun &P, int nc, cudaStream_t s);
 cudaError_t pt_launch_rk5_bf16(const PtRun &P, int nc, cudaStream_t s);
 cudaError_t pt_launch_dp853_bf16(const PtRun &P, int nc, cudaStream_t s);
-cudaError_t pt_launch_rk5_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
-                                   cudaStream_t s);
-cudaError_t pt_launch_dp853_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
-                                     cudaStream_t s);
+cudaError_t pt_launch_rk5_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int block,
+                                   int64_t ntot, cudaStream_t s);
+cudaError_t pt_launch_dp853_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int block,
+                                     int64_t ntot, cudaStream_t s);
 cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int brick, int64_t n, const double *vec,
                                   double *acc, cudaStream_t s);
 

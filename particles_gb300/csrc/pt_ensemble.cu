@@ -34,7 +34,7 @@ struct EnsBufs {
 };
 
 struct pt_ensemble {
-    int32_t method, precision, nc, nmem, minb, device;
+    int32_t method, precision, nc, nmem, minb, block, device;
     int64_t ntot, npmax;
     PtRun *d_tab;
     double *d_tstop;
@@ -195,19 +195,19 @@ static cudaError_t ens_launch(const pt_ensemble *e, int64_t ntot, cudaStream_t s
 {
     if (e->precision == PT_PREC_FP64)
         return e->method == PT_METHOD_RK5
-                   ? pt_launch_rk5_ens_exact(e->d_tab, e->nmem, e->nc, e->minb, ntot, s)
-                   : pt_launch_dp853_ens_exact(e->d_tab, e->nmem, e->nc, e->minb, ntot, s);
+                   ? pt_launch_rk5_ens_exact(e->d_tab, e->nmem, e->nc, e->minb, e->block, ntot, s)
+                   : pt_launch_dp853_ens_exact(e->d_tab, e->nmem, e->nc, e->minb, e->block, ntot, s);
     if (e->precision == PT_PREC_FP64_FMA)
         return e->method == PT_METHOD_RK5
-                   ? pt_launch_rk5_ens_fma(e->d_tab, e->nmem, e->nc, e->minb, ntot, s)
-                   : pt_launch_dp853_ens_fma(e->d_tab, e->nmem, e->nc, e->minb, ntot, s);
+                   ? pt_launch_rk5_ens_fma(e->d_tab, e->nmem, e->nc, e->minb, e->block, ntot, s)
+                   : pt_launch_dp853_ens_fma(e->d_tab, e->nmem, e->nc, e->minb, e->block, ntot, s);
     if (e->precision == PT_PREC_BF16)
         return e->method == PT_METHOD_RK5
-                   ? pt_launch_rk5_ens_bf16(e->d_tab, e->nmem, e->nc, e->minb, ntot, s)
-                   : pt_launch_dp853_ens_bf16(e->d_tab, e->nmem, e->nc, e->minb, ntot, s);
+                   ? pt_launch_rk5_ens_bf16(e->d_tab, e->nmem, e->nc, e->minb, e->block, ntot, s)
+                   : pt_launch_dp853_ens_bf16(e->d_tab, e->nmem, e->nc, e->minb, e->block, ntot, s);
     return e->method == PT_METHOD_RK5
-               ? pt_launch_rk5_ens_mixed(e->d_tab, e->nmem, e->nc, e->minb, ntot, s)
-               : pt_launch_dp853_ens_mixed(e->d_tab, e->nmem, e->nc, e->minb, ntot, s);
+               ? pt_launch_rk5_ens_mixed(e->d_tab, e->nmem, e->nc, e->minb, e->block, ntot, s)
+               : pt_launch_dp853_ens_mixed(e->d_tab, e->nmem, e->nc, e->minb, e->block, ntot, s);
 }
 
 static cudaError_t ens_window(pt_ensemble *e, cudaStream_t s)
@@ -269,6 +269,7 @@ extern "C" int pt_ensemble_create(int32_t method, int32_t nmembers, const pt_mem
         o.eta = M.eta;
         o.time_budget_s = opt ? opt->time_budget_s : 0.0;
         o.blocks_per_sm = opt ? opt->blocks_per_sm : 0;
+        o.threads_per_block = pt_opt_threads_per_block(opt);
         o.interpolation = opt ? opt->interpolation : 0;
         o.controller = opt ? opt->controller : 0;
         int rc = prepare_run(method, M.np, M.m, shape_of(M.fields), M.params, &o, tab[k]);
@@ -299,7 +300,10 @@ extern "C" int pt_ensemble_create(int32_t method, int32_t nmembers, const pt_mem
     {   /* launch variant: as requested, else tuned for the single-run kernel, else default */
         PtRun probe = tab[0];
         const int t = tuned_slot(method, f0, probe).load(std::memory_order_relaxed);
-        e->minb = (opt && opt->blocks_per_sm) ? opt->blocks_per_sm : (t ? t : PT_MINB_DEFAULT);
+        e->minb = (opt && opt->blocks_per_sm) ? opt->blocks_per_sm
+                                              : ((t & 0xff) ? (t & 0xff) : PT_MINB_DEFAULT);
+        const int32_t tpb = pt_opt_threads_per_block(opt);
+        e->block = tpb ? tpb : ((t >> 8) ? (t >> 8) : PT_BLOCK_DEFAULT);
     }
     int64_t off = 0;
     for (int k = 0; k < nmembers; ++k) {
@@ -322,6 +326,7 @@ extern "C" int pt_ensemble_create(int32_t method, int32_t nmembers, const pt_mem
         R.flags = e->d_flags;
         R.oob = reinterpret_cast<unsigned long long *>(e->d_flags + 2);
         R.minb = e->minb;
+        R.block = e->block;
         off += 4 * M.np;
     }
     err = cudaMemcpy(e->d_tab, tab, sizeof(PtRun) * nmembers, cudaMemcpyHostToDevice);

@@ -42,7 +42,6 @@
 #define PT_CAT(a, b) PT_CAT2(a, b)
 #define PT_NAME(x) PT_CAT(x, PT_SFX)
 
-#define PT_BLOCK 128
 
 namespace {
 
@@ -174,7 +173,8 @@ struct EvalF64 {
 };
 
 template <int METHOD, int NC, bool LEARN, int MINB>
-__global__ void __launch_bounds__(PT_BLOCK, MINB) k_integrate(const PtRun P)
+__global__ void __launch_bounds__(PT_BLOCK_MAX) __maxnreg__(PT_REGS_OF_MINB(MINB))
+k_integrate(const PtRun P)
 {
     pt_sm::run_machine<METHOD, EvalF64<NC>, LEARN>(pt_sm::Members<false>{ P });
 }
@@ -182,7 +182,8 @@ __global__ void __launch_bounds__(PT_BLOCK, MINB) k_integrate(const PtRun P)
 /* Several runs (members: snapshots, tolerances, particle sets) in one
  * persistent launch; every lane drains the members' queues in table order. */
 template <int METHOD, int NC, int MINB>
-__global__ void __launch_bounds__(PT_BLOCK, MINB) k_ensemble(const PtRun *__restrict__ tab, int nmem)
+__global__ void __launch_bounds__(PT_BLOCK_MAX) __maxnreg__(PT_REGS_OF_MINB(MINB))
+k_ensemble(const PtRun *__restrict__ tab, int nmem)
 {
     __shared__ PtRun sP[PT_ENS_MAX];
     __shared__ int64_t sN[PT_ENS_MAX];
@@ -224,29 +225,33 @@ cudaError_t launch1(const PtRun &P, cudaStream_t s)
 {
     static int cache[2][2] = { { -1, 1 }, { -1, 1 } };  /* without / with recording */
     const bool rec = LEARN && P.rec != nullptr, mlp = LEARN && P.mlp != nullptr;
-    return pt_sm::launch_persistent(k_integrate<METHOD, NC, LEARN, MINB>, PT_BLOCK,
-                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK, rec, mlp),
-                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK, true, LEARN), cache[rec], P.np, s,
-                                    P);
+    const int block = P.block ? P.block : PT_BLOCK_DEFAULT;
+    return pt_sm::launch_persistent(k_integrate<METHOD, NC, LEARN, MINB>, block,
+                                    pt_sm::smem_bytes<METHOD>(block, rec, mlp),
+                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK_MAX, true, LEARN), cache[rec],
+                                    P.np, s, P);
 }
 
 template <int METHOD, int NC, int MINB>
-cudaError_t launch_ens1(const PtRun *tab, int nmem, int64_t ntot, cudaStream_t s)
+cudaError_t launch_ens1(const PtRun *tab, int nmem, int block, int64_t ntot, cudaStream_t s)
 {
     static int cache[2] = { -1, 1 };
-    const int smem = pt_sm::smem_bytes<METHOD>(PT_BLOCK, false);
-    return pt_sm::launch_persistent(k_ensemble<METHOD, NC, MINB>, PT_BLOCK, smem, smem, cache, ntot, s,
+    const int smem = pt_sm::smem_bytes<METHOD>(block, false);
+    return pt_sm::launch_persistent(k_ensemble<METHOD, NC, MINB>, block, smem,
+                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK_MAX, false), cache, ntot, s,
                                     tab, nmem);
 }
 
 template <int METHOD, int NC>
-cudaError_t launch_ens(const PtRun *tab, int nmem, int minb, int64_t ntot, cudaStream_t s)
+cudaError_t launch_ens(const PtRun *tab, int nmem, int minb, int block, int64_t ntot,
+                       cudaStream_t s)
 {
     if (ntot == 0) return cudaSuccess;          /* ntot < 0: configure only */
+    if (!block) block = PT_BLOCK_DEFAULT;
     switch (minb) {
-    case 2: return launch_ens1<METHOD, NC, 2>(tab, nmem, ntot, s);
-    case 4: return launch_ens1<METHOD, NC, 4>(tab, nmem, ntot, s);
-    default: return launch_ens1<METHOD, NC, 3>(tab, nmem, ntot, s);
+    case 2: return launch_ens1<METHOD, NC, 2>(tab, nmem, block, ntot, s);
+    case 4: return launch_ens1<METHOD, NC, 4>(tab, nmem, block, ntot, s);
+    default: return launch_ens1<METHOD, NC, 3>(tab, nmem, block, ntot, s);
     }
 }
 
@@ -277,11 +282,11 @@ cudaError_t PT_NAME(pt_launch_rk5)(const PtRun &P, int nc, cudaStream_t s)
     return nc == 10 ? launch<PT_METHOD_RK5, 10>(P, s) : launch<PT_METHOD_RK5, 6>(P, s);
 }
 
-cudaError_t PT_NAME(pt_launch_rk5_ens)(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
-                                       cudaStream_t s)
+cudaError_t PT_NAME(pt_launch_rk5_ens)(const PtRun *tab, int nmem, int nc, int minb, int block,
+                                       int64_t ntot, cudaStream_t s)
 {
-    return nc == 10 ? launch_ens<PT_METHOD_RK5, 10>(tab, nmem, minb, ntot, s)
-                    : launch_ens<PT_METHOD_RK5, 6>(tab, nmem, minb, ntot, s);
+    return nc == 10 ? launch_ens<PT_METHOD_RK5, 10>(tab, nmem, minb, block, ntot, s)
+                    : launch_ens<PT_METHOD_RK5, 6>(tab, nmem, minb, block, ntot, s);
 }
 #endif
 
@@ -291,11 +296,11 @@ cudaError_t PT_NAME(pt_launch_dp853)(const PtRun &P, int nc, cudaStream_t s)
     return nc == 10 ? launch<PT_METHOD_DOP853, 10>(P, s) : launch<PT_METHOD_DOP853, 6>(P, s);
 }
 
-cudaError_t PT_NAME(pt_launch_dp853_ens)(const PtRun *tab, int nmem, int nc, int minb,
+cudaError_t PT_NAME(pt_launch_dp853_ens)(const PtRun *tab, int nmem, int nc, int minb, int block,
                                          int64_t ntot, cudaStream_t s)
 {
-    return nc == 10 ? launch_ens<PT_METHOD_DOP853, 10>(tab, nmem, minb, ntot, s)
-                    : launch_ens<PT_METHOD_DOP853, 6>(tab, nmem, minb, ntot, s);
+    return nc == 10 ? launch_ens<PT_METHOD_DOP853, 10>(tab, nmem, minb, block, ntot, s)
+                    : launch_ens<PT_METHOD_DOP853, 6>(tab, nmem, minb, block, ntot, s);
 }
 #endif
 

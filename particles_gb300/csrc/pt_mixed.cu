@@ -37,7 +37,6 @@
 #include "pt_convert.cuh"
 #include "pt_integrator.cuh"
 
-#define PT_BLOCK 128
 #ifndef PT_PART
 #define PT_PART 0
 #endif
@@ -314,7 +313,8 @@ struct EvalMixed {
 };
 
 template <int METHOD, class EV, bool LEARN, int MINB>
-__global__ void __launch_bounds__(PT_BLOCK, MINB) k_integrate_mixed(const PtRun P)
+__global__ void __launch_bounds__(PT_BLOCK_MAX) __maxnreg__(PT_REGS_OF_MINB(MINB))
+k_integrate_mixed(const PtRun P)
 {
     pt_sm::run_machine<METHOD, EV, LEARN>(pt_sm::Members<false>{ P });
 }
@@ -322,7 +322,8 @@ __global__ void __launch_bounds__(PT_BLOCK, MINB) k_integrate_mixed(const PtRun 
 /* Several runs (members: snapshots, tolerances, particle sets) in one
  * persistent launch; every lane drains the members' queues in table order. */
 template <int METHOD, class EV, int MINB>
-__global__ void __launch_bounds__(PT_BLOCK, MINB) k_ensemble_mixed(const PtRun *__restrict__ tab, int nmem)
+__global__ void __launch_bounds__(PT_BLOCK_MAX) __maxnreg__(PT_REGS_OF_MINB(MINB))
+k_ensemble_mixed(const PtRun *__restrict__ tab, int nmem)
 {
     __shared__ PtRun sP[PT_ENS_MAX];
     __shared__ int64_t sN[PT_ENS_MAX];
@@ -352,29 +353,34 @@ cudaError_t launch1(const PtRun &P, cudaStream_t s)
 {
     static int cache[2][2] = { { -1, 1 }, { -1, 1 } };  /* without / with recording */
     const bool rec = LEARN && P.rec != nullptr, mlp = LEARN && P.mlp != nullptr;
-    return pt_sm::launch_persistent(k_integrate_mixed<METHOD, EV, LEARN, MINB>, PT_BLOCK,
-                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK, rec, mlp),
-                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK, true, LEARN), cache[rec], P.np, s,
+    const int block = P.block ? P.block : PT_BLOCK_DEFAULT;
+    return pt_sm::launch_persistent(k_integrate_mixed<METHOD, EV, LEARN, MINB>, block,
+                                    pt_sm::smem_bytes<METHOD>(block, rec, mlp),
+                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK_MAX, true, LEARN), cache[rec],
+                                    P.np, s,
                                     P);
 }
 
 template <int METHOD, class EV, int MINB>
-cudaError_t launch_ens1(const PtRun *tab, int nmem, int64_t ntot, cudaStream_t s)
+cudaError_t launch_ens1(const PtRun *tab, int nmem, int block, int64_t ntot, cudaStream_t s)
 {
     static int cache[2] = { -1, 1 };
-    const int smem = pt_sm::smem_bytes<METHOD>(PT_BLOCK, false);
-    return pt_sm::launch_persistent(k_ensemble_mixed<METHOD, EV, MINB>, PT_BLOCK, smem, smem, cache,
+    const int smem = pt_sm::smem_bytes<METHOD>(block, false);
+    return pt_sm::launch_persistent(k_ensemble_mixed<METHOD, EV, MINB>, block, smem,
+                                    pt_sm::smem_bytes<METHOD>(PT_BLOCK_MAX, false), cache,
                                     ntot, s, tab, nmem);
 }
 
 template <int METHOD, class EV>
-cudaError_t launch_ens(const PtRun *tab, int nmem, int minb, int64_t ntot, cudaStream_t s)
+cudaError_t launch_ens(const PtRun *tab, int nmem, int minb, int block, int64_t ntot,
+                       cudaStream_t s)
 {
     if (ntot == 0) return cudaSuccess;          /* ntot < 0: configure only */
+    if (!block) block = PT_BLOCK_DEFAULT;
     switch (minb) {
-    case 2: return launch_ens1<METHOD, EV, 2>(tab, nmem, ntot, s);
-    case 4: return launch_ens1<METHOD, EV, 4>(tab, nmem, ntot, s);
-    default: return launch_ens1<METHOD, EV, 3>(tab, nmem, ntot, s);
+    case 2: return launch_ens1<METHOD, EV, 2>(tab, nmem, block, ntot, s);
+    case 4: return launch_ens1<METHOD, EV, 4>(tab, nmem, block, ntot, s);
+    default: return launch_ens1<METHOD, EV, 3>(tab, nmem, block, ntot, s);
     }
 }
 
@@ -412,11 +418,11 @@ cudaError_t pt_launch_rk5_mixed(const PtRun &P, int nc, cudaStream_t s)
     return nc == 16 ? launch<PT_METHOD_RK5, F32_16, true>(P, s) : launch<PT_METHOD_RK5, F32_8, true>(P, s);
 }
 
-cudaError_t pt_launch_rk5_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
-                                    cudaStream_t s)
+cudaError_t pt_launch_rk5_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int block,
+                                    int64_t ntot, cudaStream_t s)
 {
-    return nc == 16 ? launch_ens<PT_METHOD_RK5, F32_16>(tab, nmem, minb, ntot, s)
-                    : launch_ens<PT_METHOD_RK5, F32_8>(tab, nmem, minb, ntot, s);
+    return nc == 16 ? launch_ens<PT_METHOD_RK5, F32_16>(tab, nmem, minb, block, ntot, s)
+                    : launch_ens<PT_METHOD_RK5, F32_8>(tab, nmem, minb, block, ntot, s);
 }
 
 cudaError_t pt_launch_rk5_bf16(const PtRun &P, int nc, cudaStream_t s)
@@ -424,11 +430,11 @@ cudaError_t pt_launch_rk5_bf16(const PtRun &P, int nc, cudaStream_t s)
     return nc == 16 ? launch<PT_METHOD_RK5, B16_16, true>(P, s) : launch<PT_METHOD_RK5, B16_8, true>(P, s);
 }
 
-cudaError_t pt_launch_rk5_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
-                                   cudaStream_t s)
+cudaError_t pt_launch_rk5_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int block,
+                                   int64_t ntot, cudaStream_t s)
 {
-    return nc == 16 ? launch_ens<PT_METHOD_RK5, B16_16>(tab, nmem, minb, ntot, s)
-                    : launch_ens<PT_METHOD_RK5, B16_8>(tab, nmem, minb, ntot, s);
+    return nc == 16 ? launch_ens<PT_METHOD_RK5, B16_16>(tab, nmem, minb, block, ntot, s)
+                    : launch_ens<PT_METHOD_RK5, B16_8>(tab, nmem, minb, block, ntot, s);
 }
 #endif
 
@@ -439,11 +445,11 @@ cudaError_t pt_launch_dp853_mixed(const PtRun &P, int nc, cudaStream_t s)
                     : launch<PT_METHOD_DOP853, F32_8, true>(P, s);
 }
 
-cudaError_t pt_launch_dp853_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
-                                      cudaStream_t s)
+cudaError_t pt_launch_dp853_ens_mixed(const PtRun *tab, int nmem, int nc, int minb, int block,
+                                      int64_t ntot, cudaStream_t s)
 {
-    return nc == 16 ? launch_ens<PT_METHOD_DOP853, F32_16>(tab, nmem, minb, ntot, s)
-                    : launch_ens<PT_METHOD_DOP853, F32_8>(tab, nmem, minb, ntot, s);
+    return nc == 16 ? launch_ens<PT_METHOD_DOP853, F32_16>(tab, nmem, minb, block, ntot, s)
+                    : launch_ens<PT_METHOD_DOP853, F32_8>(tab, nmem, minb, block, ntot, s);
 }
 
 cudaError_t pt_launch_dp853_bf16(const PtRun &P, int nc, cudaStream_t s)
@@ -452,11 +458,11 @@ cudaError_t pt_launch_dp853_bf16(const PtRun &P, int nc, cudaStream_t s)
                     : launch<PT_METHOD_DOP853, B16_8, true>(P, s);
 }
 
-cudaError_t pt_launch_dp853_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int64_t ntot,
-                                     cudaStream_t s)
+cudaError_t pt_launch_dp853_ens_bf16(const PtRun *tab, int nmem, int nc, int minb, int block,
+                                     int64_t ntot, cudaStream_t s)
 {
-    return nc == 16 ? launch_ens<PT_METHOD_DOP853, B16_16>(tab, nmem, minb, ntot, s)
-                    : launch_ens<PT_METHOD_DOP853, B16_8>(tab, nmem, minb, ntot, s);
+    return nc == 16 ? launch_ens<PT_METHOD_DOP853, B16_16>(tab, nmem, minb, block, ntot, s)
+                    : launch_ens<PT_METHOD_DOP853, B16_8>(tab, nmem, minb, block, ntot, s);
 }
 #endif
 

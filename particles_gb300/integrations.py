@@ -48,7 +48,8 @@ def _f64(a):
 
 def _options(precision, *, eta=0.0, jj=None, open_x=False, max_steps=0, t_stop=0.0,
              status=None, carry=None, time_budget_s=0.0, model=None, records=None,
-             order=None, blocks_per_sm=0, interpolation=0, face_steps=False):
+             order=None, blocks_per_sm=0, interpolation=0, face_steps=False,
+             threads_per_block=0):
     o = N.PtOptions()
     o.struct_size = C.sizeof(N.PtOptions)
     o.precision = N.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
@@ -69,6 +70,7 @@ def _options(precision, *, eta=0.0, jj=None, open_x=False, max_steps=0, t_stop=0
     o.status = _ptr(status)
     o.carry = _ptr(carry)
     o.blocks_per_sm = int(blocks_per_sm)
+    o.threads_per_block = int(threads_per_block)
     o.interpolation = INTERPOLATIONS[interpolation] if isinstance(interpolation, str) else int(interpolation)
     return o
 
@@ -188,12 +190,13 @@ class Fields:
     def run_device(self, method, params, d_time, d_state, d_cnt, d_status=None, d_carry=None,
                    *, eta=0.0, open_x=False, max_steps=0, t_stop=0.0, time_budget_s=0.0,
                    stream=0, model=None, records=None, order=None, blocks_per_sm=0,
-                   interpolation="linear", face_steps=False):
+                   interpolation="linear", face_steps=False, threads_per_block=0):
         """Launch on device tensors (torch); returns without synchronising.
 
         model: a learned.Model for the learned controller; records: a device
         record buffer (learned.record_buffer); order: device int32 queue order;
-        blocks_per_sm: launch variant (0 = tuned or default, else 2, 3, 4);
+        blocks_per_sm: register cap (0 = tuned or default, else 2, 3, 4 resident
+        128-thread blocks); threads_per_block: 0 (tuned or 128), 64, 128 or 256;
         face_steps: trial steps end just past the next cell face (PT_CTL_FACE,
         not with precision "fp64").
         """
@@ -201,6 +204,7 @@ class Fields:
         opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
                        t_stop=t_stop, time_budget_s=time_budget_s, model=model,
                        records=records, order=order, blocks_per_sm=blocks_per_sm,
+                       threads_per_block=threads_per_block,
                        interpolation=interpolation, face_steps=face_steps)
         rc = self._L.pt_run_device(
             method_id(method), npart, m, self._h, _ptr(_f64(params)),
@@ -219,19 +223,21 @@ class Fields:
 
         t_stop > 0 times a real window up to t_stop (else max_steps attempts);
         sample: particles in the trial (0 default, -1 all).
-        Returns (blocks_per_sm, {variant: trial ms})."""
+        Returns ((blocks_per_sm, threads_per_block), {(blocks_per_sm,
+        threads_per_block): trial ms}) over the variants tried."""
         npart, m, _ = d_state.shape
         opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
                        t_stop=t_stop, model=model, records=records, interpolation=interpolation,
                        face_steps=face_steps)
-        chosen = C.c_int32(0)
-        ms = np.zeros(3, np.float64)
+        chosen = (C.c_int32 * 2)()
+        ms = np.zeros(9, np.float64)
         rc = self._L.pt_autotune(method_id(method), npart, m, self._h, _ptr(_f64(params)),
                                  C.c_void_p(d_time.data_ptr()), C.c_void_p(d_state.data_ptr()),
                                  C.byref(opt), int(sample), _stream(stream, d_state),
-                                 C.byref(chosen), _ptr(ms))
+                                 chosen, _ptr(ms))
         N.check(rc, "pt_autotune")
-        return int(chosen.value), {2 + i: float(ms[i]) for i in range(3)}
+        tried = {(2 + i // 3, (64, 128, 256)[i % 3]): float(ms[i]) for i in range(9) if ms[i] >= 0}
+        return (int(chosen[0]), int(chosen[1])), tried
 
     def run_check(self) -> int:
         return int(self._L.pt_run_check(self._h))

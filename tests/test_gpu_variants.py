@@ -1,8 +1,9 @@
-"""Launch variants (blocks_per_sm 2, 3, 4) and the autotuner (pt_autotune).
+"""Launch variants (register cap of blocks_per_sm 2, 3, 4; 64, 128 or 256
+threads per block) and the autotuner (pt_autotune).
 
-A variant changes only the register cap the kernel is compiled for, so the
-exact FP64 kernel stays bit-identical to the oracle in every variant, and the
-autotuner's choice changes no result.
+A variant changes only the register cap the kernel is compiled for and how
+lanes are grouped into blocks, so the exact FP64 kernel stays bit-identical
+to the oracle in every variant, and the autotuner's choice changes no result.
 """
 import numpy as np
 import pytest
@@ -34,10 +35,11 @@ def test_exact_variants_bitwise(cuda, oracle_lib, method):
     so, co, _ = oracle.integrate(method, prob["params"], prob["time"], uu, bb, prob["state"].copy())
     f = Fields(uu, bb)
     for v in (2, 3, 4):
-        s, c, st = _run(torch, f, prob, blocks_per_sm=v)
-        assert (st == 0).all()
-        assert np.array_equal(c, co), v
-        assert np.array_equal(s, so), v
+        for tpb in (64, 128, 256):
+            s, c, st = _run(torch, f, prob, blocks_per_sm=v, threads_per_block=tpb)
+            assert (st == 0).all()
+            assert np.array_equal(c, co), (v, tpb)
+            assert np.array_equal(s, so), (v, tpb)
 
 
 def test_mixed_learned_variants_agree(cuda):
@@ -72,9 +74,10 @@ def test_autotune_choice_keeps_results(cuda, oracle_lib, precision):
     before = d_state.clone()
     v, ms = f.autotune("dop853", prob["params"], d_time, d_state, max_steps=16)
     print("autotune", precision, v, ms)
-    assert v in (2, 3, 4)
-    assert all(t > 0.0 for t in ms.values())
-    assert ms[v] == min(ms.values())
+    assert v[0] in (2, 3, 4) and v[1] in (64, 128, 256)
+    assert len(ms) == 5 and all(t > 0.0 for t in ms.values())
+    assert {b for b, t in ms if t == 128} == {2, 3, 4}
+    assert ms[v] == min(t for (b, tpb), t in ms.items() if b == v[0])
     assert torch.equal(d_state, before)                  # the input is only read
     s, c, st = _run(torch, f, prob)                      # default = the tuned variant
     assert np.array_equal(c, ref[1]) and np.array_equal(s, ref[0])

@@ -72,8 +72,9 @@ def test_argument_errors_need_no_gpu(native):
 
 def test_options_struct_layout():
     from particles_gb300 import _native as N
-    assert C.sizeof(N.PtOptions) == 112
+    assert C.sizeof(N.PtOptions) == 120
     assert N.PtOptions.max_steps.offset == 16 and N.PtOptions.carry.offset == 64
+    assert N.PtOptions.threads_per_block.offset == 112
 
 
 def test_launch_variant_option_checked_on_host(native):
@@ -92,6 +93,14 @@ def test_launch_variant_option_checked_on_host(native):
         o.blocks_per_sm = v
         assert native.pt_debug_unpack(1, 4, 2, ptr(dm), 0, 0, ptr(p), C.byref(o), ptr(out)) == rc
     assert native.pt_autotune(1, 4, 2, None, ptr(p), None, None, None, 0, None, None, None) == N.PT_ERR_ARG
+    # threads per block: 0 (tuned or 128), 64, 128, 256; read only when the
+    # caller's struct_size covers the field (an older, shorter struct leaves it out)
+    for t, size, rc in ((0, 0, N.PT_OK), (64, 0, N.PT_OK), (256, 120, N.PT_OK),
+                        (96, 120, N.PT_ERR_ARG), (512, 0, N.PT_ERR_ARG), (96, 112, N.PT_OK)):
+        o = N.PtOptions()
+        o.struct_size = size
+        o.threads_per_block = t
+        assert native.pt_debug_unpack(1, 4, 2, ptr(dm), 0, 0, ptr(p), C.byref(o), ptr(out)) == rc
 
 
 def test_ensemble_argument_errors_need_no_gpu(native):
@@ -113,7 +122,7 @@ def test_ensemble_argument_errors_need_no_gpu(native):
 def test_interpolation_option_checked_on_host(native):
     from particles_gb300 import _native as N
     from particles_gb300.params import pack_params
-    assert N.PtOptions.interpolation.offset == 108 and C.sizeof(N.PtOptions) == 112
+    assert N.PtOptions.interpolation.offset == 108 and C.sizeof(N.PtOptions) == 120
     dm = np.array([8, 8, 8], np.int32)
     p = pack_params(qom=1.0, vunit=0.1, tmax=1.0)
     out = np.zeros(8)
