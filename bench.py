@@ -133,9 +133,10 @@ def parse():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-controller leg")
     ap.add_argument("--no-order", action="store_true",
                     help="keep the natural queue order (default: longest first)")
-    ap.add_argument("--order", choices=["work", "brick"], default="work",
+    ap.add_argument("--order", choices=["work", "brick"], default="brick",
                     help="queue order: longest first (work), or longest-first classes "
-                         "sorted inside by the Morton index of the particle's cell (brick)")
+                         "sorted inside by the Morton index of the particle's cell (brick; "
+                         "+5-17 %% accepted steps/s for the mixed-precision kernels)")
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble leg")
     ap.add_argument("--ensemble-precision", choices=["fp64", "fp64_fma", "fp32"], default="fp64")
     ap.add_argument("--no-face-ensemble", action="store_true",

@@ -97,7 +97,7 @@ typedef struct pt_options {
                                      when controller has PT_CTL_LEARNED */
     void         *records;        /* device buffer for accepted-step records (pt_run_device
                                      only): a 16-byte header whose first 8 bytes count the
-                                     records, then records of 10 floats each */
+                                     records, then records of 11 floats each */
     int64_t       record_capacity;/* records that fit after the header */
     const int32_t *order;         /* device: particle index per queue slot, e.g. longest
                                      first (pt_run_device only), or NULL */
@@ -261,23 +261,25 @@ int pt_ensemble_check(const pt_ensemble *e);
 
 /* ---- learned step-size controller (no counterpart in the reference) ----- */
 
-/* MLP 8 -> 64 -> 64 -> 1 (SiLU) from eight local invariants at the start of
+/* MLP 9 -> 64 -> 64 -> 1 (SiLU) from nine local invariants at the start of
  * an attempt (log|B|, log|E|, log gamma, pitch cosine, log(|grad B|/|B|),
- * log(Omega dt_prev), log(err_prev), log dt_prev) to log(trial dt); inference
- * on FP16 tensor cores inside the integrator.  The embedded error estimate
- * still accepts or rejects every step and a rejection falls back to the
- * classical controller.  params: PT_MLP_NPARAM floats (W1[8][64], b1[64],
- * W2[64][64], b2[64], W3[64], b3); norm: feature means[8], standard
- * deviations[8], target mean and standard deviation; safety multiplies the
- * proposed step. */
+ * log(Omega dt_prev), log(err_prev), log dt_prev, and log of the time to the
+ * next cell face along the current velocity over dt_prev) to log(trial dt);
+ * a model whose ninth input weights are zero is the 8 -> 64 -> 64 -> 1
+ * network of the first eight.  Inference on FP16 tensor cores inside the
+ * integrator.  The embedded error estimate still accepts or rejects every
+ * step and a rejection falls back to the classical controller.  params:
+ * pt_mlp_nparam() floats (W1[9][64], b1[64], W2[64][64], b2[64], W3[64],
+ * b3); norm: feature means[9], standard deviations[9], target mean and
+ * standard deviation; safety multiplies the proposed step. */
 typedef struct pt_mlp pt_mlp;
 int32_t pt_mlp_nparam(void);
-int pt_mlp_create(const float *params, const float norm[18], float safety, pt_mlp **out);
+int pt_mlp_create(const float *params, const float norm[20], float safety, pt_mlp **out);
 int pt_mlp_destroy(pt_mlp *m);
 /* Tensor-core inference on n feature rows (device pointers), as in the integrator. */
 int pt_mlp_infer(const pt_mlp *m, const float *d_X, int64_t n, float *d_out, void *stream);
 /* Training: mean-squared-error loss and its gradient over n standardised rows
- * (X n x 8, T n), and one Adam update (device pointers). */
+ * (X n x 9, T n), and one Adam update (device pointers). */
 int pt_mlp_loss_grad(const float *d_params, const float *d_X, const float *d_T, int64_t n,
                      float *d_grad, float *d_loss, void *stream);
 int pt_mlp_adam(float *d_params, const float *d_grad, float *d_m, float *d_v, int64_t step,

@@ -1,14 +1,14 @@
 """Float64 numpy MLP -- TEST INFRASTRUCTURE ONLY.
 
 The reference has no learned controller; this is the CPU oracle for the
-project's own MLP (8 -> 64 -> 64 -> 1, SiLU, mean-squared error), used to
+project's own MLP (9 -> 64 -> 64 -> 1, SiLU, mean-squared error), used to
 check the GPU training kernels' loss and gradients and the tensor-core
 inference.  Flat parameter layout as in particles_gb300/csrc/pt_mlp_train.cu:
-W1[8][64], b1[64], W2[64][64], b2[64], W3[64], b3.
+W1[9][64], b1[64], W2[64][64], b2[64], W3[64], b3.
 """
 import numpy as np
 
-NIN, NH = 8, 64
+NIN, NH = 9, 64
 SIZES = [("W1", (NIN, NH)), ("b1", (NH,)), ("W2", (NH, NH)), ("b2", (NH,)), ("W3", (NH,)),
          ("b3", (1,))]
 NPARAM = sum(int(np.prod(s)) for _, s in SIZES)

@@ -114,10 +114,11 @@ __host__ __device__ inline PtCarry pt_carry_view(unsigned char *base, int64_t np
 #define PT_CARRY_BYTES_PER_PARTICLE 128
 
 /* Accepted-step record buffer: a 16-byte header whose first 8 bytes count
- * the records written, then records of PT_REC_FLOATS floats: the eight
+ * the records written, then records of PT_REC_FLOATS floats: the nine
  * controller features at the start of an accepted step, log(dt) and
  * log(error ratio) of that step. */
-#define PT_REC_FLOATS 10
+#define PT_REC_NFEAT 9
+#define PT_REC_FLOATS 11
 #define PT_REC_HEADER_FLOATS 4
 
 /* Fortran MIN/MAX with the NaN rule of the oracle (a NaN first operand

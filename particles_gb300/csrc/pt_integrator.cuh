@@ -448,16 +448,37 @@ __device__ __forceinline__ double pt_face_cap(const PtRun &P, const double si[6]
 }
 #endif
 
+/* Time for the particle at si to reach the next cell face along its current
+ * velocity (straight path, FP32): the learned controller's ninth input, in
+ * every build (an input of the network, not part of the reference's
+ * controller).  3e38 when the particle does not move across cells. */
+__device__ __forceinline__ float pt_face_time(const PtRun &P, const double si[6])
+{
+    const float ux = pt_d2f(si[3]), uy = pt_d2f(si[4]), uz = pt_d2f(si[5]);
+    const float ig = rsqrtf(fmaf(ux, ux, fmaf(uy, uy, fmaf(uz, uz, 1.0f))));
+    const float u[3] = { ux, uy, uz };
+    float tmin = 3.0e38f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const double xn = fma(si[i], P.gsx[i], P.gox[i]);
+        const float off = pt_d2f(xn - pt_floor(xn));               /* in [0, 1] */
+        const float w = u[i] * ig * P.ivunf * P.gsxf[i];           /* cells per unit time */
+        const float aw = fabsf(w);
+        if (aw > 0.0f) tmin = fminf(tmin, ((w > 0.0f) ? 1.0f - off : off) / aw);
+    }
+    return tmin;
+}
+
 /* ---- the kernel ---------------------------------------------------------- */
 
 /* Dynamic shared memory of one block: the k rows, then (with a learned
  * controller) the MLP weight blob, then (when recording accepted steps)
- * eight pending feature floats per lane. */
+ * the pending feature floats of every lane. */
 template <int METHOD>
 __host__ __device__ constexpr int smem_bytes(int block, bool record, bool mlp = false)
 {
     return Traits<METHOD>::ROWS * 6 * 8 * block + (mlp ? PT_MLP_BLOB_BYTES : 0) +
-           (record ? 8 * 4 * block : 0);
+           (record ? PT_REC_NFEAT * 4 * block : 0);
 }
 
 /* Persistent launch of one integrator variant: as many blocks as fit on
@@ -541,7 +562,7 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
     const KRows K{ pt_ksm + threadIdx.x, (int)blockDim.x };
     unsigned char *const smem_tail =
         reinterpret_cast<unsigned char *>(pt_ksm) + T::ROWS * 6 * 8 * blockDim.x;
-    float *pend = nullptr;                 /* pending features, [8][blockDim] */
+    float *pend = nullptr;                 /* pending features, [PT_REC_NFEAT][blockDim] */
     bool have_pend = false;
     int mi = 0;                            /* member this lane draws particles from */
 #define PT_Q (MB.q(mi))
@@ -708,7 +729,7 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
                  * step (the error estimate still accepts or rejects it, and
                  * a rejection falls back to the classical controller). */
                 const bool want = (mode == M_ACCEPT) && active;
-                float feat[8] = { 0, 0, 0, 0, 0, 0, 0, 0 };
+                float feat[PT_REC_NFEAT] = { 0, 0, 0, 0, 0, 0, 0, 0, 0 };
                 if (want) {
                     int32_t fl_[3], fr_[3];
                     float fx_[3];
@@ -720,6 +741,8 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
                     feat[5] = __logf(om * dtf + 1e-30f);
                     feat[6] = __logf(pt_d2f(q) + 1e-30f);
                     feat[7] = __logf(dtf);
+                    /* time to the next cell face in units of the last step */
+                    feat[8] = __logf(fminf(pt_face_time(PT_Q, si) / dtf, 1.0e6f) + 1e-30f);
                     if (PT_Q.rec) {
                         if (have_pend) {
                             const unsigned long long i =
@@ -727,13 +750,13 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
                             if ((int64_t)i < PT_Q.rec_cap) {
                                 float *r = PT_Q.rec + PT_REC_HEADER_FLOATS + i * PT_REC_FLOATS;
 #pragma unroll
-                                for (int c = 0; c < 8; ++c) r[c] = pend[c * blockDim.x];
-                                r[8] = feat[7];
-                                r[9] = feat[6];
+                                for (int c = 0; c < PT_REC_NFEAT; ++c) r[c] = pend[c * blockDim.x];
+                                r[PT_REC_NFEAT] = feat[7];
+                                r[PT_REC_NFEAT + 1] = feat[6];
                             }
                         }
 #pragma unroll
-                        for (int c = 0; c < 8; ++c) pend[c * blockDim.x] = feat[c];
+                        for (int c = 0; c < PT_REC_NFEAT; ++c) pend[c * blockDim.x] = feat[c];
                         have_pend = true;
                     }
                 }

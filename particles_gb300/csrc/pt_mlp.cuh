@@ -1,11 +1,13 @@
 /*
  * pt_mlp.cuh -- the learned step-size controller inside the step machine.
  *
- * An MLP 8 -> 64 -> 64 -> 1 (SiLU) maps eight local invariants of a particle
- * at the start of an attempt to log(trial step).  Inference runs on the
- * tensor cores with warp-level mma.sync m16n8k16 (FP16 operands, FP32
+ * An MLP 9 -> 64 -> 64 -> 1 (SiLU) maps nine local invariants of a particle
+ * at the start of an attempt to log(trial step): the eight of the controller
+ * specification and the time to the next cell face (a model trained with
+ * that input zeroed is the 8 -> 64 -> 64 -> 1 network).  Inference runs on
+ * the tensor cores with warp-level mma.sync m16n8k16 (FP16 operands, FP32
  * accumulate): the 32 lanes of a warp are the 32 rows of the activation
- * matrix (two m16 tiles).  The layer-1 input K of 8 is zero-padded to 16, the
+ * matrix (two m16 tiles).  The layer-1 input K of 9 is zero-padded to 16, the
  * layer-3 output N of 1 to 8.  A layer's FP32 accumulators convert in place
  * into the next layer's FP16 A fragments (the C layout of two adjacent n8
  * tiles is the A layout of one k16 tile), so only the input and the output
@@ -19,8 +21,8 @@
  *
  * Weight blob (pt_mlp_create, global memory, copied to shared memory by
  * each block): B fragments pre-arranged per (k-tile, n-tile, lane) as uint2,
- * then FP32 b1[64], b2[64], b3[4], the feature means mu[8] and inverse
- * standard deviations isd[8].  Features are standardised in FP32 before the
+ * then FP32 b1[64], b2[64], b3[4], the feature means mu[12] and inverse
+ * standard deviations isd[12] (9 used, padded to 16-byte multiples).  Features are standardised in FP32 before the
  * FP16 conversion; W1, b1, W2, b2 are stored halved (see pt_silu_h2), and
  * the target scaling and the safety factor are folded into W3 and b3 when
  * the blob is built.
@@ -31,15 +33,16 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
-#define PT_MLP_NIN 8
+#define PT_MLP_NIN 9
 #define PT_MLP_NH 64
 /* uint2 fragments: W1 8 n-tiles, W2 4 k-tiles x 8 n-tiles, W3 4 k-tiles */
 #define PT_MLP_FRAG_W1 0
 #define PT_MLP_FRAG_W2 (8 * 32)
 #define PT_MLP_FRAG_W3 (PT_MLP_FRAG_W2 + 32 * 32)
 #define PT_MLP_NFRAG (PT_MLP_FRAG_W3 + 4 * 32)
-/* FP32 tail after the fragments: b1[64], b2[64], b3[4], mu[8], isd[8] */
-#define PT_MLP_BLOB_FLOATS (64 + 64 + 4 + 8 + 8)
+/* FP32 tail after the fragments: b1[64], b2[64], b3[4], mu[12], isd[12] */
+#define PT_MLP_NORM_PAD 12
+#define PT_MLP_BLOB_FLOATS (64 + 64 + 4 + 2 * PT_MLP_NORM_PAD)
 #define PT_MLP_BLOB_BYTES (PT_MLP_NFRAG * 8 + PT_MLP_BLOB_FLOATS * 4)
 
 struct PtMlpSmem {
@@ -90,27 +93,29 @@ __device__ __forceinline__ PtMlpSmem pt_mlp_load(const unsigned char *blob, unsi
     m.b2 = m.b1 + 64;
     m.b3 = m.b2 + 64;
     m.mu = m.b3 + 4;
-    m.isd = m.mu + 8;
+    m.isd = m.mu + PT_MLP_NORM_PAD;
     return m;
 }
 
 /* y = MLP(x) for the 32 lanes of a converged warp; every lane passes its own
- * eight raw features and receives its own output (log trial step). */
-static __device__ __noinline__ float pt_mlp_warp(const PtMlpSmem &M, const float x[8])
+ * nine raw features and receives its own output (log trial step). */
+static __device__ __noinline__ float pt_mlp_warp(const PtMlpSmem &M, const float x[PT_MLP_NIN])
 {
     const int lane = threadIdx.x & 31;
     const int g = lane >> 2, q = lane & 3;
-    uint32_t xp[4];
+    uint32_t xp[5];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
         xp[i] = pt_pack_h2((x[2 * i] - M.mu[2 * i]) * M.isd[2 * i],
                            (x[2 * i + 1] - M.mu[2 * i + 1]) * M.isd[2 * i + 1]);
+    xp[4] = pt_pack_h2((x[8] - M.mu[8]) * M.isd[8], 0.0f);
     /* the warp's 32 rows are two m16 tiles; every weight fragment and bias is
      * loaded once and applied to both */
     uint32_t a1[2][4];
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt) {
-        /* layer-1 A fragment: rows g and g + 8 of this m tile, columns 2q, 2q+1 */
+        /* layer-1 A fragment: rows g and g + 8 of this m tile, columns 2q, 2q+1
+         * (features 0..7) and 2q + 8, 2q + 9 (feature 8 in column 8, q == 0) */
         const int r0 = 16 * mt + g, r1 = r0 + 8;
         uint32_t v0 = 0, v1 = 0;
 #pragma unroll
@@ -119,7 +124,10 @@ static __device__ __noinline__ float pt_mlp_warp(const PtMlpSmem &M, const float
             const uint32_t s1 = __shfl_sync(0xffffffffu, xp[i], r1);
             if (q == i) { v0 = s0; v1 = s1; }
         }
-        a1[mt][0] = v0; a1[mt][1] = v1; a1[mt][2] = 0u; a1[mt][3] = 0u;
+        const uint32_t f0 = __shfl_sync(0xffffffffu, xp[4], r0);
+        const uint32_t f1 = __shfl_sync(0xffffffffu, xp[4], r1);
+        a1[mt][0] = v0; a1[mt][1] = v1;
+        a1[mt][2] = (q == 0) ? f0 : 0u; a1[mt][3] = (q == 0) ? f1 : 0u;
     }
     const float2 *b1 = reinterpret_cast<const float2 *>(M.b1);
     const float2 *b2 = reinterpret_cast<const float2 *>(M.b2);

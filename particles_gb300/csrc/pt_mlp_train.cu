@@ -1,15 +1,15 @@
 /*
  * pt_mlp_train.cu -- training and packing of the learned step-size controller.
  *
- * The MLP 8 -> 64 -> 64 -> 1 (SiLU) is trained on accepted-step records that
- * the classical integrator itself writes (PT_REC_*): inputs are the eight
+ * The MLP 9 -> 64 -> 64 -> 1 (SiLU) is trained on accepted-step records that
+ * the classical integrator itself writes (PT_REC_*): inputs are the nine
  * controller features, the target is a standardised log step.  Training runs
  * in FP32 with these kernels (one thread per output element, a grid-stride
  * loop per layer), mean-squared error, and Adam; the model's FP16 tensor-core
  * inference (pt_mlp.cuh) uses the packed blob built by pt_mlp_create.
  *
- * Flat parameter vector (FP32, PT_MLP_NPARAM = 4801):
- *   W1[8][64] (input-major), b1[64], W2[64][64], b2[64], W3[64], b3.
+ * Flat parameter vector (FP32, 4865 values):
+ *   W1[9][64] (input-major), b1[64], W2[64][64], b2[64], W3[64], b3.
  */
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -22,7 +22,7 @@
 #include "pt_common.cuh"
 #include "pt_mlp.cuh"
 
-#define NIN 8
+#define NIN PT_MLP_NIN
 #define NH 64
 #define OFF_W1 0
 #define OFF_B1 (OFF_W1 + NIN * NH)
@@ -154,9 +154,9 @@ __global__ void k_infer(const unsigned char *blob, const float *X, int64_t n, fl
     const int lane = threadIdx.x & 31;
     for (int64_t w = w0; w * 32 < n; w += warps) {
         const int64_t row = w * 32 + lane;
-        float x[8];
+        float x[NIN];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) x[i] = (row < n) ? X[row * 8 + i] : 0.0f;
+        for (int i = 0; i < NIN; ++i) x[i] = (row < n) ? X[row * NIN + i] : 0.0f;
         const float y = pt_mlp_warp(M, x);
         if (row < n) out[row] = y;
     }
@@ -225,8 +225,8 @@ extern "C" int pt_mlp_adam(float *d_params, const float *d_grad, float *d_m, flo
     return PT_OK;
 }
 
-extern "C" int pt_mlp_create(const float *params, const float norm[18], float safety,
-                             pt_mlp **out)
+extern "C" int pt_mlp_create(const float *params, const float norm[2 * PT_MLP_NIN + 2],
+                             float safety, pt_mlp **out)
 {
     if (!params || !norm || !out || !(safety > 0.0f)) {
         pt_set_last_error("pt_mlp_create: bad argument");
@@ -235,13 +235,16 @@ extern "C" int pt_mlp_create(const float *params, const float norm[18], float sa
     *out = nullptr;
     const float *W1 = params + OFF_W1, *b1 = params + OFF_B1, *W2 = params + OFF_W2;
     const float *b2 = params + OFF_B2, *W3 = params + OFF_W3, b3 = params[OFF_B3];
-    const float *mu = norm, *sd = norm + 8, ymu = norm[16], ysd = norm[17];
+    const float *mu = norm, *sd = norm + NIN, ymu = norm[2 * NIN], ysd = norm[2 * NIN + 1];
     std::vector<uint32_t> frag(2 * PT_MLP_NFRAG, 0u);
     for (int nt = 0; nt < 8; ++nt)
         for (int lane = 0; lane < 32; ++lane) {
             const int g = lane >> 2, q = lane & 3, nn = 8 * nt + g;
             frag[2 * (PT_MLP_FRAG_W1 + nt * 32 + lane)] =
                 h2bits(0.5f * W1[(2 * q) * NH + nn], 0.5f * W1[(2 * q + 1) * NH + nn]);
+            /* rows 2q + 8, 2q + 9 of the K = 16 tile: feature 8 (q == 0), else 0 */
+            if (q == 0) frag[2 * (PT_MLP_FRAG_W1 + nt * 32 + lane) + 1] =
+                h2bits(0.5f * W1[8 * NH + nn], 0.0f);
         }
     for (int kt = 0; kt < 4; ++kt)
         for (int nt = 0; nt < 8; ++nt)
@@ -265,9 +268,9 @@ extern "C" int pt_mlp_create(const float *params, const float norm[18], float sa
      * takes their accumulators as h = z / 2, and silu(z) = h + h tanh(h) */
     for (int j = 0; j < 64; ++j) { tail[j] = 0.5f * b1[j]; tail[64 + j] = 0.5f * b2[j]; }
     tail[128] = b3 * ysd + ymu + logf(safety);
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < NIN; ++i) {
         tail[132 + i] = mu[i];
-        tail[140 + i] = (sd[i] > 0.0f) ? 1.0f / sd[i] : 1.0f;
+        tail[132 + PT_MLP_NORM_PAD + i] = (sd[i] > 0.0f) ? 1.0f / sd[i] : 1.0f;
     }
     std::vector<unsigned char> blob(PT_MLP_BLOB_BYTES);
     memcpy(blob.data(), frag.data(), PT_MLP_NFRAG * 8);

@@ -1,8 +1,11 @@
 """The learned step-size controller: recording, training and the model handle.
 
 Records come from the classical integrator itself (``pt_run_device`` with a
-record buffer): for every accepted step, the eight controller features at its
-start, its log(dt) and log(error ratio).  The regression target is the
+record buffer): for every accepted step, the nine controller features at its
+start (the eight of the controller specification and the time to the next
+cell face over the last step), its log(dt) and log(error ratio).  A model
+trained with ``face_feature=False`` sees the ninth input as zero: the
+8 -> 64 -> 64 -> 1 network of the first eight.  The regression target is the
 accepted step enlarged by what its error ratio says it could have been, at
 most by a factor of 2: log dt - clip(log err, -(order) log 2, 0) / order.
 In a trilinear field the accepted error ratios are bimodal (steps inside a
@@ -24,8 +27,9 @@ from . import _native as N
 from .integrations import _stream
 
 FEATURES = ["log|B|", "log|E|", "log gamma", "pitch cosine", "log(|grad B|/|B|)",
-            "log(Omega dt_prev)", "log(err_prev)", "log dt_prev"]
-REC_FLOATS = 10
+            "log(Omega dt_prev)", "log(err_prev)", "log dt_prev", "log(t_face / dt_prev)"]
+NIN = len(FEATURES)
+REC_FLOATS = NIN + 2
 REC_HEADER_FLOATS = 4
 ORDER = {"rk5": 5, "dop853": 8, 1: 5, 2: 8}
 
@@ -37,7 +41,7 @@ def record_buffer(torch, capacity: int, device="cuda"):
 
 
 def records_from_buffer(buf) -> np.ndarray:
-    """(n, 10) float32 records out of a device record buffer."""
+    """(n, 11) float32 records out of a device record buffer."""
     raw = buf.cpu().numpy()
     n = int(raw[:2].view(np.uint64)[0])
     cap = (raw.size - REC_HEADER_FLOATS) // REC_FLOATS
@@ -45,19 +49,26 @@ def records_from_buffer(buf) -> np.ndarray:
     return raw[REC_HEADER_FLOATS:REC_HEADER_FLOATS + n * REC_FLOATS].reshape(n, REC_FLOATS)
 
 
-def dataset(records: np.ndarray, method) -> tuple[np.ndarray, np.ndarray]:
-    """Features X (n, 8) and the target log trial step (n,) from records;
-    rows with a non-finite entry are dropped."""
+def dataset(records: np.ndarray, method, face_feature: bool = True
+            ) -> tuple[np.ndarray, np.ndarray]:
+    """Features X (n, 9) and the target log trial step (n,) from records;
+    rows with a non-finite entry are dropped.  face_feature=False zeroes the
+    ninth input (the 8-input network)."""
     rec = np.asarray(records, np.float64)
-    log_dt, log_err = rec[:, 8], rec[:, 9]
+    log_dt, log_err = rec[:, NIN], rec[:, NIN + 1]
     ok = np.isfinite(rec).all(axis=1)
     p = ORDER[method] + 0.0
     t = log_dt - np.clip(log_err, -p * np.log(2.0), 0.0) / p
-    return rec[ok, :8].astype(np.float32), t[ok].astype(np.float32)
+    X = rec[ok, :NIN].astype(np.float32)
+    if not face_feature:
+        X[:, NIN - 1] = 0.0
+    return X, t[ok].astype(np.float32)
 
 
 def normalisation(X: np.ndarray, T: np.ndarray) -> np.ndarray:
-    """Feature means, standard deviations, target mean and deviation (18)."""
+    """Feature means, standard deviations, target mean and deviation (20).
+    A constant input (the zeroed ninth of the 8-input network) gets its value
+    as mean and deviation 1, so its standardised value is 0."""
     mu = X.mean(0)
     sd = X.std(0)
     sd[sd < 1e-6] = 1.0
@@ -66,7 +77,7 @@ def normalisation(X: np.ndarray, T: np.ndarray) -> np.ndarray:
 
 def init_params(seed: int) -> np.ndarray:
     rng = np.random.default_rng(seed)
-    shapes = [(8, 64), (64,), (64, 64), (64,), (64,), (1,)]
+    shapes = [(NIN, 64), (64,), (64, 64), (64,), (64,), (1,)]
     parts = []
     for sh in shapes:
         if len(sh) == 2:
@@ -85,8 +96,8 @@ def train(torch, X: np.ndarray, T: np.ndarray, norm: np.ndarray, *, epochs: int 
     """
     L = N.load()
     vp = lambda t: C.c_void_p(t.data_ptr())
-    Xs = (X - norm[:8]) / norm[8:16]
-    Ts = (T - norm[16]) / norm[17]
+    Xs = (X - norm[:NIN]) / norm[NIN:2 * NIN]
+    Ts = (T - norm[2 * NIN]) / norm[2 * NIN + 1]
     dX = torch.tensor(Xs, dtype=torch.float32, device=device)
     dT = torch.tensor(Ts, dtype=torch.float32, device=device)
     p = torch.tensor(init_params(seed), device=device)
@@ -116,6 +127,44 @@ def train(torch, X: np.ndarray, T: np.ndarray, norm: np.ndarray, *, epochs: int 
         if log:
             log(f"epoch {ep}: mse {hist[-1]:.4f}")
     return p.cpu().numpy(), hist
+
+
+def predict(params: np.ndarray, norm: np.ndarray, X: np.ndarray) -> np.ndarray:
+    """The network's log trial step on raw feature rows, in float64 on the host
+    (for choosing the safety factor; the integrator runs the FP16 tensor-core
+    version)."""
+    p = np.asarray(params, np.float64)
+    o = 0
+    parts = []
+    for shape in [(NIN, 64), (64,), (64, 64), (64,), (64,), (1,)]:
+        n = int(np.prod(shape))
+        parts.append(p[o:o + n].reshape(shape))
+        o += n
+    W1, b1, W2, b2, W3, b3 = parts
+    x = (np.asarray(X, np.float64) - norm[:NIN]) / norm[NIN:2 * NIN]
+    z1 = x @ W1 + b1
+    h1 = z1 / (1.0 + np.exp(-z1))
+    z2 = h1 @ W2 + b2
+    h2 = z2 / (1.0 + np.exp(-z2))
+    return (h2 @ W3 + b3[0]) * norm[2 * NIN + 1] + norm[2 * NIN]
+
+
+def choose_safety(params: np.ndarray, norm: np.ndarray, X: np.ndarray, T: np.ndarray,
+                  grid=None) -> tuple[float, dict]:
+    """Safety factor s that maximises the expected progress per attempt on
+    held-out records: a proposal exp(pred) s succeeds when it does not exceed
+    the attainable step exp(T), and then advances by its length.  The
+    network's prediction error makes s < 1 pay; a fixed s either wastes
+    attempts (too large) or step length (too small).  Returns (s, the
+    progress per attempt at s relative to proposing exp(T) itself)."""
+    pred = predict(params, norm, X)
+    T = np.asarray(T, np.float64)
+    grid = np.linspace(-1.5, 0.3, 73) if grid is None else np.asarray(grid)
+    prog = np.array([np.mean(np.exp(pred + ls) * (pred + ls <= T)) for ls in grid])
+    k = int(np.argmax(prog))
+    return float(np.exp(grid[k])), {"progress_per_attempt_vs_target": float(prog[k] /
+                                                                           np.mean(np.exp(T))),
+                                    "accepted_fraction": float(np.mean(pred + grid[k] <= T))}
 
 
 class Model:

@@ -49,7 +49,7 @@ def test_mixed_learned_variants_agree(cuda):
     prob = small_problem("dop853", n=16, npart=256, periods=1.0, seed=43, tol=1e-9)
     uu, bb = prob["fields"]
     f = Fields(uu, bb, precision="fp32")
-    norm = np.concatenate([np.zeros(8), np.full(8, 3.0), [-7.0, 1.0]]).astype(np.float32)
+    norm = np.concatenate([np.zeros(9), np.full(9, 3.0), [-7.0, 1.0]]).astype(np.float32)
     model = learned.Model(learned.init_params(5), norm, safety=0.9)
     out = [_run(torch, f, prob, model=model, blocks_per_sm=v) for v in (2, 3, 4)]
     for s, c, st in out:
