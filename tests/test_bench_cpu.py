@@ -69,7 +69,8 @@ def _full_line():
                   "detail": detail, "over_plain_exact": {k: 5.123456 for k in names},
                   "physics_rate_over_plain_exact": {k: 4.56789 for k in names},
                   "accuracy": {k: acc for k in names[1:]}},
-        "learned": {"physics_rate_ratio": 0.95612345},
+        "learned": {"physics_rate_ratio": 0.95612345, "attempts_ratio": 0.812345,
+                    "physics_rate_ratio_8_inputs": 0.9412345},
         "ensemble": {"a": "e" * 5000},
     }
 
