@@ -80,7 +80,8 @@ extern "C" {
 typedef struct pt_options {
     int32_t       struct_size;    /* sizeof(pt_options), or 0 */
     int32_t       precision;      /* PT_PREC_* */
-    int32_t       open_x;         /* 1: particles escape through x = xmin / xmax of the domain */
+    int32_t       open_x;         /* 1: particles escape through x = xmin / xmax of the domain
+                                     (moved out by open_x_margin) */
     int32_t       controller;     /* PT_CTL_* bits: 0 classical; PT_CTL_LEARNED learned
                                      trial step (needs a model); PT_CTL_FACE trial step
                                      capped just past the next cell face (not with
@@ -109,6 +110,9 @@ typedef struct pt_options {
                                      corner of the cell, interpolate_near (:55-83) */
     int32_t       threads_per_block; /* 64, 128 or 256 (one particle per lane); 0 = the
                                      choice of pt_autotune for this kernel, else 128 */
+    double        open_x_margin;  /* with open_x: the escape faces sit this many domain
+                                     lengths outside x = xmin and xmax (the field stays
+                                     periodic); 0 = the domain faces */
 } pt_options;
 
 /* ---- one-shot, reference-shaped call ----------------------------------- */
@@ -222,6 +226,7 @@ typedef struct pt_member {
     int64_t         *cnt;         /* device: cnt(3,np) */
     int32_t         *status;      /* device: np status words (set to PT_ST_RUNNING) */
     void            *carry;       /* device: pt_carry_bytes(np), zero-filled = fresh */
+    double           open_x_margin; /* as pt_options.open_x_margin */
 } pt_member;
 
 typedef struct pt_ensemble pt_ensemble;

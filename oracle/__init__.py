@@ -41,7 +41,7 @@ class Ext(C.Structure):
     _fields_ = [("eta", C.c_double), ("jj", C.c_void_p), ("open_x", C.c_int32),
                 ("faithful", C.c_int32), ("max_steps", C.c_int64), ("t_stop", C.c_double),
                 ("carry", C.c_void_p), ("status", C.c_void_p), ("near", C.c_int32),
-                ("pad", C.c_int32)]
+                ("pad", C.c_int32), ("open_x_margin", C.c_double)]
 
 
 def build(force: bool = False) -> Path:
@@ -88,7 +88,7 @@ def _f64(a):
 
 def integrate(method, params, time, uu, bb, state, cnt=None, *, eta=0.0, jj=None,
               open_x=False, faithful=False, max_steps=0, t_stop=0.0, carry=None,
-              status=None, nthreads=0, near=False):
+              status=None, nthreads=0, near=False, open_x_margin=0.0):
     """Run the oracle over all particles in place.
 
     ``state`` (np, m, 8) float64 is updated in place (row 0 holds the initial
@@ -108,7 +108,7 @@ def integrate(method, params, time, uu, bb, state, cnt=None, *, eta=0.0, jj=None
     ext = Ext(eta, _p(jj) if jj is not None else None, int(open_x), int(faithful),
               int(max_steps), float(t_stop),
               C.cast(carry, C.c_void_p) if carry is not None else None, _p(status),
-              int(bool(near)), 0)
+              int(bool(near)), 0, float(open_x_margin))
     rc = lib().or_integrate(int(method), npart, m, _p(dm), _p(_f64(params)), _p(_f64(time)),
                             _p(uu), _p(bb), _p(state), _p(cnt), C.byref(ext), int(nthreads))
     if rc != 0:

@@ -512,11 +512,12 @@ struct RunOpts {
     int32_t open_x;
     int64_t max_steps;
     double  t_stop;
+    double  xo_lo, xo_hi;   /* open x faces: xl, xl + xs, moved out by the margin */
 };
 
-inline bool escaped_x(double xl, double xs, double x)
+inline bool escaped_x(const RunOpts &O, double x)
 {
-    return x < xl || x >= xl + xs;
+    return x < O.xo_lo || x >= O.xo_hi;
 }
 
 /* Shared loop guards, identical in the GPU kernels: returns a status < 0 to
@@ -573,7 +574,7 @@ int32_t rk5_particle(const Ctx<double> &C, const RunOpts &O, int32_t m, const do
             have_f1 = false;
             cnt[1]++;
             dt = rk5_dt_accept(C, dt, del);
-            esc = O.open_x && escaped_x(C.xl[0], C.xs[0], si[0]);
+            esc = O.open_x && escaped_x(O, si[0]);
         } else {
             cnt[2]++;
             for (int c = 0; c < 6; ++c) F1[c] = F1n[c];        /* f(si) is unchanged */
@@ -640,7 +641,7 @@ int32_t dp853_particle(const Ctx<double> &C, const RunOpts &O, int32_t m, const 
             cnt[1]++;
             dt = dp853_dt_accept(C, dt, err, errold, rejected, expo);
             rejected = false;
-            esc = O.open_x && escaped_x(C.xl[0], C.xs[0], si[0]);
+            esc = O.open_x && escaped_x(O, si[0]);
         } else {
             cnt[2]++;                                          /* :482-490 */
             dt = dp853_dt_reject(C, dt, err, expo);
@@ -686,6 +687,9 @@ extern "C" int or_integrate(int32_t method, int64_t np, int32_t m, const int32_t
     O.open_x = e.open_x;
     O.max_steps = e.max_steps;
     O.t_stop = e.t_stop;
+    O.xo_lo = (e.open_x_margin == 0.0) ? C.xl[0] : C.xl[0] - e.open_x_margin * C.xs[0];
+    O.xo_hi = (e.open_x_margin == 0.0) ? C.xl[0] + C.xs[0]
+                                       : C.xl[0] + C.xs[0] + e.open_x_margin * C.xs[0];
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #pragma omp parallel for schedule(dynamic, 1)

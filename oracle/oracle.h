@@ -49,7 +49,8 @@ typedef struct or_carry {
 typedef struct or_ext {
     double        eta;          /* resistive E += eta J; 0 = ideal MHD */
     const double *jj;           /* J = curl B, layout of bb; used iff eta != 0 */
-    int32_t       open_x;       /* 1: particles escape through x = xl, xl+xs */
+    int32_t       open_x;       /* 1: particles escape through x = xl, xl+xs (moved out
+                                   by open_x_margin) */
     int32_t       faithful;     /* 1: also perform the reference's redundant evaluations */
     int64_t       max_steps;    /* cap on attempts (cnt[0]); 0 = none */
     double        t_stop;       /* window end; <= 0 means tmx */
@@ -58,6 +59,8 @@ typedef struct or_ext {
     int32_t       near;         /* 1: interpolate_near (interpolations.F90:55-83) in the
                                    acceleration instead of interpolate_lin */
     int32_t       pad;
+    double        open_x_margin; /* the open x faces sit this many domain lengths
+                                   outside xl and xl+xs (the field stays periodic) */
 } or_ext;
 
 /* Batched equivalent of the dispatch loop particles.F90:337-356.

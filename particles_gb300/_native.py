@@ -48,7 +48,7 @@ class PtOptions(C.Structure):
         ("status", C.c_void_p), ("carry", C.c_void_p), ("model", C.c_void_p),
         ("records", C.c_void_p), ("record_capacity", C.c_int64), ("order", C.c_void_p),
         ("blocks_per_sm", C.c_int32), ("interpolation", C.c_int32),
-        ("threads_per_block", C.c_int32),
+        ("threads_per_block", C.c_int32), ("open_x_margin", C.c_double),
     ]
 
 
@@ -57,8 +57,13 @@ class PtMember(C.Structure):
         ("fields", C.c_void_p), ("params", C.c_void_p), ("np", C.c_int64), ("m", C.c_int32),
         ("open_x", C.c_int32), ("eta", C.c_double), ("max_steps", C.c_int64),
         ("time", C.c_void_p), ("state", C.c_void_p), ("cnt", C.c_void_p),
-        ("status", C.c_void_p), ("carry", C.c_void_p),
+        ("status", C.c_void_p), ("carry", C.c_void_p), ("open_x_margin", C.c_double),
     ]
+
+
+# Accepted-step records (pt_options.records): a 4-float header, then records
+# of the nine controller features, log(dt) and log(error ratio).
+REC_HEADER_FLOATS, REC_FLOATS = 4, 11
 
 
 class PtError(RuntimeError):

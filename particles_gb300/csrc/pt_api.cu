@@ -123,6 +123,14 @@ int32_t pt_opt_threads_per_block(const pt_options *opt)
     return (opt->struct_size == 0 || opt->struct_size >= need) ? opt->threads_per_block : 0;
 }
 
+/* pt_options.open_x_margin under the same rule. */
+double pt_opt_open_x_margin(const pt_options *opt)
+{
+    if (!opt) return 0.0;
+    const int32_t need = (int32_t)(offsetof(pt_options, open_x_margin) + sizeof(double));
+    return (opt->struct_size == 0 || opt->struct_size >= need) ? opt->open_x_margin : 0.0;
+}
+
 int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
                        const double *params, const pt_options *opt, PtRun &R)
 {
@@ -165,8 +173,10 @@ int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
         open_x = opt->open_x;
         max_steps = opt->max_steps;
     }
-    if (!isfinite(eta) || !isfinite(t_stop) || !isfinite(budget))
+    const double margin = pt_opt_open_x_margin(opt);
+    if (!isfinite(eta) || !isfinite(t_stop) || !isfinite(budget) || !isfinite(margin))
         return set_err(PT_ERR_ARG, "non-finite option%s");
+    if (margin < 0.0) return set_err(PT_ERR_ARG, "open_x_margin must be >= 0%s");
     if (eta != 0.0 && !g.has_j)
         return set_err(PT_ERR_ARG, "eta != 0 needs a field handle created with J%s");
     if (eta == 0.0 && g.has_j)
@@ -176,6 +186,9 @@ int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
     R.etaf = (float)eta;
     R.has_j = g.has_j;
     R.open_x = open_x ? 1 : 0;
+    /* the same expressions as the oracle, so the escape test matches bit for bit */
+    R.xo_lo = (margin == 0.0) ? R.xl[0] : R.xl[0] - margin * R.xs[0];
+    R.xo_hi = (margin == 0.0) ? R.xl[0] + R.xs[0] : R.xl[0] + R.xs[0] + margin * R.xs[0];
     R.max_steps = max_steps > 0 ? max_steps : 1000000000LL;
     R.tend = (t_stop > 0.0 && t_stop < R.tmx) ? t_stop : R.tmx;
     R.budget_ns = (uint64_t)((budget > 0.0 ? budget : 600.0) * 1e9);

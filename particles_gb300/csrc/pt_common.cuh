@@ -41,6 +41,7 @@ struct PtRun {
     double eta;
     int32_t has_j;
     int32_t open_x;
+    double xo_lo, xo_hi;   /* open x faces: xl and xl + xs moved out by the margin */
     int64_t max_steps;
     double tend;           /* min(t_stop, tmx) */
     uint64_t budget_ns;

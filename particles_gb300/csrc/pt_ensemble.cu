@@ -265,6 +265,7 @@ extern "C" int pt_ensemble_create(int32_t method, int32_t nmembers, const pt_mem
         o.struct_size = (int32_t)sizeof o;
         o.precision = prec;
         o.open_x = M.open_x;
+        o.open_x_margin = M.open_x_margin;
         o.max_steps = M.max_steps;
         o.eta = M.eta;
         o.time_budget_s = opt ? opt->time_budget_s : 0.0;

@@ -257,7 +257,7 @@ __device__ __forceinline__ void dense_row(double t, double dt, double tn, const 
 
 __device__ __forceinline__ bool escaped_x(const PtRun &P, double x)
 {
-    return P.open_x && (x < P.xl[0] || x >= P.xl[0] + P.xs[0]);
+    return P.open_x && (x < P.xo_lo || x >= P.xo_hi);
 }
 
 /* Stage state of slot j (1..SLOTS-1) in the reference's operand order, and

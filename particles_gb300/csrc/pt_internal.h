@@ -76,6 +76,8 @@ int run_impl(int32_t method, int64_t np, int32_t m, const pt_fields *f, const do
              void *d_carry, const pt_options *opt, cudaStream_t s);
 /* pt_options.threads_per_block when the caller's struct has the field, else 0. */
 int32_t pt_opt_threads_per_block(const pt_options *opt);
+/* pt_options.open_x_margin when the caller's struct has the field, else 0. */
+double pt_opt_open_x_margin(const pt_options *opt);
 /* The launch variant pt_autotune chose for a kernel family (0: none). */
 std::atomic<int> &tuned_slot(int32_t method, const pt_fields *f, const PtRun &R);
 

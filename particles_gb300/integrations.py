@@ -49,17 +49,18 @@ def _f64(a):
 def _options(precision, *, eta=0.0, jj=None, open_x=False, max_steps=0, t_stop=0.0,
              status=None, carry=None, time_budget_s=0.0, model=None, records=None,
              order=None, blocks_per_sm=0, interpolation=0, face_steps=False,
-             threads_per_block=0):
+             threads_per_block=0, open_x_margin=0.0):
     o = N.PtOptions()
     o.struct_size = C.sizeof(N.PtOptions)
     o.precision = N.PRECISIONS[precision] if isinstance(precision, str) else int(precision)
     o.open_x = int(bool(open_x))
+    o.open_x_margin = float(open_x_margin)
     o.controller = ((N.PT_CTL_LEARNED if model is not None else 0)
                     | (N.PT_CTL_FACE if face_steps else 0))
     o.model = model.handle if model is not None else None
     if records is not None:                       # device tensor (float32) with header
         o.records = C.c_void_p(records.data_ptr())
-        o.record_capacity = (records.numel() - 4) // 10
+        o.record_capacity = (records.numel() - N.REC_HEADER_FLOATS) // N.REC_FLOATS
     if order is not None:                         # device int32 tensor
         o.order = C.c_void_p(order.data_ptr())
     o.max_steps = int(max_steps)
@@ -81,8 +82,9 @@ def carry_buffer(npart: int) -> np.ndarray:
 
 
 def integrate(method, params, time, uu, bb, state, cnt=None, *, precision="fp64", eta=0.0,
-              jj=None, open_x=False, max_steps=0, t_stop=0.0, carry=None, status=None,
-              time_budget_s=0.0, check=True, interpolation="linear", face_steps=False):
+              jj=None, open_x=False, open_x_margin=0.0, max_steps=0, t_stop=0.0, carry=None,
+              status=None, time_budget_s=0.0, check=True, interpolation="linear",
+              face_steps=False):
     """Integrate every particle of ``state`` in place on the GPU.
 
     Returns (state, cnt, status).  With ``check`` a negative return code
@@ -100,9 +102,10 @@ def integrate(method, params, time, uu, bb, state, cnt=None, *, precision="fp64"
     uu, bb = _f64(uu), _f64(bb)
     jj = _f64(jj) if jj is not None else None
     dm = np.array(uu.shape[:0:-1], np.int32)
-    opt = _options(precision, eta=eta, jj=jj, open_x=open_x, max_steps=max_steps,
-                   t_stop=t_stop, status=status, carry=carry, time_budget_s=time_budget_s,
-                   interpolation=interpolation, face_steps=face_steps)
+    opt = _options(precision, eta=eta, jj=jj, open_x=open_x, open_x_margin=open_x_margin,
+                   max_steps=max_steps, t_stop=t_stop, status=status, carry=carry,
+                   time_budget_s=time_budget_s, interpolation=interpolation,
+                   face_steps=face_steps)
     rc = L.pt_integrate(mid, npart, m, _ptr(dm), _ptr(_f64(params)), _ptr(_f64(time)),
                         _ptr(uu), _ptr(bb), _ptr(state), _ptr(cnt), C.byref(opt))
     if check:
@@ -169,17 +172,18 @@ class Fields:
             pass
 
     def integrate(self, method, params, time, state, cnt=None, *, eta=0.0, open_x=False,
-                  max_steps=0, t_stop=0.0, carry=None, status=None, time_budget_s=0.0,
-                  check=True, interpolation="linear", face_steps=False):
+                  open_x_margin=0.0, max_steps=0, t_stop=0.0, carry=None, status=None,
+                  time_budget_s=0.0, check=True, interpolation="linear", face_steps=False):
         """Host-buffer run on these fields (pt_integrate_fields)."""
         npart, m, _ = state.shape
         if cnt is None:
             cnt = np.zeros((npart, 3), np.int64)
         if status is None:
             status = np.zeros(npart, np.int32)
-        opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
-                       t_stop=t_stop, status=status, carry=carry, time_budget_s=time_budget_s,
-                       interpolation=interpolation, face_steps=face_steps)
+        opt = _options(self.precision, eta=eta, open_x=open_x, open_x_margin=open_x_margin,
+                       max_steps=max_steps, t_stop=t_stop, status=status, carry=carry,
+                       time_budget_s=time_budget_s, interpolation=interpolation,
+                       face_steps=face_steps)
         rc = self._L.pt_integrate_fields(method_id(method), npart, m, self._h,
                                          _ptr(_f64(params)), _ptr(_f64(time)), _ptr(state),
                                          _ptr(cnt), C.byref(opt))
@@ -188,8 +192,9 @@ class Fields:
         return state, cnt, status
 
     def run_device(self, method, params, d_time, d_state, d_cnt, d_status=None, d_carry=None,
-                   *, eta=0.0, open_x=False, max_steps=0, t_stop=0.0, time_budget_s=0.0,
-                   stream=0, model=None, records=None, order=None, blocks_per_sm=0,
+                   *, eta=0.0, open_x=False, open_x_margin=0.0, max_steps=0, t_stop=0.0,
+                   time_budget_s=0.0, stream=0, model=None, records=None, order=None,
+                   blocks_per_sm=0,
                    interpolation="linear", face_steps=False, threads_per_block=0):
         """Launch on device tensors (torch); returns without synchronising.
 
@@ -201,9 +206,9 @@ class Fields:
         not with precision "fp64").
         """
         npart, m, _ = d_state.shape
-        opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
-                       t_stop=t_stop, time_budget_s=time_budget_s, model=model,
-                       records=records, order=order, blocks_per_sm=blocks_per_sm,
+        opt = _options(self.precision, eta=eta, open_x=open_x, open_x_margin=open_x_margin,
+                       max_steps=max_steps, t_stop=t_stop, time_budget_s=time_budget_s,
+                       model=model, records=records, order=order, blocks_per_sm=blocks_per_sm,
                        threads_per_block=threads_per_block,
                        interpolation=interpolation, face_steps=face_steps)
         rc = self._L.pt_run_device(
@@ -252,7 +257,7 @@ class Ensemble:
 
     members: list of dicts with keys fields, params, time, state, cnt,
     status, carry (torch CUDA tensors for the last five) and optionally
-    open_x, eta, max_steps.
+    open_x, open_x_margin, eta, max_steps.
     """
 
     def __init__(self, method, members, *, precision="fp64", blocks_per_sm=0,
@@ -272,6 +277,7 @@ class Ensemble:
             a.params = prm.ctypes.data_as(C.c_void_p)
             a.np, a.m = int(st.shape[0]), int(st.shape[1])
             a.open_x = int(bool(mb.get("open_x", False)))
+            a.open_x_margin = float(mb.get("open_x_margin", 0.0))
             a.eta = float(mb.get("eta", 0.0))
             a.max_steps = int(mb.get("max_steps", 0))
             for key in ("time", "state", "cnt", "status", "carry"):

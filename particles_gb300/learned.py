@@ -30,6 +30,7 @@ FEATURES = ["log|B|", "log|E|", "log gamma", "pitch cosine", "log(|grad B|/|B|)"
             "log(Omega dt_prev)", "log(err_prev)", "log dt_prev", "log(t_face / dt_prev)"]
 NIN = len(FEATURES)
 REC_FLOATS = NIN + 2
+assert REC_FLOATS == N.REC_FLOATS
 REC_HEADER_FLOATS = 4
 ORDER = {"rk5": 5, "dop853": 8, 1: 5, 2: 8}
 

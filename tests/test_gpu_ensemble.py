@@ -18,21 +18,22 @@ T0 = 2.0 * np.pi / 200.0
 
 def _members(torch, precision, method="dop853"):
     from particles_gb300 import Fields
-    specs = [  # grid, particles, tolerance, open x
-        dict(n=12, npart=150, tol=1e-7, open_x=False, seed=51),
-        dict(n=16, npart=300, tol=1e-9, open_x=True, seed=52),
-        dict(n=20, npart=600, tol=1e-8, open_x=True, seed=53),
+    specs = [  # grid, particles, tolerance, open x (faces moved out by the margin)
+        dict(n=12, npart=150, tol=1e-7, open_x=False, margin=0.0, seed=51),
+        dict(n=16, npart=300, tol=1e-9, open_x=True, margin=0.0, seed=52),
+        dict(n=20, npart=600, tol=1e-8, open_x=True, margin=0.5, seed=53),
     ]
     probs, members = [], []
     for sp in specs:
         pr = small_problem(method, n=sp["n"], npart=sp["npart"], periods=1.0, seed=sp["seed"],
                            tol=sp["tol"])
         pr["open_x"] = sp["open_x"]
+        pr["margin"] = sp["margin"]
         uu, bb = pr["fields"]
         f = Fields(uu, bb, precision=precision)
         npart = pr["state"].shape[0]
         members.append(dict(
-            fields=f, params=pr["params"], open_x=sp["open_x"],
+            fields=f, params=pr["params"], open_x=sp["open_x"], open_x_margin=sp["margin"],
             time=torch.tensor(pr["time"], device="cuda"),
             state=torch.tensor(pr["state"], device="cuda"),
             cnt=torch.zeros((npart, 3), dtype=torch.int64, device="cuda"),
@@ -61,7 +62,8 @@ def test_ensemble_exact_matches_oracle_per_member(cuda, oracle_lib, method):
     for k, (pr, mb) in enumerate(zip(probs, members)):
         uu, bb = pr["fields"]
         so, co, sto = oracle.integrate(method, pr["params"], pr["time"], uu, bb,
-                                       pr["state"].copy(), open_x=pr["open_x"])
+                                       pr["state"].copy(), open_x=pr["open_x"],
+                                       open_x_margin=pr["margin"])
         st = mb["status"].cpu().numpy()
         assert np.array_equal(st, sto), k
         assert np.array_equal(mb["cnt"].cpu().numpy(), co), k
@@ -104,6 +106,38 @@ def test_ensemble_graph_replay_equals_stepwise(cuda, precision):
     for a, b in zip(outs[0], outs[1]):
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("method", ["rk5", "dop853"])
+def test_ensemble_graph_replay_matches_oracle_per_member(cuda, oracle_lib, method):
+    """Exact FP64: a captured CUDA graph of four windows (compaction and
+    reordering between them included), then the rest of the run, reproduces
+    the oracle run of every member alone bit for bit -- states, counters,
+    statuses and the escaped lists."""
+    torch = cuda
+    import oracle
+    from particles_gb300 import Ensemble
+    probs, members = _members(torch, "fp64", method)
+    ens = Ensemble(method, members, precision="fp64")
+    stream = torch.cuda.Stream()
+    stream.wait_stream(torch.cuda.current_stream())
+    ens.capture(4, 0.2 * T0, stream=stream.cuda_stream)
+    ens.replay(stream=stream.cuda_stream)
+    ens.run(0.0, stream=stream.cuda_stream)              # the rest of the run
+    stream.synchronize()
+    assert ens.check() == 0
+    live, esc = ens.counts()
+    assert (live == 0).all()
+    for k, (pr, mb) in enumerate(zip(probs, members)):
+        uu, bb = pr["fields"]
+        so, co, sto = oracle.integrate(method, pr["params"], pr["time"], uu, bb,
+                                       pr["state"].copy(), open_x=pr["open_x"],
+                                       open_x_margin=pr["margin"])
+        assert np.array_equal(mb["status"].cpu().numpy(), sto), k
+        assert np.array_equal(mb["cnt"].cpu().numpy(), co), k
+        assert np.array_equal(mb["state"].cpu().numpy(), so), k
+        assert np.array_equal(np.sort(ens.escaped(k)), np.flatnonzero(sto == 2)), k
+    ens.close()
 
 
 def test_output_stream_rows_match_final_state(cuda):

@@ -72,7 +72,7 @@ def test_argument_errors_need_no_gpu(native):
 
 def test_options_struct_layout():
     from particles_gb300 import _native as N
-    assert C.sizeof(N.PtOptions) == 120
+    assert C.sizeof(N.PtOptions) == 128
     assert N.PtOptions.max_steps.offset == 16 and N.PtOptions.carry.offset == 64
     assert N.PtOptions.threads_per_block.offset == 112
 
@@ -122,7 +122,7 @@ def test_ensemble_argument_errors_need_no_gpu(native):
 def test_interpolation_option_checked_on_host(native):
     from particles_gb300 import _native as N
     from particles_gb300.params import pack_params
-    assert N.PtOptions.interpolation.offset == 108 and C.sizeof(N.PtOptions) == 120
+    assert N.PtOptions.interpolation.offset == 108 and C.sizeof(N.PtOptions) == 128
     dm = np.array([8, 8, 8], np.int32)
     p = pack_params(qom=1.0, vunit=0.1, tmax=1.0)
     out = np.zeros(8)

@@ -736,3 +736,26 @@ def test_interpolate_near_restated_from_the_fortran_text():
             p.append(int(math.floor(float(dm[a]) * (x - math.floor(x)))) % dm[a])
         u, b = oracle.interpolate_near(uu, bb, pos, xl=xl, xs=xs)
         assert np.array_equal(u, uu[:, p[2], p[1], p[0]]) and np.array_equal(b, bb[:, p[2], p[1], p[0]])
+
+
+def test_open_x_margin_moves_the_escape_faces(oracle_lib):
+    """A particle streaming along x in a uniform field B = B0 x^ escapes when
+    it crosses xl - margin xs or xl + xs + margin xs, not the domain face."""
+    import oracle
+    from particles_gb300 import fields, params
+    uu, bb = fields.uniform_field(8, b=(1.0, 0.0, 0.0))
+    tmax = 0.2
+    # dtmax 1e-3: the last step does not overshoot tmax by much
+    prm = params.pack_params(qom=200.0, vunit=0.05, tmax=tmax, dtmax=1e-3, atol=1e-8, rtol=1e-8)
+    tg = params.time_grid(4, tmax)
+    st = np.zeros((2, tg.size, 8))
+    st[0, 0, :6] = [0.5, 0.5, 0.5, 0.5, 0.0, 0.0]     # dx/dt = 0.447 c / vun: 1.79 domains
+    st[1, 0, :6] = [0.5, 0.5, 0.5, -0.5, 0.0, 0.0]
+    _, _, s0 = oracle.integrate("rk5", prm, tg, uu, bb, st.copy(), open_x=True)
+    _, _, s1 = oracle.integrate("rk5", prm, tg, uu, bb, st.copy(), open_x=True, open_x_margin=1.0)
+    _, _, s5 = oracle.integrate("rk5", prm, tg, uu, bb, st.copy(), open_x=True, open_x_margin=5.0)
+    assert (s0 == 2).all()                 # both leave through the domain faces
+    assert (s1 == 2).all()                 # ... and through the faces at -1 and 2
+    assert (s5 == 0).all()                 # faces at -5 and 6: both reach tmax inside
+    _, c1, _ = oracle.integrate("rk5", prm, tg, uu, bb, st.copy(), open_x=True, open_x_margin=1.0)
+    assert (c1[:, 1] > oracle.integrate("rk5", prm, tg, uu, bb, st.copy(), open_x=True)[1][:, 1]).all()
