@@ -245,3 +245,18 @@ def test_header_is_plain_c_and_cxx(tmp_path):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.split() == ["1", "2"], (r.stdout, r.stderr)
+
+
+def test_record_capacity_matches_the_record_width():
+    """The capacity the options announce for a record buffer must be the
+    number of whole records that fit after the header: the kernel trusts it
+    and writes up to that many records of 11 floats."""
+    import torch
+    from particles_gb300 import _native as N, learned
+    from particles_gb300.integrations import _options
+    assert N.REC_FLOATS == learned.REC_FLOATS == learned.NIN + 2 == 11
+    for cap in (1, 7, 1000):
+        buf = learned.record_buffer(torch, cap, device="cpu")
+        o = _options("fp64", records=buf)
+        assert o.record_capacity == cap
+        assert N.REC_HEADER_FLOATS + o.record_capacity * N.REC_FLOATS <= buf.numel()
