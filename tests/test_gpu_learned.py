@@ -12,6 +12,9 @@ pytestmark = pytest.mark.gpu
 
 
 def test_training_gradient_matches_oracle(cuda):
+    """The tensor-core training kernels (mma.sync, FP16 operands, FP32
+    accumulation) against the float64 oracle, on a batch that is not a
+    multiple of the kernels' 32-row tiles and 256-row chunks."""
     torch = cuda
     from oracle import mlp
     from particles_gb300 import _native as N
@@ -20,7 +23,7 @@ def test_training_gradient_matches_oracle(cuda):
     rng = np.random.default_rng(4)
     p = (mlp.init_params(2) + rng.normal(0, 0.05, mlp.NPARAM)).astype(np.float32)
     X = rng.normal(size=(1000, 9)).astype(np.float32)
-    T = rng.normal(size=1000).astype(np.float32)
+    T = rng.normal(size=1000).astype(np.float32)   # 1000 = 3 chunks of 256 + 232
     dp, dX, dT = (torch.tensor(a, device="cuda") for a in (p, X, T))
     g = torch.zeros_like(dp)
     loss = torch.zeros(1, device="cuda")
@@ -28,9 +31,11 @@ def test_training_gradient_matches_oracle(cuda):
     N.check(L.pt_mlp_loss_grad(vp(dp), vp(dX), vp(dT), 1000, vp(g), vp(loss), None), "grad")
     torch.cuda.synchronize()
     ref_loss, ref_g = mlp.loss_grad(p.astype(np.float64), X, T)
-    assert abs(loss.item() / ref_loss - 1.0) < 1e-4
+    # tensor-core training: FP16 operands (11-bit significands), FP32 sums
+    assert abs(loss.item() / ref_loss - 1.0) < 2e-3
     got = g.cpu().numpy()
-    assert np.abs(got - ref_g).max() <= 1e-4 * np.abs(ref_g).max()
+    assert np.linalg.norm(got - ref_g) <= 5e-3 * np.linalg.norm(ref_g)
+    assert np.abs(got - ref_g).max() <= 2e-2 * np.abs(ref_g).max()
 
 
 def test_adam_step_decreases_loss(cuda):
