@@ -88,10 +88,11 @@ WORKLOADS = {
 # Distance of the ensemble's open x faces outside the domain, in domain
 # lengths (the field is periodic): particles stream along the guide field
 # B0 x^ at up to c (20 domain lengths per unit time, 6.3 per 10 gyro-periods),
-# so faces at the domain edge let most of them out within a gyro-period; at
-# this distance about 5 % leave within the workload's 10 gyro-periods
-# (measured on a 2^17-particle sample of the three members).
-ENSEMBLE_OPEN_X_MARGIN = 3.0
+# so faces at the domain edge let 92 % of them out within the workload's 10
+# gyro-periods.  Measured on a 2^17-particle sample of the three members
+# (positions sampled every 0.1 gyro-period): 35 % leave at a margin of 3,
+# 9.1 % at 5, 0.4 % at 6; 5.5 lets about 5 % leave.
+ENSEMBLE_OPEN_X_MARGIN = 5.5
 
 
 def train_controller(torch, records, method, face_feature=True):

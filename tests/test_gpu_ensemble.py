@@ -21,7 +21,7 @@ def _members(torch, precision, method="dop853"):
     specs = [  # grid, particles, tolerance, open x (faces moved out by the margin)
         dict(n=12, npart=150, tol=1e-7, open_x=False, margin=0.0, seed=51),
         dict(n=16, npart=300, tol=1e-9, open_x=True, margin=0.0, seed=52),
-        dict(n=20, npart=600, tol=1e-8, open_x=True, margin=0.5, seed=53),
+        dict(n=20, npart=600, tol=1e-8, open_x=True, margin=0.1, seed=53),
     ]
     probs, members = [], []
     for sp in specs:
