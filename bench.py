@@ -969,27 +969,32 @@ def ensemble_leg(args, dev, stream):
 
 
 def learned_leg(args, dev, stream):
-    """The learned-controller workload: a controller trained on accepted-step records of the
-    plain integrator on the headline shape (DOP853, 256^3, eta J) with field seed 10, then
-    evaluated with field seed 11, 2^20 particles, DOP853 rtol 1e-10 (exact
-    FP64): rejected fraction, attempts/s, accepted steps/s and simulated
-    particle-time per second against the classical controller."""
+    """The learned-controller workload (DOP853 rtol 1e-10, 256^3 with eta J):
+    controllers trained on accepted-step records of the plain integrator with
+    field seed 10 (the nine-input network, and the eight-input one without
+    the cell-face input), then evaluated with field seed 11 on 2^20
+    particles: the exact FP64 kernel with the classical controller (the
+    plain kernel), with either network, and the mixed-precision kernel (FP32
+    fields and gather) with the classical controller, the network, face-capped
+    steps and both -- accepted steps/s, attempts, rejected fraction and
+    simulated particle time per second, and the energy error of the mixed
+    variants against the exact kernel after one gyro-period."""
     import torch
-    from particles_gb300 import Fields, fields, initial, learned, params
+    from particles_gb300 import Fields, errors, fields, initial, learned, params
     cfg = WORKLOADS["dop853-256"]
     npart, window = cfg["npart"], cfg["window"]
+    steps, warm = min(args.steps, 8), min(args.warmup, 3)
     tmax = cfg["periods"] * T0
     prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=tmax, atol=cfg["tol"],
                              rtol=cfg["tol"], facmin=0.333, facmax=6.0, safe=0.9, beta=0.0)
     tg = params.time_grid(cfg["periods"], tmax)
     d_time = torch.tensor(tg, device=dev)
-    L = None
 
-    def setup(seed):
+    def setup(seed, precisions=("fp64",)):
         uu, bb, jj = fields.snapshot(cfg["n"], db_rms=cfg["db_rms"], v_rms=cfg["v_rms"],
                                      vunit=VUN, spectrum=cfg["spectrum"], nmin=1.0,
                                      nmax=cfg["nmax"], seed=seed, with_j=True, backend="torch")
-        f = Fields(uu, bb, jj, stream=stream.cuda_stream)
+        fs = {p: Fields(uu, bb, jj, precision=p, stream=stream.cuda_stream) for p in precisions}
         del uu, bb, jj
         torch.cuda.empty_cache()
         s0 = initial.isotropic_state(npart, seed, gamma_range=cfg["gamma"])
@@ -997,11 +1002,13 @@ def learned_leg(args, dev, stream):
         st[:, 0, :6] = torch.tensor(s0, device=dev)
         cnt = torch.zeros((npart, 3), dtype=torch.int64, device=dev)
         status = torch.zeros(npart, dtype=torch.int32, device=dev)
-        carry = torch.zeros(int(f._L.pt_carry_bytes(npart)), dtype=torch.uint8, device=dev)
-        return f, st, cnt, status, carry
+        carry = torch.zeros(int(fs["fp64"]._L.pt_carry_bytes(npart)), dtype=torch.uint8,
+                            device=dev)
+        return fs, st, cnt, status, carry
 
     # records from the classical run, field seed 10
-    f, st, cnt, status, carry = setup(10)
+    fs, st, cnt, status, carry = setup(10)
+    f = fs["fp64"]
     rec = learned.record_buffer(torch, args.records)
     t_rec = time.perf_counter()
     w = 0
@@ -1025,34 +1032,39 @@ def learned_leg(args, dev, stream):
     t_tr = time.perf_counter() - t_tr
     out = {"workload": "dop853-256, field seed 11 (trained on seed 10)",
            "record_seconds": t_rec, "train_seconds": t_tr, "training": training,
-           "training_8_inputs": training8,
+           "training_8_inputs": training8, "steps": steps, "warmup": warm,
            "target": "accepted log dt + at most log 2 of error headroom"}
-    f, st, cnt, status, carry = setup(11)
+    fs, st, cnt, status, carry = setup(11, ("fp64", "fp32"))
     snap = (st.clone(), cnt.clone(), carry.clone())
-    for name, mdl in (("classical", None), ("learned", model), ("learned_8_inputs", model8)):
+    variants = (("classical", "fp64", None, False), ("learned", "fp64", model, False),
+                ("learned_8_inputs", "fp64", model8, False), ("fp32", "fp32", None, False),
+                ("fp32_learned", "fp32", model, False), ("fp32_face", "fp32", None, True),
+                ("fp32_learned_face", "fp32", model, True))
+    for name, prec, mdl, face in variants:
+        f = fs[prec]
         st.copy_(snap[0]); cnt.copy_(snap[1]); carry.copy_(snap[2])
         launch = tune(args, f, "dop853", prm, d_time, st, stream, window * T0, eta=cfg["eta"],
-                      model=mdl)
+                      model=mdl, face_steps=face)
         ordq = QueueOrder(torch, cnt, enabled=not args.no_order,
                           cells=(cfg["n"],) * 3 if args.order == "brick" else None, d_carry=carry)
         w = 0
-        for _ in range(args.warmup):
+        for _ in range(warm):
             w += 1
             o = ordq.before()
             f.run_device("dop853", prm, d_time, st, cnt, status, carry, eta=cfg["eta"],
                          t_stop=w * window * T0, time_budget_s=900.0,
-                         stream=stream.cuda_stream, order=o, model=mdl)
+                         stream=stream.cuda_stream, order=o, model=mdl, face_steps=face)
             ordq.after()
         stream.synchronize()
         c0 = cnt.sum(0).cpu().numpy()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             w += 1
             o = ordq.before()
             f.run_device("dop853", prm, d_time, st, cnt, status, carry, eta=cfg["eta"],
                          t_stop=w * window * T0, time_budget_s=900.0,
-                         stream=stream.cuda_stream, order=o, model=mdl)
+                         stream=stream.cuda_stream, order=o, model=mdl, face_steps=face)
             ordq.after()
         e1.record(stream)
         stream.synchronize()
@@ -1063,19 +1075,41 @@ def learned_leg(args, dev, stream):
                      "attempts_per_s": float(d[0]) / sec,
                      "rejected_fraction": float(d[2] / max(d[0], 1)),
                      "attempts": int(d[0]), "accepted": int(d[1]),
-                     "particle_gyroperiods_per_s": npart * window * args.steps / sec,
-                     "stopped_particles": stopped, "launch": launch}
+                     "particle_gyroperiods_per_s": npart * window * steps / sec,
+                     "stopped_particles": stopped, "launch": launch, "precision": prec}
+    # energy error of every variant against the exact kernel after one gyro-period
+    na = min(16384, npart)
+    res = {}
+    for name, prec, mdl, face in variants:
+        s1 = torch.zeros((na, tg.size, 8), dtype=torch.float64, device=dev)
+        s1[:, 0] = snap[0][:na, 0]
+        c1 = torch.zeros((na, 3), dtype=torch.int64, device=dev)
+        q1 = torch.zeros(na, dtype=torch.int32, device=dev)
+        k1 = torch.zeros(int(fs[prec]._L.pt_carry_bytes(na)), dtype=torch.uint8, device=dev)
+        fs[prec].run_device("dop853", prm, d_time, s1, c1, q1, k1, eta=cfg["eta"],
+                            t_stop=tg[1] * (1 + 1e-12), time_budget_s=900.0,
+                            stream=stream.cuda_stream, model=mdl, face_steps=face)
+        stream.synchronize()
+        res[name] = s1.cpu().numpy()
+    for name, *_ in variants[1:]:
+        out[name]["accuracy_1_gyroperiod"] = errors.report(res["classical"], res[name],
+                                                           rows=(1,))["rows"]["1"]
     model.close()
     model8.close()
-    f.close()
+    for f in fs.values():
+        f.close()
     c = out["classical"]
-    for name in ("learned", "learned_8_inputs"):
+    for name, *_ in variants[1:]:
         l = out[name]
+        l["over_plain_exact"] = {"accepted": l["accepted_steps_per_s"] / c["accepted_steps_per_s"],
+                                 "simulated_time": l["particle_gyroperiods_per_s"]
+                                 / c["particle_gyroperiods_per_s"],
+                                 "attempts": l["attempts"] / c["attempts"]}
+    for name in ("learned", "learned_8_inputs"):
         sfx = "" if name == "learned" else "_8_inputs"
-        out["accepted_steps_per_s_ratio" + sfx] = l["accepted_steps_per_s"] / c["accepted_steps_per_s"]
-        out["physics_rate_ratio" + sfx] = (l["particle_gyroperiods_per_s"]
-                                           / c["particle_gyroperiods_per_s"])
-        out["attempts_ratio" + sfx] = l["attempts"] / c["attempts"]
+        for key, sub in (("accepted_steps_per_s_ratio", "accepted"),
+                         ("physics_rate_ratio", "simulated_time"), ("attempts_ratio", "attempts")):
+            out[key + sfx] = out[name]["over_plain_exact"][sub]
     return out
 
 
@@ -1097,10 +1131,10 @@ def targets(line):
     accuracy."""
     t = {}
     roof = line.get("roofline", {})
-    t["plain_exact_frac_of_fp64_fma_peak"] = roof.get("frac")
-    t["plain_exact_frac_of_no_fma_peak"] = roof.get("frac_of_no_fma_peak")
+    t["exact_frac_fp64_peak"] = roof.get("frac")
+    t["exact_frac_no_fma_peak"] = roof.get("frac_of_no_fma_peak")
     if "plain_fma" in line:
-        t["plain_fma_frac_of_fp64_fma_peak"] = line["plain_fma"]["roofline"]["frac"]
+        t["fma_frac_fp64_peak"] = line["plain_fma"]["roofline"]["frac"]
     mx = line.get("mixed")
     if mx:
         ov, ph = mx["over_plain_exact"], mx["physics_rate_over_plain_exact"]
@@ -1110,29 +1144,33 @@ def targets(line):
                                                           "fp32_learned", "fp32_learned_face")
                 if k in mx["accepted_steps_per_s"]}
         best = max(pick, key=pick.get)
-        t["mixed_learned_variant"] = best
-        t["mixed_learned_over_plain_exact"] = {"accepted": ov[best], "simulated_time": ph[best]}
-        t["mixed_learned_over_plain_fma"] = {
-            "accepted": pick[best] / fma,
-            "simulated_time": mx["detail"][best]["particle_gyroperiods_per_s"] / fma_ph}
-        nf = best.replace("_face", "")
-        if nf != best and nf in ov:
-            t["mixed_learned_no_face_over_plain_exact"] = {"accepted": ov[nf],
-                                                           "simulated_time": ph[nf]}
+        t["mixed_learned_rk5"] = {
+            "variant": best, "exact": {"accepted": ov[best], "simulated_time": ph[best]},
+            "fma": {"accepted": pick[best] / fma,
+                    "simulated_time": mx["detail"][best]["particle_gyroperiods_per_s"] / fma_ph}}
         acc = mx.get("accuracy", {}).get(best)
         if acc:
             last = max(acc["rows"], key=int)
             r1, rl = acc["rows"]["1"], acc["rows"][last]
-            t["mixed_learned_energy_err"] = {
+            t["mixed_learned_rk5_err"] = {
                 "t1": {"median": r1["energy_rel_err_median"],
                        "frac_le_1e-6": r1["fraction_energy_err_le_1e-6"]},
                 f"t{last}": {"ks": rl["ks_energy"], "ks_bound": acc.get("ks_bound"),
                              "mean": rl["mean_energy_rel_err"]}}
     if "learned" in line:
         lr = line["learned"]
-        t["learned_dop853_over_classical"] = {
+        t["learned_vs_classical_dop853"] = {
             "simulated_time": lr["physics_rate_ratio"], "attempts": lr["attempts_ratio"],
             "simulated_time_8_inputs": lr.get("physics_rate_ratio_8_inputs")}
+        ml = {k: lr[k] for k in ("fp32_learned", "fp32_learned_face") if k in lr}
+        if ml:
+            best = max(ml, key=lambda k: ml[k]["over_plain_exact"]["simulated_time"])
+            acc = ml[best].get("accuracy_1_gyroperiod", {})
+            t["mixed_learned_dop853"] = {
+                "variant": best, **{k: v for k, v in ml[best]["over_plain_exact"].items()
+                                    if k != "attempts"},
+                "err_median_t1": acc.get("energy_rel_err_median"),
+                "frac_le_1e-6_t1": acc.get("fraction_energy_err_le_1e-6")}
     return {k: v for k, v in t.items() if v is not None}
 
 
@@ -1149,7 +1187,7 @@ def compact_line(line, legs_path):
     out["roofline"] = {"bound": roof["bound"], "achieved": roof["achieved"],
                        "peak": roof["peak"], "unit": roof["unit"], "frac": roof["frac"],
                        "traffic": roof.get("traffic"),
-                       "peak_source": "FP64 FMA peak measured live (pt_probe_peak)",
+                       "peak_source": "FP64 FMA rate measured live",
                        "frac_of_no_fma_peak": roof.get("frac_of_no_fma_peak")}
     for k in ("e2e", "cpu_baseline", "parity", "clocks", "gpu_launches", "rejected_fraction",
               "stopped_particles"):
@@ -1160,9 +1198,10 @@ def compact_line(line, legs_path):
                                                  "d2h_bytes_per_step")}
     if "parity" in out:
         out["parity"] = {k: out["parity"][k] for k in ("bitwise", "particles", "mismatched")}
-    out["targets"] = targets(line)
     out["legs"] = legs_path
-    return _r(out)
+    out = _r(out)
+    out["targets"] = _r(targets(line), 3)
+    return out
 
 
 def main():
@@ -1385,26 +1424,6 @@ def main():
         del d_state, d_cnt, d_status, d_carry
         torch.cuda.empty_cache()
         line["mixed"] = mixed_leg(args, dev, stream, peak)
-    if "mixed" in line:
-        # the headline ratios in one place: mixed precision with the learned
-        # controller against the plain exact kernel, and their accuracy
-        mx = line["mixed"]
-        acc1 = {k: v["rows"]["1"] for k, v in mx.get("accuracy", {}).items() if "1" in v["rows"]}
-        line["targets"] = {
-            "plain_roofline_frac_of_fma_peak": roof["frac"],
-            "plain_roofline_frac_of_no_fma_peak": roof["frac_of_no_fma_peak"],
-            "mixed_learned_accepted_over_plain": {
-                k: mx["over_plain_exact"][k] for k in ("bf16_learned", "bf16_learned_face")},
-            "mixed_learned_simulated_time_over_plain": {
-                k: mx["physics_rate_over_plain_exact"][k]
-                for k in ("bf16_learned", "bf16_learned_face")},
-            "energy_rel_err_median_at_1_gyroperiod": {
-                k: acc1[k]["energy_rel_err_median"] for k in ("bf16_learned", "bf16_learned_face")
-                if k in acc1},
-            "fraction_energy_err_le_1e-6_at_1_gyroperiod": {
-                k: acc1[k]["fraction_energy_err_le_1e-6"]
-                for k in ("bf16_learned", "bf16_learned_face") if k in acc1},
-        }
     if not args.no_learned and "learned" in legs and rank == 0 and args.workload == "dop853-256":
         torch.cuda.empty_cache()
         line["learned"] = learned_leg(args, dev, stream)

@@ -70,7 +70,12 @@ def _full_line():
                   "physics_rate_over_plain_exact": {k: 4.56789 for k in names},
                   "accuracy": {k: acc for k in names[1:]}},
         "learned": {"physics_rate_ratio": 0.95612345, "attempts_ratio": 0.812345,
-                    "physics_rate_ratio_8_inputs": 0.9412345},
+                    "physics_rate_ratio_8_inputs": 0.9412345,
+                    **{k: {"over_plain_exact": {"accepted": 5.123456, "simulated_time": 5.98765,
+                                                "attempts": 0.5123},
+                           "accuracy_1_gyroperiod": {"energy_rel_err_median": 2.6789e-9,
+                                                     "fraction_energy_err_le_1e-6": 0.998123}}
+                       for k in ("fp32_learned", "fp32_learned_face")}},
         "ensemble": {"a": "e" * 5000},
     }
 
