@@ -249,8 +249,10 @@ void attach_fields(const pt_fields *f, PtRun &R)
     R.fld16 = f->rec16;
     R.bscale = f->bscale;
     for (int i = 0; i < 3; ++i) R.nb[i] = f->nb[i];
-    R.nrec = (f->precision == PT_PREC_BF16 || f->precision == PT_PREC_FP32)
-                 ? (int64_t)f->nb[0] * f->nb[1] * f->nb[2] * 729 : f->nodes;
+    const int64_t nbk = (int64_t)f->nb[0] * f->nb[1] * f->nb[2];
+    R.nrec = f->precision == PT_PREC_BF16 ? nbk * 729                 /* halo bricks */
+           : f->precision == PT_PREC_FP32 ? nbk * 512                 /* compact bricks */
+           : f->nodes;
     R.oob = f->scratch + 2;
 }
 

@@ -1,7 +1,7 @@
 /*
  * pt_fields.cu -- field handles of the C ABI: the snapshot converted once on
- * the device into the store of the handle's precision (FP64 or FP32 node
- * records, BF16 bricks), freed with the handle.  The reference keeps uu, bb
+ * the device into the store of the handle's precision (FP64 node records,
+ * compact FP32 bricks, BF16 halo bricks), freed with the handle.  The reference keeps uu, bb
  * in module fields (sources/fields.F90:35, :51-76); the GPU holds this copy.
  */
 #include <cuda_bf16.h>
@@ -33,33 +33,36 @@ __global__ void k_pack_records64(int64_t nn, const double *__restrict__ uu,
     }
 }
 
-/* Planar reference layout -> FP32 8^3 bricks with a one-node halo on the
- * high faces (9^3 records per brick, record (lx, ly, lz) of brick (bx, by,
- * bz) holding node ((8 bx + lx) mod d0, ...)), so every trilinear stencil
- * reads one brick.  A record is 8 floats {U, B, 0, 0} (32 B, one 256-bit
- * load) or 16 floats {U, B, J, 0...} (64 B, two).  One thread per record. */
-__global__ void k_pack_bricks32(int32_t d0, int32_t d1, int32_t d2, int32_t nbx, int32_t nby,
-                                int64_t nrec, const double *__restrict__ uu,
-                                const double *__restrict__ bb, const double *__restrict__ jj,
-                                int nc, float *__restrict__ rec)
+/* Planar reference layout -> the FP32 store: 8^3-node bricks without a halo
+ * (bricks x-fastest, nodes x-fastest inside a brick; node n of brick b is
+ * store node 512 b + n), per node a 32-B record {Ux, Uy, Uz, Bx, By, Bz, 0, 0}
+ * or, with J, {Ux, Uy, Uz, Bx, By, Bz, Jx, Jy} and Jz in a second plane.
+ * Padding nodes of partial bricks (beyond dm) hold zeros and are never
+ * gathered.  One thread per store node. */
+__global__ void k_pack_f32(int32_t d0, int32_t d1, int32_t d2, int32_t nbx, int32_t nby,
+                           int64_t nrec, const double *__restrict__ uu,
+                           const double *__restrict__ bb, const double *__restrict__ jj,
+                           float *__restrict__ rec)
 {
     const int64_t nn = (int64_t)d0 * d1 * d2;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrec;
          r += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t b = r / 729;
-        const int t = (int)(r - b * 729);
+        const int64_t b = r >> 9;
+        const int t = (int)(r & 511);
         const int bx = (int)(b % nbx), by = (int)((b / nbx) % nby), bz = (int)(b / ((int64_t)nbx * nby));
-        const int i = (bx * 8 + t % 9) % d0, j = (by * 8 + (t / 9) % 9) % d1, k = (bz * 8 + t / 81) % d2;
-        const int64_t g = i + (int64_t)d0 * (j + (int64_t)d1 * k);
-        float4 *o = reinterpret_cast<float4 *>(rec + r * nc);
-        o[0] = make_float4((float)uu[g], (float)uu[g + nn], (float)uu[g + 2 * nn], (float)bb[g]);
-        if (nc == 16) {
-            o[1] = make_float4((float)bb[g + nn], (float)bb[g + 2 * nn], (float)jj[g], (float)jj[g + nn]);
-            o[2] = make_float4((float)jj[g + 2 * nn], 0.f, 0.f, 0.f);
-            o[3] = make_float4(0.f, 0.f, 0.f, 0.f);
-        } else {
-            o[1] = make_float4((float)bb[g + nn], (float)bb[g + 2 * nn], 0.f, 0.f);
+        const int i = bx * 8 + (t & 7), j = by * 8 + ((t >> 3) & 7), k = bz * 8 + (t >> 6);
+        const bool in = i < d0 && j < d1 && k < d2;
+        const int64_t g = in ? i + (int64_t)d0 * (j + (int64_t)d1 * k) : 0;
+        float v[9];
+        for (int c = 0; c < 3; ++c) {
+            v[c] = in ? (float)uu[g + c * nn] : 0.f;
+            v[3 + c] = in ? (float)bb[g + c * nn] : 0.f;
+            v[6 + c] = (in && jj) ? (float)jj[g + c * nn] : 0.f;
         }
+        float4 *o = reinterpret_cast<float4 *>(rec + 8 * r);
+        o[0] = make_float4(v[0], v[1], v[2], v[3]);
+        o[1] = make_float4(v[4], v[5], v[6], v[7]);
+        if (jj) rec[8 * nrec + r] = v[8];
     }
 }
 
@@ -184,8 +187,9 @@ static int fields_create_impl(const int32_t dm[3], const double *uu, const doubl
         f->bytes = nbk * 729 * f->nc16 * 2 + nbk * ns * 4 + 256;
     } else if (precision == PT_PREC_FP32) {
         const int64_t nbk = (int64_t)f->nb[0] * f->nb[1] * f->nb[2];
-        PT_CU(cudaMalloc(&f->rec32, (size_t)nbk * 729 * f->nc32 * sizeof(float)));
-        f->bytes = nbk * 729 * f->nc32 * (int64_t)sizeof(float) + 256;
+        const int64_t fl = nbk * 512 * (f->has_j ? 9 : 8);     /* floats of the store */
+        PT_CU(cudaMalloc(&f->rec32, (size_t)fl * sizeof(float)));
+        f->bytes = fl * (int64_t)sizeof(float) + 256;
     } else {
         PT_CU(cudaMalloc(&f->rec64, (size_t)nn * f->nc * sizeof(double)));
         f->bytes = (int64_t)nn * f->nc * sizeof(double) + 256;
@@ -215,9 +219,9 @@ static int fields_create_impl(const int32_t dm[3], const double *uu, const doubl
             k_pack_bricks16<6><<<(unsigned)nbk, 768, 0, stream>>>(dm[0], dm[1], dm[2], f->nb[0], f->nb[1],
                                                                   d_uu, d_bb, d_jj, f->rec16, f->bscale);
         else if (precision == PT_PREC_FP32)
-            k_pack_bricks32<<<(int)((nbk * 729 + 255) / 256 < 65536 ? (nbk * 729 + 255) / 256 : 65536), 256, 0,
-                              stream>>>(dm[0], dm[1], dm[2], f->nb[0], f->nb[1], nbk * 729, d_uu, d_bb,
-                                        d_jj, f->nc32, f->rec32);
+            k_pack_f32<<<(int)((nbk * 512 + 255) / 256 < 65536 ? (nbk * 512 + 255) / 256 : 65536), 256, 0,
+                         stream>>>(dm[0], dm[1], dm[2], f->nb[0], f->nb[1], nbk * 512, d_uu, d_bb,
+                                   d_jj, f->rec32);
         else
             k_pack_records64<<<(int)blocks, 256, 0, stream>>>(nn, d_uu, d_bb, d_jj, f->nc, f->rec64);
         PT_CU(cudaGetLastError());

@@ -391,11 +391,21 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
         double del = 0.0;
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
+#ifdef PT_EXACT
             double a = 0.0, e = 0.0;
             a = a + CK_C1 * K(0, c); a = a + CK_C2 * K(1, c); a = a + CK_C3 * K(2, c);
             a = a + CK_C4 * K(3, c); a = a + CK_C5 * K(4, c); a = a + CK_C6 * K(5, c);
             e = e + CK_D1 * K(0, c); e = e + CK_D2 * K(1, c); e = e + CK_D3 * K(2, c);
             e = e + CK_D4 * K(3, c); e = e + CK_D5 * K(4, c); e = e + CK_D6 * K(5, c);
+#else
+            /* c2 = c5 = d2 = 0 (:94-97): the zero terms change nothing but
+             * the sign of a zero sum, so the other builds leave them out
+             * (18 FP64 operations per attempt) */
+            static_assert(CK_C2 == 0.0 && CK_C5 == 0.0 && CK_D2 == 0.0, "Cash-Karp zero weights");
+            const double a = CK_C1 * K(0, c) + CK_C3 * K(2, c) + CK_C4 * K(3, c) + CK_C6 * K(5, c);
+            const double e = CK_D1 * K(0, c) + CK_D3 * K(2, c) + CK_D4 * K(3, c) + CK_D5 * K(4, c)
+                           + CK_D6 * K(5, c);
+#endif
             dsf[c] = a;
             sf[c] = si[c] + a;
 #ifdef PT_EXACT
@@ -562,16 +572,14 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
     const KRows K{ pt_ksm + threadIdx.x, (int)blockDim.x };
     unsigned char *const smem_tail =
         reinterpret_cast<unsigned char *>(pt_ksm) + T::ROWS * 6 * 8 * blockDim.x;
-    float *pend = nullptr;                 /* pending features, [PT_REC_NFEAT][blockDim] */
     bool have_pend = false;
     int mi = 0;                            /* member this lane draws particles from */
 #define PT_Q (MB.q(mi))
     /* the MLP weights are read by every warp at every accepted step: one
-     * copy per block in shared memory (11.9 KB) */
-    PtMlpSmem mlpw{};
-    const int mlp_bytes = (LEARN && PT_Q.mlp) ? PT_MLP_BLOB_BYTES : 0;
-    if (LEARN && PT_Q.mlp) mlpw = pt_mlp_load(PT_Q.mlp, smem_tail);
-    if (LEARN && PT_Q.rec) pend = reinterpret_cast<float *>(smem_tail + mlp_bytes) + threadIdx.x;
+     * copy per block in shared memory (11.9 KB), addressed from smem_tail
+     * where they are used; after them the pending features of a recording
+     * run, [PT_REC_NFEAT][blockDim] */
+    if (LEARN && PT_Q.mlp) (void)pt_mlp_load(PT_Q.mlp, smem_tail);
     const uint64_t t_start = pt_globaltimer();
     Lane L;
     L.p = 0; L.t = 0.0; L.dt = 0.0; L.errold = 0.0; L.tnext = 0.0; L.n = 0;
@@ -744,6 +752,8 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
                     /* time to the next cell face in units of the last step */
                     feat[8] = __logf(fminf(pt_face_time(PT_Q, si) / dtf, 1.0e6f) + 1e-30f);
                     if (PT_Q.rec) {
+                        float *const pend = reinterpret_cast<float *>(
+                            smem_tail + (PT_Q.mlp ? PT_MLP_BLOB_BYTES : 0)) + threadIdx.x;
                         if (have_pend) {
                             const unsigned long long i =
                                 atomicAdd(reinterpret_cast<unsigned long long *>(PT_Q.rec), 1ULL);
@@ -761,7 +771,7 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
                     }
                 }
                 if (PT_Q.mlp && __any_sync(0xffffffffu, want)) {
-                    const float y = pt_mlp_warp(mlpw, feat);
+                    const float y = pt_mlp_warp(pt_mlp_view(smem_tail), feat, want);
                     if (want) {
                         const double lo = PT_Q.fcmn * dt;
                         const double hi = (METHOD == PT_METHOD_DOP853 && was_rejected) ? dt : PT_Q.fcmx * dt;

@@ -37,8 +37,8 @@ struct pt_fields {
     int32_t device;
     int64_t nodes;
     double *rec64;              /* FP64 records (PT_PREC_FP64, PT_PREC_FP64_FMA) */
-    float *rec32;               /* FP32 brick records (PT_PREC_FP32) */
-    int32_t nc32;               /* FP32 record width: 8 or 16 */
+    float *rec32;               /* compact FP32 brick store (PT_PREC_FP32) */
+    int32_t nc32;               /* FP32 gather variant: 8 (U, B) or 16 (U, B, J) */
     uint4 *rec16;               /* BF16 brick records (PT_PREC_BF16) */
     float *bscale;              /* per brick: offsets and scales (16 or 24 floats) */
     int32_t nb[3];              /* bricks per axis */

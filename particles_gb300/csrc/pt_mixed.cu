@@ -20,15 +20,16 @@
  *     integer pipe (pt_convert.cuh), so an evaluation issues no FP64-pipe
  *     instruction at all (the exact FP64 evaluation issues ~290).
  *
- * Field stores (HBM), chosen by the gather policy:
- *   Both stores are 8^3-node bricks with a one-node halo on their high
- *   faces (9^3 records, bricks x-fastest, records x-fastest), so the eight
- *   corners of a stencil lie in one brick.
- *   GatherF32:   records of 8 floats {U,B,0,0} = 32 B (one 256-bit load), or
- *                16 floats {U,B,J,0...} = 64 B with eta J.
- *   GatherBrick: records of 8 BF16 {U,B,0,0} = 16 B, or 16 BF16 {U,B,J,0...}
- *                = 32 B with J; per brick and component an FP32 offset and
- *                scale, value = offset + scale * q.
+ * Field stores (HBM), chosen by the gather policy; both are 8^3-node
+ * bricks (bricks x-fastest, nodes x-fastest inside a brick):
+ *   GatherF32:   no halo; per node a 32-B record {U,B,0,0} (one sector,
+ *                one 256-bit load), with eta J {U,B,Jx,Jy} plus Jz in a
+ *                second plane (36 B): 0.67 / 0.45 of the FP64 records.
+ *   GatherBrick: a one-node halo on the high faces (9^3 records), so the
+ *                eight corners of a stencil lie in one brick and share one
+ *                scale load; records of 8 BF16 {U,B,0,0} = 16 B, or 16 BF16
+ *                {U,B,J,0...} = 32 B with J; per brick and component an FP32
+ *                offset and scale, value = offset + scale * q.
  */
 #include <cuda_runtime.h>
 #include <math.h>
@@ -59,62 +60,81 @@ __device__ __forceinline__ int64_t pt_brick_base(const PtRun &P, const int32_t l
     return b * 729 + (l[0] & 7) + 9 * (l[1] & 7) + 81 * (l[2] & 7);
 }
 
-/* Trilinear sums over FP32 bricks: the brick layout of the BF16 store (8^3
- * owned nodes + a one-node halo on the high faces, 9^3 records), records of
- * 8 floats {U, B, 0, 0} (32 B, one 256-bit load) or 16 floats {U, B, J, 0...}
- * (64 B, two), values stored as they are (no offset/scale). */
+/* Trilinear sums over the FP32 store: 8^3-node bricks without a halo (bricks
+ * x-fastest, nodes x-fastest inside a brick; P.nrec nodes in all, padding
+ * included).  Plane A holds one 32-B record per node, {Ux, Uy, Uz, Bx, By,
+ * Bz, 0, 0} or with eta J {Ux, Uy, Uz, Bx, By, Bz, Jx, Jy} (one 32-B sector,
+ * one 256-bit load); with J plane C holds Jz (4 B).  Values are stored as
+ * they are (no offset/scale).  A corner may lie in a neighbouring brick, so
+ * the node index of (x, y, z) is the sum of one term per axis,
+ * X(x) + Y(y) + Z(z), formed for the left and the right index of each axis. */
 template <int NC>
 struct GatherF32 {
     static constexpr int NV = (NC == 16) ? 9 : 6;
-    static __device__ __forceinline__ void load_node(const float *__restrict__ fld, int64_t node,
-                                                     float v[NV])
+    static __device__ __forceinline__ void load_node(const float *__restrict__ fld, int64_t nrec,
+                                                     int64_t node, float v[NV])
     {
         float t[8];
-        pt_ld8(fld + node * NC, t);
+        pt_ld8(fld + node * 8, t);
 #pragma unroll
         for (int c = 0; c < 6; ++c) v[c] = t[c];
         if (NV == 9) {
             v[6 % NV] = t[6];
             v[7 % NV] = t[7];
-            float u[8];
-            pt_ld8(fld + node * NC + 8, u);
-            v[8 % NV] = u[0];
+            v[8 % NV] = __ldg(fld + 8 * nrec + node);
         }
     }
-    /* Corner loader for the learned controller's features (the brick of l
-     * holds every corner). */
+    /* The per-axis node-index terms of the left ([0]) and right ([1]) index. */
+    struct Axes {
+        int64_t x[2], y[2], z[2];
+    };
+    static __device__ __forceinline__ Axes axes(const PtRun &P, const int32_t l[3], const int32_t r[3])
+    {
+        Axes A;
+        const int64_t sy = (int64_t)P.nb[0] * 512, sz = sy * P.nb[1];
+        A.x[0] = (int64_t)(l[0] >> 3) * 512 + (l[0] & 7);
+        A.x[1] = (int64_t)(r[0] >> 3) * 512 + (r[0] & 7);
+        A.y[0] = (int64_t)(l[1] >> 3) * sy + ((l[1] & 7) << 3);
+        A.y[1] = (int64_t)(r[1] >> 3) * sy + ((r[1] & 7) << 3);
+        A.z[0] = (int64_t)(l[2] >> 3) * sz + ((l[2] & 7) << 6);
+        A.z[1] = (int64_t)(r[2] >> 3) * sz + ((r[2] & 7) << 6);
+        return A;
+    }
+    /* Corner loader for the learned controller's features. */
     struct Loader {
         static constexpr int NJ = (NV == 9) ? 3 : 0;
         const float *fld;
-        int64_t base;
+        int64_t nrec;
+        Axes A;
+        unsigned long long *oob;           /* bounds-checked builds */
         __device__ __forceinline__ void corner(int bx, int by, int bz, float v[9]) const
         {
-            load_node(fld, base + bx + 9 * by + 81 * bz, v);
+            load_node(fld, nrec, PT_CHK(*this, A.x[bx] + A.y[by] + A.z[bz], nrec), v);
         }
     };
     static __device__ __forceinline__ Loader loader(const PtRun &P, const int32_t l[3],
-                                                    const int32_t *)
+                                                    const int32_t r[3])
     {
         Loader L;
-        int64_t b;
         L.fld = P.fld32;
-        L.base = pt_brick_base(P, l, b);
+        L.nrec = P.nrec;
+        L.A = axes(P, l, r);
+        L.oob = P.oob;
         return L;
     }
     static __device__ __forceinline__ void gather(const PtRun &P, const int32_t l[3],
-                                                  const int32_t *, const float w8[8], float acc[NV])
+                                                  const int32_t r[3], const float w8[8], float acc[NV])
     {
-        int64_t b;
-        const int64_t base = pt_brick_base(P, l, b);
+        const Axes A = axes(P, l, r);
         if (P.near) {                          /* interpolate_near: the node l */
-            load_node(P.fld32, PT_CHK(P, base, P.nrec), acc);
+            load_node(P.fld32, P.nrec, PT_CHK(P, A.x[0] + A.y[0] + A.z[0], P.nrec), acc);
             return;
         }
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             float v[NV];
-            load_node(P.fld32, PT_CHK(P, base + ((q & 4) ? 1 : 0) + ((q & 2) ? 9 : 0) + ((q & 1) ? 81 : 0),
-                                      P.nrec), v);
+            load_node(P.fld32, P.nrec,
+                      PT_CHK(P, A.x[(q >> 2) & 1] + A.y[(q >> 1) & 1] + A.z[q & 1], P.nrec), v);
 #pragma unroll
             for (int c = 0; c < NV; ++c) acc[c] = (q == 0) ? w8[0] * v[c] : fmaf(w8[q], v[c], acc[c]);
         }

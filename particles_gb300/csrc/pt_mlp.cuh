@@ -6,8 +6,9 @@
  * specification and the time to the next cell face (a model trained with
  * that input zeroed is the 8 -> 64 -> 64 -> 1 network).  Inference runs on
  * the tensor cores with warp-level mma.sync m16n8k16 (FP16 operands, FP32
- * accumulate): the 32 lanes of a warp are the 32 rows of the activation
- * matrix (two m16 tiles).  The layer-1 input K of 9 is zero-padded to 16, the
+ * accumulate): the lanes of a warp are the rows of the activation matrix
+ * (two m16 tiles, or one when a warp vote finds at most 16 lanes that want a
+ * proposal and a shuffle regroups their rows).  The layer-1 input K of 9 is zero-padded to 16, the
  * layer-3 output N of 1 to 8.  A layer's FP32 accumulators convert in place
  * into the next layer's FP16 A fragments (the C layout of two adjacent n8
  * tiles is the A layout of one k16 tile), so only the input and the output
@@ -80,13 +81,10 @@ __device__ __forceinline__ uint32_t pt_silu_h2(float h0, float h1)
     return *reinterpret_cast<const uint32_t *>(&y);
 }
 
-/* Copies the blob into shared memory (whole block, before the main loop). */
-__device__ __forceinline__ PtMlpSmem pt_mlp_load(const unsigned char *blob, unsigned char *smem)
+/* The blob's parts in shared memory at smem (no data movement: recomputed
+ * where it is used, so no pointer stays live in registers). */
+__device__ __forceinline__ PtMlpSmem pt_mlp_view(const unsigned char *smem)
 {
-    const uint4 *src = reinterpret_cast<const uint4 *>(blob);
-    uint4 *dst = reinterpret_cast<uint4 *>(smem);
-    for (int i = threadIdx.x; i < PT_MLP_BLOB_BYTES / 16; i += blockDim.x) dst[i] = src[i];
-    __syncthreads();
     PtMlpSmem m;
     m.frag = reinterpret_cast<const uint2 *>(smem);
     m.b1 = reinterpret_cast<const float *>(smem + PT_MLP_NFRAG * 8);
@@ -97,26 +95,43 @@ __device__ __forceinline__ PtMlpSmem pt_mlp_load(const unsigned char *blob, unsi
     return m;
 }
 
-/* y = MLP(x) for the 32 lanes of a converged warp; every lane passes its own
- * nine raw features and receives its own output (log trial step). */
-static __device__ __noinline__ float pt_mlp_warp(const PtMlpSmem &M, const float x[PT_MLP_NIN])
+/* Copies the blob into shared memory (whole block, before the main loop). */
+__device__ __forceinline__ PtMlpSmem pt_mlp_load(const unsigned char *blob, unsigned char *smem)
+{
+    const uint4 *src = reinterpret_cast<const uint4 *>(blob);
+    uint4 *dst = reinterpret_cast<uint4 *>(smem);
+    for (int i = threadIdx.x; i < PT_MLP_BLOB_BYTES / 16; i += blockDim.x) dst[i] = src[i];
+    __syncthreads();
+    return pt_mlp_view(smem);
+}
+
+/* The k-th (0-based) set bit of m, for k < popc(m): a binary search on
+ * population counts (five steps, integer pipe). */
+__device__ __forceinline__ int pt_nth_set_bit(uint32_t m, int k)
+{
+    int pos = 0;
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        const int c = __popc(m & ((1u << s) - 1u));
+        if (k >= c) { k -= c; m >>= s; pos += s; }
+    }
+    return pos;
+}
+
+/* The MLP on one m16 tile of the activation matrix: row g of the tile holds
+ * the features of lane r0, row g + 8 those of lane r1 (xp: every lane's
+ * normalised, packed features).  Returns the layer-3 accumulators of this
+ * lane's C fragment (column 0 is the output: row g in c3[0] and row g + 8 in
+ * c3[2] of the lanes with q == 0). */
+__device__ __forceinline__ void pt_mlp_tile(const PtMlpSmem &M, const uint32_t xp[5], int r0, int r1,
+                                            float c3[4])
 {
     const int lane = threadIdx.x & 31;
-    const int g = lane >> 2, q = lane & 3;
-    uint32_t xp[5];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-        xp[i] = pt_pack_h2((x[2 * i] - M.mu[2 * i]) * M.isd[2 * i],
-                           (x[2 * i + 1] - M.mu[2 * i + 1]) * M.isd[2 * i + 1]);
-    xp[4] = pt_pack_h2((x[8] - M.mu[8]) * M.isd[8], 0.0f);
-    /* the warp's 32 rows are two m16 tiles; every weight fragment and bias is
-     * loaded once and applied to both */
-    uint32_t a1[2][4];
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
-        /* layer-1 A fragment: rows g and g + 8 of this m tile, columns 2q, 2q+1
-         * (features 0..7) and 2q + 8, 2q + 9 (feature 8 in column 8, q == 0) */
-        const int r0 = 16 * mt + g, r1 = r0 + 8;
+    const int q = lane & 3;
+    /* layer-1 A fragment: columns 2q, 2q+1 (features 0..7) and 2q + 8, 2q + 9
+     * (feature 8 in column 8, q == 0) */
+    uint32_t a1[4];
+    {
         uint32_t v0 = 0, v1 = 0;
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -126,64 +141,85 @@ static __device__ __noinline__ float pt_mlp_warp(const PtMlpSmem &M, const float
         }
         const uint32_t f0 = __shfl_sync(0xffffffffu, xp[4], r0);
         const uint32_t f1 = __shfl_sync(0xffffffffu, xp[4], r1);
-        a1[mt][0] = v0; a1[mt][1] = v1;
-        a1[mt][2] = (q == 0) ? f0 : 0u; a1[mt][3] = (q == 0) ? f1 : 0u;
+        a1[0] = v0; a1[1] = v1;
+        a1[2] = (q == 0) ? f0 : 0u; a1[3] = (q == 0) ? f1 : 0u;
     }
     const float2 *b1 = reinterpret_cast<const float2 *>(M.b1);
     const float2 *b2 = reinterpret_cast<const float2 *>(M.b2);
     /* layer 1 -> SiLU -> layer-2 A fragments */
-    uint32_t a2[2][4][4];
+    uint32_t a2[4][4];
 #pragma unroll
     for (int nt = 0; nt < 8; ++nt) {
         const float2 bb = b1[4 * nt + q];
         const uint2 w = M.frag[PT_MLP_FRAG_W1 + nt * 32 + lane];
         const int kt = nt >> 1, hiw = (nt & 1) * 2;
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-            float c[4] = { bb.x, bb.y, bb.x, bb.y };
-            pt_mma16816(c, a1[mt], w);
-            a2[mt][kt][hiw] = pt_silu_h2(c[0], c[1]);
-            a2[mt][kt][hiw + 1] = pt_silu_h2(c[2], c[3]);
-        }
+        float c[4] = { bb.x, bb.y, bb.x, bb.y };
+        pt_mma16816(c, a1, w);
+        a2[kt][hiw] = pt_silu_h2(c[0], c[1]);
+        a2[kt][hiw + 1] = pt_silu_h2(c[2], c[3]);
     }
     /* layer 2 -> SiLU -> layer 3, one k16 slice of layer 3 per pair of
-     * layer-2 n tiles; column 0 of layer 3's n8 tile is the output */
-    float c3[2][4];
-#pragma unroll
-    for (int mt = 0; mt < 2; ++mt) { c3[mt][0] = c3[mt][2] = M.b3[0]; c3[mt][1] = c3[mt][3] = 0.0f; }
+     * layer-2 n tiles */
+    c3[0] = c3[2] = M.b3[0];
+    c3[1] = c3[3] = 0.0f;
 #pragma unroll
     for (int kt3 = 0; kt3 < 4; ++kt3) {
-        uint32_t a3[2][4];
+        uint32_t a3[4];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int nt = 2 * kt3 + h;
             const float2 bb = b2[4 * nt + q];
-            float c[2][4] = { { bb.x, bb.y, bb.x, bb.y }, { bb.x, bb.y, bb.x, bb.y } };
+            float c[4] = { bb.x, bb.y, bb.x, bb.y };
 #pragma unroll
-            for (int kt = 0; kt < 4; ++kt) {
-                const uint2 w = M.frag[PT_MLP_FRAG_W2 + (kt * 8 + nt) * 32 + lane];
-                pt_mma16816(c[0], a2[0][kt], w);
-                pt_mma16816(c[1], a2[1][kt], w);
-            }
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt) {
-                a3[mt][2 * h] = pt_silu_h2(c[mt][0], c[mt][1]);
-                a3[mt][2 * h + 1] = pt_silu_h2(c[mt][2], c[mt][3]);
-            }
+            for (int kt = 0; kt < 4; ++kt)
+                pt_mma16816(c, a2[kt], M.frag[PT_MLP_FRAG_W2 + (kt * 8 + nt) * 32 + lane]);
+            a3[2 * h] = pt_silu_h2(c[0], c[1]);
+            a3[2 * h + 1] = pt_silu_h2(c[2], c[3]);
         }
-        const uint2 w3 = M.frag[PT_MLP_FRAG_W3 + kt3 * 32 + lane];
-        pt_mma16816(c3[0], a3[0], w3);
-        pt_mma16816(c3[1], a3[1], w3);
+        pt_mma16816(c3, a3, M.frag[PT_MLP_FRAG_W3 + kt3 * 32 + lane]);
     }
-    /* row r0 of tile mt sits in c0 of lane 4g, row r1 in c2 of lane 4g (q == 0) */
-    float out = 0.0f;
+}
+
+/* y = MLP(x) for the lanes of a converged warp that want a proposal; every
+ * lane passes its own nine raw features and a wanting lane receives its own
+ * output (log trial step).  The rows of the activation matrix are m16 tiles:
+ * when at most 16 lanes want a proposal (a warp vote), their rows are
+ * regrouped into one tile in lane order -- half the tensor-core and SiLU
+ * work of the two tiles that 32 rows take. */
+static __device__ __forceinline__ float pt_mlp_warp(const PtMlpSmem &M, const float x[PT_MLP_NIN],
+                                                    bool want)
+{
+    const int lane = threadIdx.x & 31;
+    const int g = lane >> 2;
+    uint32_t xp[5];
 #pragma unroll
-    for (int mt = 0; mt < 2; ++mt) {
-        const int r = lane - 16 * mt;
-        const int src = 4 * (r & 7);
-        const float y0 = __shfl_sync(0xffffffffu, c3[mt][0], src);
-        const float y1 = __shfl_sync(0xffffffffu, c3[mt][2], src);
-        if (r >= 0 && r < 16) out = (r < 8) ? y0 : y1;
+    for (int i = 0; i < 4; ++i)
+        xp[i] = pt_pack_h2((x[2 * i] - M.mu[2 * i]) * M.isd[2 * i],
+                           (x[2 * i + 1] - M.mu[2 * i + 1]) * M.isd[2 * i + 1]);
+    xp[4] = pt_pack_h2((x[8] - M.mu[8]) * M.isd[8], 0.0f);
+    const uint32_t wm = __ballot_sync(0xffffffffu, want);
+    const int nw = __popc(wm);
+    const bool one = nw <= 16;                     /* warp-uniform */
+    const int rank = __popc(wm & ((1u << lane) - 1u));
+    float out = 0.0f;
+    for (int mt = 0; mt < (one ? 1 : 2); ++mt) {
+        int r0, r1, row;
+        if (one) {                                 /* rows: the wanting lanes in order */
+            r0 = (g < nw) ? pt_nth_set_bit(wm, g) : lane;
+            r1 = (g + 8 < nw) ? pt_nth_set_bit(wm, g + 8) : lane;
+            row = want ? rank : -1;
+        } else {                                   /* rows: the lanes of half mt */
+            r0 = 16 * mt + g;
+            r1 = r0 + 8;
+            row = lane - 16 * mt;
+        }
+        float c3[4];
+        pt_mlp_tile(M, xp, r0, r1, c3);
+        /* row r of the tile sits in c0 (r < 8) or c2 (r >= 8) of lane 4 (r & 7) */
+        const int src = 4 * (row & 7);
+        const float y0 = __shfl_sync(0xffffffffu, c3[0], src);
+        const float y1 = __shfl_sync(0xffffffffu, c3[2], src);
+        if (row >= 0 && row < 16) out = (row < 8) ? y0 : y1;
     }
     return out;
 }

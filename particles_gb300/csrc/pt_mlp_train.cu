@@ -433,7 +433,7 @@ __global__ void k_infer(const unsigned char *blob, const float *X, int64_t n, fl
         float x[NIN];
 #pragma unroll
         for (int i = 0; i < NIN; ++i) x[i] = (row < n) ? X[row * NIN + i] : 0.0f;
-        const float y = pt_mlp_warp(M, x);
+        const float y = pt_mlp_warp(M, x, row < n);
         if (row < n) out[row] = y;
     }
 }

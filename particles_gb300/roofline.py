@@ -95,12 +95,12 @@ def split_work(method: str, cnt: np.ndarray, *, with_eta: bool = False) -> dict:
             "eval_flops": float(evals * FLOPS["eval_j" if with_eta else "eval"])}
 
 
-# bytes one evaluation gathers from each field store: 8 corner records
-# (FP64 records 48 / 80 B; FP32 brick records 32 / 64 B; BF16 brick records
+# bytes one evaluation gathers from each field store: 8 corners (FP64
+# records 48 / 80 B; FP32 records 32 B, with J 32 + 4 B; BF16 brick records
 # 16 / 32 B plus the brick's FP32 offset/scale pairs, 48 / 80 B)
 EVAL_BYTES = {("fp64", False): 8 * 48, ("fp64", True): 8 * 80,
               ("fp64_fma", False): 8 * 48, ("fp64_fma", True): 8 * 80,
-              ("fp32", False): 8 * 32, ("fp32", True): 8 * 64,
+              ("fp32", False): 8 * 32, ("fp32", True): 8 * 36,
               ("bf16", False): 8 * 16 + 48, ("bf16", True): 8 * 32 + 80}
 
 

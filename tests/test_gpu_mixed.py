@@ -146,3 +146,23 @@ def test_near_gather_mixed_statistics(cuda, oracle_lib, precision):
     g_o, g_g = so[:, -1, 6], sg[:, -1, 6]
     assert abs(g_g.mean() / g_o.mean() - 1.0) < 2e-3
     assert 0.7 < cg[:, 1].sum() / co[:, 1].sum() < 1.4
+
+
+@pytest.mark.parametrize("with_j", [False, True])
+def test_fp32_store_size(cuda, with_j):
+    """The FP32 store keeps 32 B per node (36 B with J) in 8^3 bricks without a
+    halo: 2/3 of the FP64 records (48 B; 0.45 of 80 B with J) on a grid of
+    whole bricks, and whole bricks (zero padding) on a grid that is not."""
+    from particles_gb300 import Fields, fields
+    uu, bb = fields.snapshot(16, db_rms=0.5, v_rms=0.1, seed=3)
+    jj = np.ones_like(bb) if with_j else None
+    f64, f32 = Fields(uu, bb, jj, precision="fp64"), Fields(uu, bb, jj, precision="fp32")
+    nn = 16 ** 3
+    assert f64.nbytes == nn * (80 if with_j else 48) + 256
+    assert f32.nbytes == nn * (36 if with_j else 32) + 256
+    f64.close()
+    f32.close()
+    g = Fields(uu[:, :12, :12, :12].copy(), bb[:, :12, :12, :12].copy(),
+               None if jj is None else jj[:, :12, :12, :12].copy(), precision="fp32")
+    assert g.nbytes == 8 * 512 * (36 if with_j else 32) + 256
+    g.close()
