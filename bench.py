@@ -118,10 +118,14 @@ MIXED_VARIANTS = (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"), 
                   ("fp32_face", "fp32"), ("bf16_face", "bf16"), ("fp32_learned_face", "fp32"),
                   ("bf16_learned_face", "bf16"))
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one timed full-size window,
-# from a single-pass ncu capture of the same command
-# (profiles/k_integrate_full_size_single_pass.md)
-DRAM_BYTES_PER_WINDOW = {("dop853-256", "fp64"): 27380003072 + 4665027584}
+# DRAM bytes per attempt (dram__bytes_read.sum + dram__bytes_write.sum of one
+# launch / the attempts it made), from a one-pass ncu capture of a small case
+# of the same kernel and workload: 2^17 particles, the fourth window of the
+# benchmark's window length (the bench's own first timed window).  A run's
+# traffic per launch is this figure times the attempts of its launches.  The
+# figure is an upper estimate at full size: with 8x fewer particles, fewer
+# concurrently integrated particles share the field lines held in L2.
+DRAM_BYTES_PER_ATTEMPT = {("dop853-256", "fp64"): (5435572992 + 862161408) / 14067525}
 
 
 def parse():
@@ -314,9 +318,8 @@ def cpu_baseline(cfg, prm, tg, out, s0_all, window, warm, steps, seconds, gpu=No
     el = time.perf_counter() - t0
     acc = float(cnt[:, 1].sum() - acc0)
     base = {"value": acc / el, "unit": "particle-steps/s", "cores": nthreads, "kind": "port",
-            "sample": f"{nsub} of {s0_all.shape[0]} particles (seeded), the same {steps} timed "
-                      f"windows of {window} gyro-periods after {warm} warm-up; {int(acc)} "
-                      f"accepted steps in {el:.1f} s"}
+            "sample": f"{nsub} of {s0_all.shape[0]} particles, the same {steps} windows "
+                      f"after {warm}: {int(acc)} accepted steps in {el:.1f} s"}
     return base, (parity_check(sample, gpu, s0_all.shape[0]) if gpu is not None else None)
 
 
@@ -1127,7 +1130,7 @@ def _r(x, d=4):
 def targets(line):
     """At most ten headline figures gathered from the legs: the plain kernel's
     roofline fractions, the mixed + learned ratios against the plain exact and
-    FMA kernels (accepted steps/s and simulated time per second) and their
+    FMA kernels as [accepted steps/s, simulated time per second], and their
     accuracy."""
     t = {}
     roof = line.get("roofline", {})
@@ -1145,32 +1148,31 @@ def targets(line):
                 if k in mx["accepted_steps_per_s"]}
         best = max(pick, key=pick.get)
         t["mixed_learned_rk5"] = {
-            "variant": best, "exact": {"accepted": ov[best], "simulated_time": ph[best]},
-            "fma": {"accepted": pick[best] / fma,
-                    "simulated_time": mx["detail"][best]["particle_gyroperiods_per_s"] / fma_ph}}
+            "variant": best, "x_exact": [ov[best], ph[best]],
+            "x_fma": [pick[best] / fma, mx["detail"][best]["particle_gyroperiods_per_s"] / fma_ph]}
         acc = mx.get("accuracy", {}).get(best)
         if acc:
             last = max(acc["rows"], key=int)
             r1, rl = acc["rows"]["1"], acc["rows"][last]
             t["mixed_learned_rk5_err"] = {
-                "t1": {"median": r1["energy_rel_err_median"],
-                       "frac_le_1e-6": r1["fraction_energy_err_le_1e-6"]},
-                f"t{last}": {"ks": rl["ks_energy"], "ks_bound": acc.get("ks_bound"),
-                             "mean": rl["mean_energy_rel_err"]}}
+                "t1_median": r1["energy_rel_err_median"],
+                "t1_le_1e-6": r1["fraction_energy_err_le_1e-6"],
+                f"t{last}_ks": rl["ks_energy"], "ks_bound": acc.get("ks_bound"),
+                f"t{last}_mean": rl["mean_energy_rel_err"]}
     if "learned" in line:
         lr = line["learned"]
         t["learned_vs_classical_dop853"] = {
-            "simulated_time": lr["physics_rate_ratio"], "attempts": lr["attempts_ratio"],
-            "simulated_time_8_inputs": lr.get("physics_rate_ratio_8_inputs")}
+            "sim_time": lr["physics_rate_ratio"], "attempts": lr["attempts_ratio"],
+            "sim_time_8_inputs": lr.get("physics_rate_ratio_8_inputs")}
         ml = {k: lr[k] for k in ("fp32_learned", "fp32_learned_face") if k in lr}
         if ml:
             best = max(ml, key=lambda k: ml[k]["over_plain_exact"]["simulated_time"])
             acc = ml[best].get("accuracy_1_gyroperiod", {})
+            ox = ml[best]["over_plain_exact"]
             t["mixed_learned_dop853"] = {
-                "variant": best, **{k: v for k, v in ml[best]["over_plain_exact"].items()
-                                    if k != "attempts"},
-                "err_median_t1": acc.get("energy_rel_err_median"),
-                "frac_le_1e-6_t1": acc.get("fraction_energy_err_le_1e-6")}
+                "variant": best, "x_exact": [ox["accepted"], ox["simulated_time"]],
+                "t1_median": acc.get("energy_rel_err_median"),
+                "t1_le_1e-6": acc.get("fraction_energy_err_le_1e-6")}
     return {k: v for k, v in t.items() if v is not None}
 
 
@@ -1182,7 +1184,7 @@ def compact_line(line, legs_path):
                                  "ms_per_step", "higher_is_better", "scaling", "vs_baseline",
                                  "dtype", "data") if k in line}
     cfg = dict(line["config"])
-    cfg["l2"] = "inputs larger than L2, no flush"
+    cfg["l2"] = "inputs > L2, no flush"
     out["config"] = cfg
     out["roofline"] = {"bound": roof["bound"], "achieved": roof["achieved"],
                        "peak": roof["peak"], "unit": roof["unit"], "frac": roof["frac"],
@@ -1198,7 +1200,10 @@ def compact_line(line, legs_path):
                                                  "d2h_bytes_per_step")}
     if "parity" in out:
         out["parity"] = {k: out["parity"][k] for k in ("bitwise", "particles", "mismatched")}
-    out["legs"] = legs_path
+    try:                                        # the side file, relative to the repository
+        out["legs"] = str(Path(legs_path).resolve().relative_to(ROOT))
+    except ValueError:
+        out["legs"] = legs_path
     out = _r(out)
     out["targets"] = _r(targets(line), 3)
     return out
@@ -1231,7 +1236,7 @@ def main():
     if big:                                   # host copies only for the CPU baseline
         out = tuple(a.cpu().numpy() for a in out) if not args.no_cpu else None
         torch.cuda.empty_cache()
-    rec_bytes = {"fp32": (16 if cfg["eta"] != 0.0 else 8) * 4,
+    rec_bytes = {"fp32": (9 if cfg["eta"] != 0.0 else 8) * 4,
                  "bf16": (16 if cfg["eta"] != 0.0 else 8) * 2}.get(
         args.precision, (10 if cfg["eta"] != 0.0 else 6) * 8)
     stream = torch.cuda.Stream(device=dev)
@@ -1327,11 +1332,14 @@ def main():
     pk2 = C.c_double()
     L.pt_probe_peak(2, 16384, C.byref(pk2))
     peak_split = pk2.value
-    traffic = DRAM_BYTES_PER_WINDOW.get((args.workload, args.precision))
+    bpa = DRAM_BYTES_PER_ATTEMPT.get((args.workload, args.precision))
+    traffic = bpa * float(dcnt_tot[0]) / args.steps if bpa else None
     roof = {"bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12,
             "unit": "TFLOP/s", "frac": achieved / peak,
             "traffic": traffic, "traffic_unit": "DRAM bytes per launch (one window)",
-            "traffic_source": "profiles/k_integrate_full_size_single_pass.md" if traffic else None,
+            "traffic_rule": ("DRAM bytes per attempt of a one-pass ncu capture of a 2^17-particle "
+                             "window of the same kernel and workload x this run's attempts per "
+                             "window (upper estimate)") if bpa else None,
             "peak_source": "FP64 FMA peak measured live on this GPU (pt_probe_peak); "
                            "the measured-peaks file lists only HBM and bf16",
             "peak_no_fma": peak_split / 1e12,

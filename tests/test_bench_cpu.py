@@ -60,7 +60,7 @@ def _full_line():
         "e2e": {"value": 4.68e7, "unit": "particle-steps/s", "h2d_bytes_per_step": 226000000,
                 "d2h_bytes_per_step": 164000000, "steps": 4, "api": "w" * 200},
         "cpu_baseline": {"value": 6.89e6, "unit": "particle-steps/s", "cores": 16, "kind": "port",
-                         "sample": "s" * 130},
+                         "sample": "s" * 90},
         "parity": {"bitwise": True, "particles": 603720, "mismatched": 0, "compared": "c" * 200},
         "clocks": {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": [], "samples": 100},
         "gpu_launches": 20, "rejected_fraction": 0.58712345, "stopped_particles": {},
@@ -83,9 +83,10 @@ def _full_line():
 def test_compact_line_is_small_and_complete():
     sys.path.insert(0, str(ROOT))
     import bench
-    out = bench.compact_line(_full_line(), "gpurun_out/bench_legs.json")
+    out = bench.compact_line(_full_line(), str(ROOT / "gpurun_out" / "bench_legs.json"))
     text = json.dumps(out)
-    assert len(text) <= 2048, len(text)
+    assert len(text) <= 1900, len(text)
+    assert out["legs"] == "gpurun_out/bench_legs.json"
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
                 "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
                 "roofline", "cpu_baseline", "e2e", "clocks", "gpu_launches", "parity", "targets"):
