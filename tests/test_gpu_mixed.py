@@ -94,24 +94,38 @@ def test_mixed_fixed_steps_turbulent_field(cuda, oracle_lib):
 def test_mixed_turbulent_statistics(cuda, oracle_lib, method):
     """Adaptive steps in a turbulent trilinear field: FP32 rounding picks
     another valid step sequence (about half of all attempts sit near the
-    accept/reject threshold at cell faces), so trajectories separate like any
-    two roundings do.  Ensemble energy and step statistics must still agree.
-    DOP853 runs at rtol = 1e-7: FP32 noise in the stages floors its error
-    estimate, so tighter tolerances only shrink the steps."""
+    accept/reject threshold at cell faces), so trajectories separate from the
+    oracle's like any two roundings do.  The yardstick is the FP64 FMA build,
+    which differs from the oracle by rounding alone: the FP32 kernel may
+    depart from the oracle no further than it (within a factor 3 on the
+    median and the maximum relative energy error after two gyro-periods;
+    measured 0.7x-1.5x), BF16 no further than 30x on the median (measured
+    1.7x for RK5, 11x for DOP853) and 5x on the maximum.  Ensemble energy
+    and step counts must agree.  DOP853 runs at rtol = 1e-7: FP32 noise in
+    the stages floors its error estimate, so tighter tolerances only shrink
+    the steps."""
     prob = small_problem(method, n=24, npart=128, periods=2.0, seed=13,
                          tol=1e-8 if method == "rk5" else 1e-7)
     import oracle
     from particles_gb300 import integrate
     uu, bb = prob["fields"]
     so, co, _ = oracle.integrate(method, prob["params"], prob["time"], uu, bb, prob["state"].copy())
-    sg, cg, stg = integrate(method, prob["params"], prob["time"], uu, bb, prob["state"].copy(),
-                            precision="fp32")
-    assert (stg == 0).all()
-    g_o, g_g = so[:, -1, 6], sg[:, -1, 6]
-    rel = np.abs(g_g - g_o) / g_o
-    assert np.median(rel) < 1e-4 and rel.max() < 2e-3
-    assert abs(g_g.mean() / g_o.mean() - 1.0) < 2e-5
-    assert 0.9 < cg[:, 1].sum() / co[:, 1].sum() < 1.3
+    g_o = so[:, -1, 6]
+    rel, acc = {}, {}
+    for prec in ("fp64_fma", "fp32", "bf16"):
+        sg, cg, stg = integrate(method, prob["params"], prob["time"], uu, bb,
+                                prob["state"].copy(), precision=prec)
+        assert (stg == 0).all()
+        rel[prec] = np.abs(sg[:, -1, 6] - g_o) / g_o
+        acc[prec] = cg[:, 1].sum() / co[:, 1].sum()
+        assert abs(sg[:, -1, 6].mean() / g_o.mean() - 1.0) < 2e-5
+    med = {k: float(np.median(v)) for k, v in rel.items()}
+    mx = {k: float(v.max()) for k, v in rel.items()}
+    print(f"{method}: median {med}, max {mx}, accepted ratio {acc}")
+    assert med["fp32"] <= 3.0 * med["fp64_fma"] and mx["fp32"] <= 3.0 * mx["fp64_fma"]
+    assert med["bf16"] <= 30.0 * med["fp64_fma"] and mx["bf16"] <= 5.0 * mx["fp64_fma"]
+    assert 0.9 < acc["fp64_fma"] < 1.1
+    assert 0.9 < acc["fp32"] < 1.4 and 0.9 < acc["bf16"] < 1.4
 
 
 def test_mixed_windowed_resume_matches_single_run(cuda):
