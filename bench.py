@@ -112,11 +112,14 @@ def train_controller(torch, records, method, face_feature=True):
 # Variants of the mixed-precision leg: (name, field precision).  "_learned":
 # the learned controller proposes trial steps (trained on records of the
 # exact classical run; with "_face", on records of the FP32 face-capped run);
-# "_face": trial steps end just past the next cell face (PT_CTL_FACE).
+# "_face": trial steps end just past the next cell face (PT_CTL_FACE);
+# "_noise": the error norm with the FP32 evaluation's rounding floor
+# (PT_CTL_NOISE).
 MIXED_VARIANTS = (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"), ("bf16", "bf16"),
                   ("fp32_learned", "fp32"), ("bf16_learned", "bf16"), ("fp64_fma_face", "fp64_fma"),
                   ("fp32_face", "fp32"), ("bf16_face", "bf16"), ("fp32_learned_face", "fp32"),
-                  ("bf16_learned_face", "bf16"))
+                  ("bf16_learned_face", "bf16"), ("fp32_noise", "fp32"), ("bf16_noise", "bf16"),
+                  ("fp32_learned_noise", "fp32"), ("bf16_learned_noise", "bf16"))
 
 # DRAM bytes per attempt (dram__bytes_read.sum + dram__bytes_write.sum of one
 # launch / the attempts it made), from a one-pass ncu capture of a small case
@@ -142,6 +145,8 @@ def parse():
                          "is trained on them and the later windows use it")
     ap.add_argument("--face", action="store_true",
                     help="face-capped trial steps (PT_CTL_FACE; not with --precision fp64)")
+    ap.add_argument("--noise", action="store_true",
+                    help="error norm with the FP32 evaluation's rounding floor (PT_CTL_NOISE)")
     ap.add_argument("--particles", type=int, default=0,
                     help="override the particle count (profiling of small cases only)")
     ap.add_argument("--window", type=float, default=0.0,
@@ -645,10 +650,11 @@ def mixed_leg(args, dev, stream, peak):
     for name, prec in MIXED_VARIANTS:
         f = handles[prec]
         face = name.endswith("_face")
+        noise = "_noise" in name
         mdl = (model_face if face else model) if "_learned" in name else None
         st, cnt, status, carry = fresh(npart)
         launch = tune(args, f, "rk5", prm, d_time, st, stream, window * T0, model=mdl,
-                      face_steps=face)
+                      face_steps=face, noise_floor=noise)
         ordq = QueueOrder(torch, cnt, enabled=not args.no_order,
                           cells=(cfg["n"],) * 3 if args.order == "brick" else None, d_carry=carry)
         w = 0
@@ -657,7 +663,7 @@ def mixed_leg(args, dev, stream, peak):
             o = ordq.before()
             f.run_device("rk5", prm, d_time, st, cnt, status, carry, t_stop=w * window * T0,
                          time_budget_s=900.0, stream=stream.cuda_stream, order=o, model=mdl,
-                         face_steps=face)
+                         face_steps=face, noise_floor=noise)
             ordq.after()
         stream.synchronize()
         c0 = cnt.sum(0).cpu().numpy()
@@ -668,7 +674,7 @@ def mixed_leg(args, dev, stream, peak):
             o = ordq.before()
             f.run_device("rk5", prm, d_time, st, cnt, status, carry, t_stop=w * window * T0,
                          time_budget_s=900.0, stream=stream.cuda_stream, order=o, model=mdl,
-                         face_steps=face)
+                         face_steps=face, noise_floor=noise)
             ordq.after()
         e1.record(stream)
         stream.synchronize()
@@ -737,6 +743,7 @@ def mixed_leg(args, dev, stream, peak):
     w_ref = cfg["periods"]
     for name, prec in (MIXED_VARIANTS if na > 0 else ()):
         face = name.endswith("_face")
+        noise = "_noise" in name
         mdl = (model_face if face else model) if "_learned" in name else None
         st, cnt, status, carry = fresh(na)
         t_start = time.perf_counter()
@@ -745,7 +752,8 @@ def mixed_leg(args, dev, stream, peak):
             w += 1
             handles[prec].run_device("rk5", prm, d_time, st, cnt, status, carry,
                                      t_stop=tg[min(w, m - 1)] * (1 + 1e-12), time_budget_s=900.0,
-                                     stream=stream.cuda_stream, model=mdl, face_steps=face)
+                                     stream=stream.cuda_stream, model=mdl, face_steps=face,
+                                     noise_floor=noise)
             stream.synchronize()
             if w >= w_ref or (name == "fp64" and
                               time.perf_counter() - t_start > args.accuracy_seconds):
@@ -1042,12 +1050,14 @@ def learned_leg(args, dev, stream):
     variants = (("classical", "fp64", None, False), ("learned", "fp64", model, False),
                 ("learned_8_inputs", "fp64", model8, False), ("fp32", "fp32", None, False),
                 ("fp32_learned", "fp32", model, False), ("fp32_face", "fp32", None, True),
-                ("fp32_learned_face", "fp32", model, True))
+                ("fp32_learned_face", "fp32", model, True), ("fp32_noise", "fp32", None, False),
+                ("fp32_learned_noise", "fp32", model, False))
     for name, prec, mdl, face in variants:
         f = fs[prec]
+        noise = "_noise" in name
         st.copy_(snap[0]); cnt.copy_(snap[1]); carry.copy_(snap[2])
         launch = tune(args, f, "dop853", prm, d_time, st, stream, window * T0, eta=cfg["eta"],
-                      model=mdl, face_steps=face)
+                      model=mdl, face_steps=face, noise_floor=noise)
         ordq = QueueOrder(torch, cnt, enabled=not args.no_order,
                           cells=(cfg["n"],) * 3 if args.order == "brick" else None, d_carry=carry)
         w = 0
@@ -1056,7 +1066,8 @@ def learned_leg(args, dev, stream):
             o = ordq.before()
             f.run_device("dop853", prm, d_time, st, cnt, status, carry, eta=cfg["eta"],
                          t_stop=w * window * T0, time_budget_s=900.0,
-                         stream=stream.cuda_stream, order=o, model=mdl, face_steps=face)
+                         stream=stream.cuda_stream, order=o, model=mdl, face_steps=face,
+                         noise_floor=noise)
             ordq.after()
         stream.synchronize()
         c0 = cnt.sum(0).cpu().numpy()
@@ -1067,7 +1078,8 @@ def learned_leg(args, dev, stream):
             o = ordq.before()
             f.run_device("dop853", prm, d_time, st, cnt, status, carry, eta=cfg["eta"],
                          t_stop=w * window * T0, time_budget_s=900.0,
-                         stream=stream.cuda_stream, order=o, model=mdl, face_steps=face)
+                         stream=stream.cuda_stream, order=o, model=mdl, face_steps=face,
+                         noise_floor=noise)
             ordq.after()
         e1.record(stream)
         stream.synchronize()
@@ -1091,7 +1103,8 @@ def learned_leg(args, dev, stream):
         k1 = torch.zeros(int(fs[prec]._L.pt_carry_bytes(na)), dtype=torch.uint8, device=dev)
         fs[prec].run_device("dop853", prm, d_time, s1, c1, q1, k1, eta=cfg["eta"],
                             t_stop=tg[1] * (1 + 1e-12), time_budget_s=900.0,
-                            stream=stream.cuda_stream, model=mdl, face_steps=face)
+                            stream=stream.cuda_stream, model=mdl, face_steps=face,
+                            noise_floor="_noise" in name)
         stream.synchronize()
         res[name] = s1.cpu().numpy()
     for name, *_ in variants[1:]:
@@ -1143,9 +1156,8 @@ def targets(line):
         ov, ph = mx["over_plain_exact"], mx["physics_rate_over_plain_exact"]
         fma = mx["accepted_steps_per_s"]["fp64_fma"]
         fma_ph = mx["detail"]["fp64_fma"]["particle_gyroperiods_per_s"]
-        pick = {k: mx["accepted_steps_per_s"][k] for k in ("bf16_learned", "bf16_learned_face",
-                                                          "fp32_learned", "fp32_learned_face")
-                if k in mx["accepted_steps_per_s"]}
+        pick = {k: mx["accepted_steps_per_s"][k] for k in mx["accepted_steps_per_s"]
+                if "_learned" in k}
         best = max(pick, key=pick.get)
         t["mixed_learned_rk5"] = {
             "variant": best, "x_exact": [ov[best], ph[best]],
@@ -1164,7 +1176,8 @@ def targets(line):
         t["learned_vs_classical_dop853"] = {
             "sim_time": lr["physics_rate_ratio"], "attempts": lr["attempts_ratio"],
             "sim_time_8_inputs": lr.get("physics_rate_ratio_8_inputs")}
-        ml = {k: lr[k] for k in ("fp32_learned", "fp32_learned_face") if k in lr}
+        ml = {k: lr[k] for k in ("fp32_learned", "fp32_learned_face", "fp32_learned_noise")
+              if k in lr}
         if ml:
             best = max(ml, key=lambda k: ml[k]["over_plain_exact"]["simulated_time"])
             acc = ml[best].get("accuracy_1_gyroperiod", {})
@@ -1265,7 +1278,7 @@ def main():
         f.run_device(cfg["method"], prm, d_time, d_state, d_cnt, d_status, d_carry,
                      eta=cfg["eta"], t_stop=w * window * T0, time_budget_s=900.0,
                      stream=stream.cuda_stream, order=order, model=model, records=records,
-                     face_steps=args.face)
+                     face_steps=args.face, noise_floor=args.noise)
         ordq.after()
 
     w = 0
@@ -1279,7 +1292,7 @@ def main():
         training["recorded_in"] = "the first warm-up window (classical controller)"
         del rec
     launch = tune(args, f, cfg["method"], prm, d_time, d_state, stream, window * T0,
-                  eta=cfg["eta"], model=model, face_steps=args.face)
+                  eta=cfg["eta"], model=model, face_steps=args.face, noise_floor=args.noise)
     for _ in range(args.warmup - w):
         w += 1
         window_run(w)
@@ -1368,7 +1381,8 @@ def main():
         "attempts_per_s": float(dcnt_tot[0]) / elapsed,
         "particle_gyroperiods_per_s": world * npart * window * args.steps / elapsed,
         "roofline": roof, "clocks": clocks.summary(), "launch": launch,
-        "controller": args.controller + (", face-capped steps" if args.face else ""),
+        "controller": args.controller + (", face-capped steps" if args.face else "")
+                      + (", noise-floor norm" if args.noise else ""),
     }
     if training:
         line["learned_training"] = training
@@ -1392,7 +1406,7 @@ def main():
             w += 1
             o = _options(args.precision, eta=cfg["eta"], t_stop=w * window * T0,
                          status=None, carry=None, time_budget_s=900.0, model=model,
-                         face_steps=args.face)
+                         face_steps=args.face, noise_floor=args.noise)
             o.status = C.c_void_p(h_status.data_ptr())
             o.carry = C.c_void_p(h_carry.data_ptr())
             rc = L.pt_integrate_fields(method_id(cfg["method"]), npart, m, f.handle, prm.ctypes.data_as(C.c_void_p),

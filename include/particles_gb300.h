@@ -53,6 +53,9 @@ extern "C" {
 #define PT_CTL_CLASSICAL   0  /* pt_options.controller: the reference's controller */
 #define PT_CTL_LEARNED     1  /* bit: the learned MLP proposes the trial step */
 #define PT_CTL_FACE        2  /* bit: trial steps end just past the next cell face */
+#define PT_CTL_NOISE       4  /* bit: the embedded error norm treats differences below the
+                                 rounding floor of the FP32 evaluation as zero (FP32 / BF16
+                                 only; not in the reference) */
 
 /* Return codes. */
 #define PT_OK               0
@@ -85,7 +88,9 @@ typedef struct pt_options {
     int32_t       controller;     /* PT_CTL_* bits: 0 classical; PT_CTL_LEARNED learned
                                      trial step (needs a model); PT_CTL_FACE trial step
                                      capped just past the next cell face (not with
-                                     PT_PREC_FP64, which keeps the reference's controller) */
+                                     PT_PREC_FP64, which keeps the reference's controller);
+                                     PT_CTL_NOISE error norm with the FP32 evaluation's
+                                     rounding floor (PT_PREC_FP32 / PT_PREC_BF16 only) */
     int64_t       max_steps;      /* attempt cap per particle; 0 = 1e9 */
     double        eta;            /* resistivity: E = -U x B + eta J; 0 = ideal */
     const double *jj;             /* J = curl B in the layout of bb; required iff eta != 0 */

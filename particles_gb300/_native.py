@@ -37,7 +37,7 @@ EXPORTS = [
 ]
 
 PT_INIT_SPEED, PT_INIT_GAMMA, PT_INIT_MAXWELLIAN = 0, 1, 2
-PT_CTL_CLASSICAL, PT_CTL_LEARNED, PT_CTL_FACE = 0, 1, 2
+PT_CTL_CLASSICAL, PT_CTL_LEARNED, PT_CTL_FACE, PT_CTL_NOISE = 0, 1, 2, 4
 
 
 class PtOptions(C.Structure):

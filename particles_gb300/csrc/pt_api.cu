@@ -17,6 +17,7 @@
 
 #include "pt_common.cuh"
 #include "pt_detmath.h"
+#include "pt_tableau.h"
 #include "pt_internal.h"
 #include "pt_tableau.h"
 
@@ -102,6 +103,41 @@ void unpack_params(const double *p, const RunShape &g, PtRun &R)
     R.qomf = (float)R.qom;
 }
 
+/* PT_CTL_NOISE: the embedded error estimate is a combination sum_j e_j k_j of
+ * the stage derivatives, and an FP32 evaluation (trilinear sums and force
+ * in FP32) carries a rounding error of a few units in the last place of the
+ * largest component of its group (positions, momenta).  The stages round
+ * independently, so with PT_NOISE_ULP such units per stage the estimate's
+ * noise is nu = PT_NOISE_ULP 2^-24 sqrt(sum_j e_j^2) |f|_max.  The norm adds
+ * twice that to each component's scale sr, so that an estimate made of
+ * noise alone scores at most about 1/2 and the controller responds to
+ * truncation errors only:
+ *   RK5 (del = max |er / sr| / atol, k = dt f):  sr += 2 nu / atol with
+ *       |f|_max read as |k1|_max, coefficient 2 PT_NOISE_ULP 2^-24 |d|_2 / atol;
+ *   DOP853 (err = |dt| ||e / sr|| with e in units of f):  sr += 2 |dt| nu,
+ *       coefficient 2 PT_NOISE_ULP 2^-24 |er|_2.
+ * Without it the reference's per-component scales (RK5: |si| + |k1|) become
+ * tiny where a momentum component crosses zero during a gyration, an
+ * estimate made of FP32 rounding exceeds them at every step size, and the
+ * controller shrinks dt without end (measured: 17,535 attempts in a
+ * 0.1-gyro-period window for a particle the FP64 kernel takes in 365). */
+#define PT_NOISE_ULP 8.0
+static double noise_floor(int method, double atol)
+{
+    using namespace pt_tab;
+    const double u = PT_NOISE_ULP * 5.9604644775390625e-08;     /* 2^-24 */
+    if (method == PT_METHOD_DOP853) {
+        const double e[8] = { ER01, ER06, ER07, ER08, ER09, ER10, ER11, ER12 };
+        double s = 0.0;
+        for (double x : e) s += x * x;
+        return 2.0 * u * sqrt(s);
+    }
+    const double d[5] = { CK_D1, CK_D3, CK_D4, CK_D5, CK_D6 };
+    double s = 0.0;
+    for (double x : d) s += x * x;
+    return 2.0 * u * sqrt(s) / atol;
+}
+
 /* Face-cap constants (PT_CTL_FACE) per method [RK5, DOP853]: faces reached
  * within skip x the proposed step are crossed; steps end `over` cells of the
  * fastest axis past the capping face.  pt_debug_face_params sets them.
@@ -149,8 +185,12 @@ int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
     if (opt) {
         if (opt->precision != g.precision)
             return set_err(PT_ERR_ARG, "options precision differs from the field handle%s");
-        if (opt->controller < 0 || opt->controller > (PT_CTL_LEARNED | PT_CTL_FACE))
+        if (opt->controller < 0 || opt->controller > (PT_CTL_LEARNED | PT_CTL_FACE | PT_CTL_NOISE))
             return set_err(PT_ERR_ARG, "unknown controller%s");
+        if ((opt->controller & PT_CTL_NOISE) && g.precision != PT_PREC_FP32 &&
+            g.precision != PT_PREC_BF16)
+            return set_err(PT_ERR_UNSUPPORTED, "the error norm's rounding floor is for the FP32 "
+                                               "evaluation (PT_PREC_FP32 / PT_PREC_BF16)%s");
         if ((opt->controller & PT_CTL_LEARNED) && !opt->model)
             return set_err(PT_ERR_ARG, "the learned controller needs opt->model%s");
         if ((opt->controller & PT_CTL_FACE) && g.precision == PT_PREC_FP64)
@@ -200,6 +240,7 @@ int prepare_run(int32_t method, int64_t np, int32_t m, const RunShape &g,
         R.face = (opt->controller & PT_CTL_FACE) ? 1 : 0;
         R.face_skip = g_face_skip[method == PT_METHOD_DOP853];
         R.face_over = g_face_over[method == PT_METHOD_DOP853];
+        R.noise = (opt->controller & PT_CTL_NOISE) ? noise_floor(method, R.atol) : 0.0;
         R.rec = static_cast<float *>(opt->records);
         R.rec_cap = opt->record_capacity;
         R.order = opt->order;

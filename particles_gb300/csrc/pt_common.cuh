@@ -37,6 +37,9 @@ struct PtRun {
     int32_t face;          /* 1: trial steps capped just past the next cell face */
     float face_skip;       /* faces within face_skip x the proposed step are crossed */
     float face_over;       /* overshoot past the capping face, in cells of the fastest axis */
+    double noise;          /* PT_CTL_NOISE: rounding floor of the FP32 evaluation in the error
+                              norm, per unit of the largest |f(si)| component of a group
+                              (positions, momenta); 0 = the reference's norm */
     /* extensions */
     double eta;
     int32_t has_j;

@@ -354,6 +354,15 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
             sf[c] = si[c] + dsf[c];
             sr[c] = P.atol + P.rtol * pt_max(fabs(si[c]), fabs(sf[c]));
         }
+#ifndef PT_EXACT
+        if (P.noise != 0.0) {            /* PT_CTL_NOISE: sr += 2 |dt| nu per group */
+            const double fp = pt_max(fabs(K(0, 0)), pt_max(fabs(K(0, 1)), fabs(K(0, 2))));
+            const double fm = pt_max(fabs(K(0, 3)), pt_max(fabs(K(0, 4)), fabs(K(0, 5))));
+            const double np_ = P.noise * fabs(dt) * fp, nm_ = P.noise * fabs(dt) * fm;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) sr[c] += (c < 3) ? np_ : nm_;
+        }
+#endif
         double err3 = 0.0, err5 = 0.0;                          /* :426-437 */
 #ifndef PT_EXACT
 #pragma unroll
@@ -389,6 +398,13 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
 #endif
     } else {                                                    /* :140-148 */
         double del = 0.0;
+#ifndef PT_EXACT
+        double nfl[2] = { 0.0, 0.0 };    /* PT_CTL_NOISE: (2 nu / atol) per group */
+        if (P.noise != 0.0) {
+            nfl[0] = P.noise * pt_max(fabs(K(0, 0)), pt_max(fabs(K(0, 1)), fabs(K(0, 2))));
+            nfl[1] = P.noise * pt_max(fabs(K(0, 3)), pt_max(fabs(K(0, 4)), fabs(K(0, 5))));
+        }
+#endif
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
 #ifdef PT_EXACT
@@ -413,6 +429,7 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
 #else
             /* + DBL_MIN only changes a zero sum: test the bits instead (integer pipe) */
             double sr = fabs(si[c]) + fabs(K(0, c));
+            if (P.noise != 0.0) sr += nfl[c / 3];
             if (__double_as_longlong(sr) == 0) sr = 2.2250738585072014e-308;
 #endif
             const double q = fabs(PT_DIV(e, sr));

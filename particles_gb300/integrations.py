@@ -48,7 +48,7 @@ def _f64(a):
 
 def _options(precision, *, eta=0.0, jj=None, open_x=False, max_steps=0, t_stop=0.0,
              status=None, carry=None, time_budget_s=0.0, model=None, records=None,
-             order=None, blocks_per_sm=0, interpolation=0, face_steps=False,
+             order=None, blocks_per_sm=0, interpolation=0, face_steps=False, noise_floor=False,
              threads_per_block=0, open_x_margin=0.0):
     o = N.PtOptions()
     o.struct_size = C.sizeof(N.PtOptions)
@@ -56,7 +56,8 @@ def _options(precision, *, eta=0.0, jj=None, open_x=False, max_steps=0, t_stop=0
     o.open_x = int(bool(open_x))
     o.open_x_margin = float(open_x_margin)
     o.controller = ((N.PT_CTL_LEARNED if model is not None else 0)
-                    | (N.PT_CTL_FACE if face_steps else 0))
+                    | (N.PT_CTL_FACE if face_steps else 0)
+                    | (N.PT_CTL_NOISE if noise_floor else 0))
     o.model = model.handle if model is not None else None
     if records is not None:                       # device tensor (float32) with header
         o.records = C.c_void_p(records.data_ptr())
@@ -84,7 +85,7 @@ def carry_buffer(npart: int) -> np.ndarray:
 def integrate(method, params, time, uu, bb, state, cnt=None, *, precision="fp64", eta=0.0,
               jj=None, open_x=False, open_x_margin=0.0, max_steps=0, t_stop=0.0, carry=None,
               status=None, time_budget_s=0.0, check=True, interpolation="linear",
-              face_steps=False):
+              face_steps=False, noise_floor=False):
     """Integrate every particle of ``state`` in place on the GPU.
 
     Returns (state, cnt, status).  With ``check`` a negative return code
@@ -105,7 +106,7 @@ def integrate(method, params, time, uu, bb, state, cnt=None, *, precision="fp64"
     opt = _options(precision, eta=eta, jj=jj, open_x=open_x, open_x_margin=open_x_margin,
                    max_steps=max_steps, t_stop=t_stop, status=status, carry=carry,
                    time_budget_s=time_budget_s, interpolation=interpolation,
-                   face_steps=face_steps)
+                   face_steps=face_steps, noise_floor=noise_floor)
     rc = L.pt_integrate(mid, npart, m, _ptr(dm), _ptr(_f64(params)), _ptr(_f64(time)),
                         _ptr(uu), _ptr(bb), _ptr(state), _ptr(cnt), C.byref(opt))
     if check:
@@ -173,7 +174,8 @@ class Fields:
 
     def integrate(self, method, params, time, state, cnt=None, *, eta=0.0, open_x=False,
                   open_x_margin=0.0, max_steps=0, t_stop=0.0, carry=None, status=None,
-                  time_budget_s=0.0, check=True, interpolation="linear", face_steps=False):
+                  time_budget_s=0.0, check=True, interpolation="linear", face_steps=False,
+                  noise_floor=False):
         """Host-buffer run on these fields (pt_integrate_fields)."""
         npart, m, _ = state.shape
         if cnt is None:
@@ -183,7 +185,7 @@ class Fields:
         opt = _options(self.precision, eta=eta, open_x=open_x, open_x_margin=open_x_margin,
                        max_steps=max_steps, t_stop=t_stop, status=status, carry=carry,
                        time_budget_s=time_budget_s, interpolation=interpolation,
-                       face_steps=face_steps)
+                       face_steps=face_steps, noise_floor=noise_floor)
         rc = self._L.pt_integrate_fields(method_id(method), npart, m, self._h,
                                          _ptr(_f64(params)), _ptr(_f64(time)), _ptr(state),
                                          _ptr(cnt), C.byref(opt))
@@ -195,7 +197,8 @@ class Fields:
                    *, eta=0.0, open_x=False, open_x_margin=0.0, max_steps=0, t_stop=0.0,
                    time_budget_s=0.0, stream=0, model=None, records=None, order=None,
                    blocks_per_sm=0,
-                   interpolation="linear", face_steps=False, threads_per_block=0):
+                   interpolation="linear", face_steps=False, noise_floor=False,
+                   threads_per_block=0):
         """Launch on device tensors (torch); returns without synchronising.
 
         model: a learned.Model for the learned controller; records: a device
@@ -204,13 +207,16 @@ class Fields:
         128-thread blocks); threads_per_block: 0 (tuned or 128), 64, 128 or 256;
         face_steps: trial steps end just past the next cell face (PT_CTL_FACE,
         not with precision "fp64").
+        noise_floor: the error norm treats differences below the FP32
+        evaluation's rounding floor as zero (PT_CTL_NOISE, "fp32" / "bf16").
         """
         npart, m, _ = d_state.shape
         opt = _options(self.precision, eta=eta, open_x=open_x, open_x_margin=open_x_margin,
                        max_steps=max_steps, t_stop=t_stop, time_budget_s=time_budget_s,
                        model=model, records=records, order=order, blocks_per_sm=blocks_per_sm,
                        threads_per_block=threads_per_block,
-                       interpolation=interpolation, face_steps=face_steps)
+                       interpolation=interpolation, face_steps=face_steps,
+                       noise_floor=noise_floor)
         rc = self._L.pt_run_device(
             method_id(method), npart, m, self._h, _ptr(_f64(params)),
             C.c_void_p(d_time.data_ptr()), C.c_void_p(d_state.data_ptr()),
@@ -222,7 +228,7 @@ class Fields:
 
     def autotune(self, method, params, d_time, d_state, *, eta=0.0, open_x=False, max_steps=0,
                  t_stop=0.0, sample=0, stream=0, model=None, records=None,
-                 interpolation="linear", face_steps=False):
+                 interpolation="linear", face_steps=False, noise_floor=False):
         """Time the launch variants of the kernel run_device would use with
         these arguments (pt_autotune) and make the fastest its default.
 
@@ -233,7 +239,7 @@ class Fields:
         npart, m, _ = d_state.shape
         opt = _options(self.precision, eta=eta, open_x=open_x, max_steps=max_steps,
                        t_stop=t_stop, model=model, records=records, interpolation=interpolation,
-                       face_steps=face_steps)
+                       face_steps=face_steps, noise_floor=noise_floor)
         chosen = (C.c_int32 * 2)()
         ms = np.zeros(9, np.float64)
         rc = self._L.pt_autotune(method_id(method), npart, m, self._h, _ptr(_f64(params)),
@@ -261,7 +267,8 @@ class Ensemble:
     """
 
     def __init__(self, method, members, *, precision="fp64", blocks_per_sm=0,
-                 time_budget_s=0.0, interpolation="linear", face_steps=False):
+                 time_budget_s=0.0, interpolation="linear", face_steps=False,
+                 noise_floor=False):
         self._L = N.load()
         self._h = C.c_void_p()
         self.n = len(members)
@@ -283,7 +290,8 @@ class Ensemble:
             for key in ("time", "state", "cnt", "status", "carry"):
                 setattr(a, key, C.c_void_p(mb[key].data_ptr()))
         opt = _options(precision, time_budget_s=time_budget_s, blocks_per_sm=blocks_per_sm,
-                       interpolation=interpolation, face_steps=face_steps)
+                       interpolation=interpolation, face_steps=face_steps,
+                       noise_floor=noise_floor)
         N.check(self._L.pt_ensemble_create(method_id(method), self.n, C.byref(arr), C.byref(opt),
                                            C.byref(self._h)), "pt_ensemble_create")
 

@@ -180,3 +180,40 @@ def test_fp32_store_size(cuda, with_j):
                None if jj is None else jj[:, :12, :12, :12].copy(), precision="fp32")
     assert g.nbytes == 8 * 512 * (36 if with_j else 32) + 256
     g.close()
+
+
+@pytest.mark.parametrize("method,tol", [("rk5", 1e-8), ("dop853", 1e-7), ("dop853", 1e-10)])
+def test_noise_floor_norm(cuda, oracle_lib, method, tol):
+    """PT_CTL_NOISE: the error norm treats differences below the FP32
+    evaluation's rounding floor as zero.  With the reference's norm the
+    FP32 kernel can take many times the oracle's steps -- where a momentum
+    component crosses zero (RK5's per-component scale |si| + |k1|), or at a
+    tolerance below the FP32 force's precision (DOP853 at 1e-10, ~30x the
+    accepted steps) -- while with the floor its step counts stay near the
+    oracle's (within 1.5x; at rtol 1e-10, where the floor sets the accuracy,
+    down to 0.3x) and its departure from the oracle stays that of the
+    reference-norm FP32 run (median relative energy error within 3x; at rtol
+    1e-10 below 1e-6)."""
+    prob = small_problem(method, n=24, npart=128, periods=2.0, seed=13, tol=tol)
+    import oracle
+    from particles_gb300 import integrate
+    uu, bb = prob["fields"]
+    so, co, _ = oracle.integrate(method, prob["params"], prob["time"], uu, bb, prob["state"].copy())
+    g_o = so[:, -1, 6]
+    res = {}
+    for noise in (False, True):
+        sg, cg, stg = integrate(method, prob["params"], prob["time"], uu, bb,
+                                prob["state"].copy(), precision="fp32", noise_floor=noise)
+        assert (stg == 0).all()
+        rel = np.abs(sg[:, -1, 6] - g_o) / g_o
+        res[noise] = (float(np.median(rel)), float(rel.max()), cg[:, 1].sum() / co[:, 1].sum(),
+                      float((cg[:, 0] / co[:, 0]).max()))
+    print(f"{method} {tol}: (median, max, accepted ratio, max attempts ratio) "
+          f"reference norm {res[False]}, floor {res[True]}")
+    med, mx, acc, att = res[True]
+    assert (0.7 if tol >= 1e-8 else 0.3) < acc < 1.5 and att < 3.0
+    assert abs(sg[:, -1, 6].mean() / g_o.mean() - 1.0) < 2e-5
+    if tol >= 1e-8:
+        assert med <= 3.0 * res[False][0] + 1e-9
+    else:
+        assert med < 1e-6 and res[False][2] > 5.0 * acc

@@ -164,7 +164,9 @@ def test_initial_state_argument_errors_need_no_gpu(native):
 
 
 def test_face_controller_checked_on_host(native):
-    """PT_CTL_FACE is a controller bit of the non-exact precisions only."""
+    """PT_CTL_FACE is a controller bit of the non-exact precisions only,
+    PT_CTL_NOISE of the FP32-evaluation precisions only; other bits are
+    unknown."""
     from particles_gb300 import _native as N
     from particles_gb300.params import pack_params
     dm = np.array([8, 8, 8], np.int32)
@@ -174,7 +176,10 @@ def test_face_controller_checked_on_host(native):
     for prec, ctl, rc in ((0, N.PT_CTL_FACE, N.PT_ERR_UNSUPPORTED), (1, N.PT_CTL_FACE, N.PT_OK),
                           (2, N.PT_CTL_FACE, N.PT_OK), (3, N.PT_CTL_FACE, N.PT_OK),
                           (2, N.PT_CTL_FACE | N.PT_CTL_LEARNED, N.PT_ERR_ARG),   # no model
-                          (2, 4, N.PT_ERR_ARG), (2, -1, N.PT_ERR_ARG)):
+                          (0, N.PT_CTL_NOISE, N.PT_ERR_UNSUPPORTED),
+                          (1, N.PT_CTL_NOISE, N.PT_ERR_UNSUPPORTED),
+                          (2, N.PT_CTL_NOISE, N.PT_OK), (3, N.PT_CTL_NOISE | N.PT_CTL_FACE, N.PT_OK),
+                          (2, 8, N.PT_ERR_ARG), (2, -1, N.PT_ERR_ARG)):
         o = N.PtOptions()
         o.struct_size = C.sizeof(o)
         o.precision = prec
