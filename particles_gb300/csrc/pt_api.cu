@@ -95,6 +95,7 @@ void unpack_params(const double *p, const RunShape &g, PtRun &R)
         R.gsx[i] = (double)g.dm[i] / R.xs[i];
         R.gox[i] = -R.xl[i] * R.gsx[i];
         R.gsxf[i] = (float)R.gsx[i];
+        R.inv_xs[i] = 1.0 / R.xs[i];
         unit = unit && (R.xl[i] == 0.0) && !signbit(R.xl[i]) && (R.xs[i] == 1.0);
     }
     R.unit_map = unit ? 1 : 0;
@@ -569,6 +570,14 @@ extern "C" int pt_debug_intpipe(int64_t n, const double *d_x, int32_t d, double 
     if (n < 0 || (n > 0 && (!d_x || !d_out || !d_idx))) return set_err(PT_ERR_ARG, "bad argument%s");
     const cudaError_t e = pt_launch_intpipe(n, d_x, d, d_out, d_idx, (cudaStream_t)stream);
     return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_intpipe");
+}
+
+extern "C" int pt_debug_qdiv(int64_t n, const double *d_a, const double *d_b, double *d_out,
+                             void *stream)
+{
+    if (n < 0 || (n > 0 && (!d_a || !d_b || !d_out))) return set_err(PT_ERR_ARG, "bad argument%s");
+    const cudaError_t e = pt_launch_qdiv(n, d_a, d_b, d_out, (cudaStream_t)stream);
+    return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_qdiv");
 }
 
 extern "C" int pt_debug_ctl_pow(int64_t n, const double *d_x, const double *d_y, double *d_out,

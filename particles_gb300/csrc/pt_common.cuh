@@ -28,6 +28,7 @@ struct PtRun {
     double inv_dm[3], dmr[3];
     double gsx[3], gox[3];  /* node coordinate = x * gsx + gox = (x - xl) / xs * dm */
     double inv_vun;         /* 1 / vun, correctly rounded */
+    double inv_xs[3];       /* 1 / xs, correctly rounded */
     float gsxf[3];          /* gsx rounded to FP32 (mixed precision) */
     float ivunf, qomf, etaf;
     int32_t dm[3];
@@ -176,6 +177,24 @@ __device__ __forceinline__ int32_t pt_node_index(double q, int32_t d)
     return v < d ? v : 0;
 }
 
+/* a / b correctly rounded from y = RN(1/b) (Markstein's quotient correction,
+ * P. Markstein, IBM J. Res. Develop. 34(1), 1990): q0 = RN(a y) is within an
+ * ulp of a / b, so the remainder r = a - b q0 is exact in one FMA and
+ * RN(q0 + r y) is the correctly rounded quotient -- bit-identical to IEEE
+ * a / b while the quotient stays well inside the normal range.  Three FP64
+ * operations instead of a division sequence, and one reciprocal serves
+ * every quotient by the same b.  Zeros, tiny or huge quotients, infinities
+ * and NaN take the IEEE division (never on physical states; the exponent
+ * test runs on the integer pipe). */
+__device__ __forceinline__ double pt_qdiv(double a, double b, double y)
+{
+    const double q0 = a * y;
+    const uint32_t e = (uint32_t)((unsigned long long)__double_as_longlong(q0) >> 52) & 0x7ffu;
+    if (e - 63u > 1920u) return a / b;                      /* |q0| outside [2^-960, 2^961) */
+    const double r = fma(-b, q0, a);
+    return fma(r, y, q0);
+}
+
 __device__ __forceinline__ uint64_t pt_globaltimer()
 {
     uint64_t t;
@@ -253,6 +272,8 @@ cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int brick, int64_t n, 
 
 cudaError_t pt_launch_debug_pow(int64_t n, const double *x, const double *y, double *out,
                                 cudaStream_t s);
+cudaError_t pt_launch_qdiv(int64_t n, const double *a, const double *b, double *out,
+                           cudaStream_t s);
 cudaError_t pt_launch_ctl_pow(int64_t n, const double *x, const double *y, double *out,
                               cudaStream_t s);
 cudaError_t pt_launch_face_cap(const PtRun &P, int64_t n, const double *si, const double *h,

@@ -86,7 +86,7 @@ struct EvalF64 {
 #ifdef PT_EXACT
 #pragma unroll
         for (int i = 0; i < 3; ++i) {                            /* :140-149 */
-            const double x = P.unit_map ? s[i] : (s[i] - P.xl[i]) / P.xs[i];
+            const double x = P.unit_map ? s[i] : pt_qdiv(s[i] - P.xl[i], P.xs[i], P.inv_xs[i]);
             const double xr = x + P.inv_dm[i];
             double xp = P.dmr[i] * (xr - pt_floor(xr));
             r[i] = pt_node_index(pt_floor(xp), P.dm[i]);
@@ -146,11 +146,14 @@ struct EvalF64 {
             }
         }
 #ifdef PT_EXACT
+        /* the quotients by g and vun through one correctly rounded
+         * reciprocal each: bit-identical to the divisions (pt_qdiv) */
         const double g = sqrt(s[3] * s[3] + s[4] * s[4] + s[5] * s[5] + 1.0);
-        const double v0 = s[3] / g, v1 = s[4] / g, v2 = s[5] / g;
-        a[0] = v0 / P.vun;
-        a[1] = v1 / P.vun;
-        a[2] = v2 / P.vun;
+        const double yg = 1.0 / g;
+        const double v0 = pt_qdiv(s[3], g, yg), v1 = pt_qdiv(s[4], g, yg), v2 = pt_qdiv(s[5], g, yg);
+        a[0] = pt_qdiv(v0, P.vun, P.inv_vun);
+        a[1] = pt_qdiv(v1, P.vun, P.inv_vun);
+        a[2] = pt_qdiv(v2, P.vun, P.inv_vun);
 #else
         /* 1/gamma once, then multiplies (within an ulp of the divisions) */
         const double ig = pt_sm::pt_rsqrt(fma(s[3], s[3], fma(s[4], s[4], fma(s[5], s[5], 1.0))));

@@ -369,7 +369,12 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
         for (int c = 0; c < 6; ++c) sr[c] = pt_rcp(sr[c]);     /* now 1/sr */
 #define PT_OVER_SR(e, c) ((e) * sr[c])
 #else
-#define PT_OVER_SR(e, c) ((e) / sr[c])
+        /* e / sr through one correctly rounded reciprocal per component,
+         * shared by the two sums: bit-identical to the divisions (pt_qdiv) */
+        double ysr[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) ysr[c] = 1.0 / sr[c];
+#define PT_OVER_SR(e, c) pt_qdiv((e), sr[c], ysr[c])
 #endif
 #pragma unroll
         for (int c = 0; c < 6; ++c) {

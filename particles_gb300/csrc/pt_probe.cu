@@ -48,6 +48,18 @@ __global__ void k_face_cap(const PtRun P, int64_t n, const double *si, const dou
     }
 }
 
+/* pt_qdiv next to the IEEE division: out[2i] = pt_qdiv(a, b, 1 / b),
+ * out[2i + 1] = a / b. */
+__global__ void k_qdiv(int64_t n, const double *a, const double *b, double *out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double x = a[i], y = b[i];
+        out[2 * i] = pt_qdiv(x, y, 1.0 / y);
+        out[2 * i + 1] = x / y;
+    }
+}
+
 /* The non-exact builds' controller power, for its accuracy test. */
 __global__ void k_ctl_pow(int64_t n, const double *x, const double *y, double *o)
 {
@@ -114,6 +126,15 @@ extern "C" int pt_probe_peak(int32_t kind, int32_t iters, double *flops_per_s)
                    : (kind == 1) ? measure<float>(iters) : measure<double, true>(iters);
     *flops_per_s = r;
     return r > 0 ? PT_OK : PT_ERR_CUDA;
+}
+
+cudaError_t pt_launch_qdiv(int64_t n, const double *a, const double *b, double *out,
+                           cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    k_qdiv<<<grid, 256, 0, s>>>(n, a, b, out);
+    return cudaGetLastError();
 }
 
 cudaError_t pt_launch_ctl_pow(int64_t n, const double *x, const double *y, double *out,

@@ -228,6 +228,54 @@ def test_controller_pow_of_the_fast_builds(cuda, oracle_lib):
     assert np.array_equal(got[6001:], ref)             # outside the Newton range: same bits
 
 
+def test_reciprocal_quotient_bitwise(cuda):
+    """The exact build divides by g = gamma, vun and xs through one correctly
+    rounded reciprocal each (Markstein's quotient correction, pt_qdiv); it
+    must equal the IEEE division bit for bit: random operands over 120
+    binades, the kernel's own shapes (u / gamma with gamma = sqrt(u.u + 1),
+    v / vun), divisors with all-ones and single-bit mantissas, and zeros,
+    signed zeros, infinities, NaN and quotients near the range limits (which
+    take the division itself)."""
+    torch = cuda
+    from particles_gb300 import _native as N
+    g = torch.Generator(device="cuda").manual_seed(7)
+    n = 1 << 24
+
+    def rnd(lo, hi):
+        m = 1.0 + torch.rand(n, generator=g, device="cuda", dtype=torch.float64)
+        e = torch.randint(lo, hi, (n,), generator=g, device="cuda").to(torch.float64)
+        sgn = torch.where(torch.rand(n, generator=g, device="cuda") < 0.5, -1.0, 1.0).to(torch.float64)
+        return sgn * m * torch.pow(2.0, e)
+
+    cases = [(rnd(-60, 60), rnd(-60, 60))]
+    u = rnd(-30, 12)
+    w = rnd(-30, 12)
+    gam = torch.sqrt(u * u + w * w + 1.0)
+    cases.append((u, gam))
+    cases.append((u / gam, torch.full_like(u, 0.05)))
+    ones = torch.tensor([2.0 - 2.0 ** -52, 1.0 + 2.0 ** -52, 1.0, 1.5 - 2.0 ** -52],
+                        dtype=torch.float64, device="cuda")
+    cases.append((rnd(-40, 40), ones[torch.randint(0, 4, (n,), generator=g, device="cuda")]
+                  * torch.pow(2.0, torch.randint(-40, 40, (n,), generator=g,
+                                                 device="cuda").to(torch.float64))))
+    sp = torch.tensor([0.0, -0.0, float("inf"), -float("inf"), float("nan"), 2.0 ** -1000,
+                       -(2.0 ** -1000), 2.0 ** 1000, 5e-324, 1.0, -3.0], dtype=torch.float64,
+                      device="cuda")
+    aa, bb = torch.meshgrid(sp, torch.cat([sp, torch.tensor([0.05, 7.0, 2.0 ** 60],
+                                                            dtype=torch.float64, device="cuda")]),
+                            indexing="ij")
+    cases.append((aa.reshape(-1).contiguous(), bb.reshape(-1).contiguous()))
+    L = N.load()
+    for a, b in cases:
+        a, b = a.contiguous(), b.contiguous()
+        out = torch.empty(2 * a.numel(), dtype=torch.float64, device="cuda")
+        N.check(L.pt_debug_qdiv(a.numel(), C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
+                                C.c_void_p(out.data_ptr()), None), "pt_debug_qdiv")
+        q, d = out[0::2], out[1::2]
+        same = (q.view(torch.int64) == d.view(torch.int64)) | (torch.isnan(q) & torch.isnan(d))
+        assert bool(same.all()), (a[~same][:4].tolist(), b[~same][:4].tolist())
+
+
 def test_host_buffer_calls_move_only_the_rows_they_write(cuda, oracle_lib):
     """pt_integrate_fields copies in the first row (and the carry), copies out
     only the rows each particle wrote: host rows beyond the window keep their
