@@ -114,9 +114,10 @@ void unpack_params(const double *p, const RunShape &g, PtRun &R)
  * noise alone scores at most about 1/2 and the controller responds to
  * truncation errors only:
  *   RK5 (del = max |er / sr| / atol, k = dt f):  sr += 2 nu / atol with
- *       |f|_max read as |k1|_max, coefficient 2 PT_NOISE_ULP 2^-24 |d|_2 / atol;
+ *       dt |f|_max read as |k1|_max, coefficient 2 PT_NOISE_ULP 2^-24 |d|_2 / atol;
  *   DOP853 (err = |dt| ||e / sr|| with e in units of f):  sr += 2 |dt| nu,
- *       coefficient 2 PT_NOISE_ULP 2^-24 |er|_2.
+ *       with |dt| |f|_max read as the largest component of the step's
+ *       increment dt k4 (in registers), coefficient 2 PT_NOISE_ULP 2^-24 |er|_2.
  * Without it the reference's per-component scales (RK5: |si| + |k1|) become
  * tiny where a momentum component crosses zero during a gyration, an
  * estimate made of FP32 rounding exceeds them at every step size, and the

@@ -39,7 +39,7 @@ struct PtRun {
     float face_skip;       /* faces within face_skip x the proposed step are crossed */
     float face_over;       /* overshoot past the capping face, in cells of the fastest axis */
     double noise;          /* PT_CTL_NOISE: rounding floor of the FP32 evaluation in the error
-                              norm, per unit of the largest |f(si)| component of a group
+                              norm, per unit of the largest dt |f| component of a group
                               (positions, momenta); 0 = the reference's norm */
     /* extensions */
     double eta;

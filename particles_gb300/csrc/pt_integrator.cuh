@@ -355,10 +355,10 @@ __device__ __forceinline__ double finish_attempt(const PtRun &P, const KRows &K,
             sr[c] = P.atol + P.rtol * pt_max(fabs(si[c]), fabs(sf[c]));
         }
 #ifndef PT_EXACT
-        if (P.noise != 0.0) {            /* PT_CTL_NOISE: sr += 2 |dt| nu per group */
-            const double fp = pt_max(fabs(K(0, 0)), pt_max(fabs(K(0, 1)), fabs(K(0, 2))));
-            const double fm = pt_max(fabs(K(0, 3)), pt_max(fabs(K(0, 4)), fabs(K(0, 5))));
-            const double np_ = P.noise * fabs(dt) * fp, nm_ = P.noise * fabs(dt) * fm;
+        if (P.noise != 0.0) {            /* PT_CTL_NOISE: sr += 2 |dt| nu per group, */
+            /* |dt f|_max read off the step's increment dsf = dt k4 (registers) */
+            const double np_ = P.noise * pt_max(fabs(dsf[0]), pt_max(fabs(dsf[1]), fabs(dsf[2])));
+            const double nm_ = P.noise * pt_max(fabs(dsf[3]), pt_max(fabs(dsf[4]), fabs(dsf[5])));
 #pragma unroll
             for (int c = 0; c < 6; ++c) sr[c] += (c < 3) ? np_ : nm_;
         }
