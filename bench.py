@@ -128,7 +128,7 @@ MIXED_VARIANTS = (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"), 
 # traffic per launch is this figure times the attempts of its launches.  The
 # figure is an upper estimate at full size: with 8x fewer particles, fewer
 # concurrently integrated particles share the field lines held in L2.
-DRAM_BYTES_PER_ATTEMPT = {("dop853-256", "fp64"): (5435572992 + 862161408) / 14067525}
+DRAM_BYTES_PER_ATTEMPT = {("dop853-256", "fp64"): (5439085056 + 1313298688) / 14067525}
 
 
 def parse():
