@@ -95,15 +95,20 @@ WORKLOADS = {
 ENSEMBLE_OPEN_X_MARGIN = 5.5
 
 
+TRAIN_EPOCHS = 2
+
+
 def train_controller(torch, records, method, face_feature=True):
-    """Network + safety factor from accepted-step records: 90 % train (two
-    epochs of Adam on the GPU), the safety factor maximises the expected
-    progress per attempt on the held-out 10 % (learned.choose_safety)."""
+    """Network + safety factor from accepted-step records: 90 % train
+    (TRAIN_EPOCHS epochs of Adam on the GPU), the safety factor maximises
+    the expected progress per attempt on the held-out 10 %
+    (learned.choose_safety)."""
     from particles_gb300 import learned as LRN
     X, T = LRN.dataset(records, method, face_feature=face_feature)
     k = int(0.9 * X.shape[0])
     norm = LRN.normalisation(X[:k], T[:k])
-    params, hist = LRN.train(torch, X[:k], T[:k], norm, epochs=2, batch=16384, lr=2e-3)
+    params, hist = LRN.train(torch, X[:k], T[:k], norm, epochs=TRAIN_EPOCHS, batch=16384,
+                             lr=2e-3)
     safety, info = LRN.choose_safety(params, norm, X[k:], T[k:])
     model = LRN.Model(params, norm, safety=safety)
     return model, {"records": int(X.shape[0]), "mse_per_epoch": hist, "safety": safety,
@@ -169,6 +174,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true",
                     help="launch every kernel in its default variant (3 blocks per SM)")
     ap.add_argument("--records", type=int, default=10_000_000)
+    ap.add_argument("--train-epochs", type=int, default=TRAIN_EPOCHS,
+                    help="epochs of Adam for the learned controllers")
     ap.add_argument("--legs", default="headline,fma,mixed,learned,ensemble",
                     help="comma list of legs to run (headline always prints the line)")
     ap.add_argument("--mixed-steps", type=int, default=5)
@@ -1223,7 +1230,9 @@ def compact_line(line, legs_path):
 
 
 def main():
+    global TRAIN_EPOCHS
     args = parse()
+    TRAIN_EPOCHS = args.train_epochs
     rank, world, local = dist_env()
     cfg = WORKLOADS[args.workload]
     if args.impl == "reference":
