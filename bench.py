@@ -50,6 +50,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 from pathlib import Path
@@ -182,7 +183,8 @@ def parse():
     ap.add_argument("--accuracy-particles", type=int, default=32768)
     ap.add_argument("--accuracy-seconds", type=float, default=60.0,
                     help="time limit of the exact kernel's accuracy reference run")
-    ap.add_argument("--legs-out", default="gpurun_out/bench_legs.json",
+    ap.add_argument("--legs-out",
+                    default=os.path.join(tempfile.gettempdir(), "particles_gb300_bench_legs.json"),
                     help="file that receives the full result with every leg (stdout gets one "
                          "compact line)")
     return ap.parse_args()

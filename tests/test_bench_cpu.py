@@ -83,10 +83,10 @@ def _full_line():
 def test_compact_line_is_small_and_complete():
     sys.path.insert(0, str(ROOT))
     import bench
-    out = bench.compact_line(_full_line(), str(ROOT / "gpurun_out" / "bench_legs.json"))
+    out = bench.compact_line(_full_line(), str(ROOT / "legs" / "bench_legs.json"))
     text = json.dumps(out)
     assert len(text) <= 1900, len(text)
-    assert out["legs"] == "gpurun_out/bench_legs.json"
+    assert out["legs"] == "legs/bench_legs.json"
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
                 "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
                 "roofline", "cpu_baseline", "e2e", "clocks", "gpu_launches", "parity", "targets"):
