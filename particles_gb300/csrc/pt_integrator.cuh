@@ -483,8 +483,9 @@ __device__ __forceinline__ double pt_face_cap(const PtRun &P, const double si[6]
 /* Time for the particle at si to reach the next cell face along its current
  * velocity (straight path, FP32): the learned controller's ninth input, in
  * every build (an input of the network, not part of the reference's
- * controller).  3e38 when the particle does not move across cells. */
-__device__ __forceinline__ float pt_face_time(const PtRun &P, const double si[6])
+ * controller).  xd: the offset of si in its cell, as the feature gather
+ * has it.  3e38 when the particle does not move across cells. */
+__device__ __forceinline__ float pt_face_time(const PtRun &P, const double si[6], const float xd[3])
 {
     const float ux = pt_d2f(si[3]), uy = pt_d2f(si[4]), uz = pt_d2f(si[5]);
     const float ig = rsqrtf(fmaf(ux, ux, fmaf(uy, uy, fmaf(uz, uz, 1.0f))));
@@ -492,8 +493,7 @@ __device__ __forceinline__ float pt_face_time(const PtRun &P, const double si[6]
     float tmin = 3.0e38f;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        const double xn = fma(si[i], P.gsx[i], P.gox[i]);
-        const float off = pt_d2f(xn - pt_floor(xn));               /* in [0, 1] */
+        const float off = xd[i];                                   /* in [0, 1] */
         const float w = u[i] * ig * P.ivunf * P.gsxf[i];           /* cells per unit time */
         const float aw = fabsf(w);
         if (aw > 0.0f) tmin = fminf(tmin, ((w > 0.0f) ? 1.0f - off : off) / aw);
@@ -772,7 +772,7 @@ __device__ __forceinline__ void run_machine(const Members<ENS> &MB)
                     feat[6] = __logf(pt_d2f(q) + 1e-30f);
                     feat[7] = __logf(dtf);
                     /* time to the next cell face in units of the last step */
-                    feat[8] = __logf(fminf(pt_face_time(PT_Q, si) / dtf, 1.0e6f) + 1e-30f);
+                    feat[8] = __logf(fminf(pt_face_time(PT_Q, si, fx_) / dtf, 1.0e6f) + 1e-30f);
                     if (PT_Q.rec) {
                         float *const pend = reinterpret_cast<float *>(
                             smem_tail + (PT_Q.mlp ? PT_MLP_BLOB_BYTES : 0)) + threadIdx.x;
