@@ -125,7 +125,9 @@ MIXED_VARIANTS = (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"), 
                   ("fp32_learned", "fp32"), ("bf16_learned", "bf16"), ("fp64_fma_face", "fp64_fma"),
                   ("fp32_face", "fp32"), ("bf16_face", "bf16"), ("fp32_learned_face", "fp32"),
                   ("bf16_learned_face", "bf16"), ("fp32_noise", "fp32"), ("bf16_noise", "bf16"),
-                  ("fp32_learned_noise", "fp32"), ("bf16_learned_noise", "bf16"))
+                  ("fp32_learned_noise", "fp32"), ("bf16_learned_noise", "bf16"),
+                  ("fp32_face_noise", "fp32"), ("bf16_face_noise", "bf16"),
+                  ("bf16_learned_face_noise", "bf16"))
 
 # DRAM bytes per attempt (dram__bytes_read.sum + dram__bytes_write.sum of one
 # launch / the attempts it made), from a one-pass ncu capture of a small case
@@ -658,7 +660,7 @@ def mixed_leg(args, dev, stream, peak):
     model = model_face = None
     for name, prec in MIXED_VARIANTS:
         f = handles[prec]
-        face = name.endswith("_face")
+        face = "_face" in name
         noise = "_noise" in name
         mdl = (model_face if face else model) if "_learned" in name else None
         st, cnt, status, carry = fresh(npart)
@@ -751,7 +753,7 @@ def mixed_leg(args, dev, stream, peak):
     res = {}
     w_ref = cfg["periods"]
     for name, prec in (MIXED_VARIANTS if na > 0 else ()):
-        face = name.endswith("_face")
+        face = "_face" in name
         noise = "_noise" in name
         mdl = (model_face if face else model) if "_learned" in name else None
         st, cnt, status, carry = fresh(na)
