@@ -127,7 +127,7 @@ MIXED_VARIANTS = (("fp64", "fp64"), ("fp64_fma", "fp64_fma"), ("fp32", "fp32"), 
                   ("bf16_learned_face", "bf16"), ("fp32_noise", "fp32"), ("bf16_noise", "bf16"),
                   ("fp32_learned_noise", "fp32"), ("bf16_learned_noise", "bf16"),
                   ("fp32_face_noise", "fp32"), ("bf16_face_noise", "bf16"),
-                  ("bf16_learned_face_noise", "bf16"))
+                  ("fp32_learned_face_noise", "fp32"), ("bf16_learned_face_noise", "bf16"))
 
 # DRAM bytes per attempt (dram__bytes_read.sum + dram__bytes_write.sum of one
 # launch / the attempts it made), from a one-pass ncu capture of a small case
