@@ -1062,7 +1062,9 @@ def learned_leg(args, dev, stream):
                 ("learned_8_inputs", "fp64", model8, False), ("fp32", "fp32", None, False),
                 ("fp32_learned", "fp32", model, False), ("fp32_face", "fp32", None, True),
                 ("fp32_learned_face", "fp32", model, True), ("fp32_noise", "fp32", None, False),
-                ("fp32_learned_noise", "fp32", model, False))
+                ("fp32_learned_noise", "fp32", model, False),
+                ("fp32_face_noise", "fp32", None, True),
+                ("fp32_learned_face_noise", "fp32", model, True))
     for name, prec, mdl, face in variants:
         f = fs[prec]
         noise = "_noise" in name
@@ -1187,8 +1189,8 @@ def targets(line):
         t["learned_vs_classical_dop853"] = {
             "sim_time": lr["physics_rate_ratio"], "attempts": lr["attempts_ratio"],
             "sim_time_8_inputs": lr.get("physics_rate_ratio_8_inputs")}
-        ml = {k: lr[k] for k in ("fp32_learned", "fp32_learned_face", "fp32_learned_noise")
-              if k in lr}
+        ml = {k: lr[k] for k in ("fp32_learned", "fp32_learned_face", "fp32_learned_noise",
+                                 "fp32_learned_face_noise") if k in lr}
         if ml:
             best = max(ml, key=lambda k: ml[k]["over_plain_exact"]["simulated_time"])
             acc = ml[best].get("accuracy_1_gyroperiod", {})
