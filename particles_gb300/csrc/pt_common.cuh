@@ -181,16 +181,18 @@ __device__ __forceinline__ int32_t pt_node_index(double q, int32_t d)
  * P. Markstein, IBM J. Res. Develop. 34(1), 1990): q0 = RN(a y) is within an
  * ulp of a / b, so the remainder r = a - b q0 is exact in one FMA and
  * RN(q0 + r y) is the correctly rounded quotient -- bit-identical to IEEE
- * a / b while the quotient stays well inside the normal range.  Three FP64
- * operations instead of a division sequence, and one reciprocal serves
- * every quotient by the same b.  Zeros, tiny or huge quotients, infinities
- * and NaN take the IEEE division (never on physical states; the exponent
- * test runs on the integer pipe). */
+ * a / b while the quotient and the remainder stay inside the normal range.
+ * Three FP64 operations instead of a division sequence, and one reciprocal
+ * serves every quotient by the same b.  Zeros, quotients outside [2^-960,
+ * 2^961), dividends below 2^-907 (whose remainder could be subnormal),
+ * infinities and NaN take the IEEE division (never on physical states; the
+ * exponent tests run on the integer pipe). */
 __device__ __forceinline__ double pt_qdiv(double a, double b, double y)
 {
     const double q0 = a * y;
     const uint32_t e = (uint32_t)((unsigned long long)__double_as_longlong(q0) >> 52) & 0x7ffu;
-    if (e - 63u > 1920u) return a / b;                      /* |q0| outside [2^-960, 2^961) */
+    const uint32_t ea = (uint32_t)((unsigned long long)__double_as_longlong(a) >> 52) & 0x7ffu;
+    if (e - 63u > 1920u || ea < 116u) return a / b;
     const double r = fma(-b, q0, a);
     return fma(r, y, q0);
 }

@@ -233,9 +233,9 @@ def test_reciprocal_quotient_bitwise(cuda):
     rounded reciprocal each (Markstein's quotient correction, pt_qdiv); it
     must equal the IEEE division bit for bit: random operands over 120
     binades, the kernel's own shapes (u / gamma with gamma = sqrt(u.u + 1),
-    v / vun), divisors with all-ones and single-bit mantissas, and zeros,
-    signed zeros, infinities, NaN and quotients near the range limits (which
-    take the division itself)."""
+    v / vun), divisors with all-ones and single-bit mantissas, dividends
+    down to 2^-1022, and zeros, signed zeros, infinities, NaN and quotients
+    near the range limits (which take the division itself)."""
     torch = cuda
     from particles_gb300 import _native as N
     g = torch.Generator(device="cuda").manual_seed(7)
@@ -258,6 +258,7 @@ def test_reciprocal_quotient_bitwise(cuda):
     cases.append((rnd(-40, 40), ones[torch.randint(0, 4, (n,), generator=g, device="cuda")]
                   * torch.pow(2.0, torch.randint(-40, 40, (n,), generator=g,
                                                  device="cuda").to(torch.float64))))
+    cases.append((rnd(-1022, -900), rnd(-80, 80)))       # tiny dividends: subnormal remainders
     sp = torch.tensor([0.0, -0.0, float("inf"), -float("inf"), float("nan"), 2.0 ** -1000,
                        -(2.0 ** -1000), 2.0 ** 1000, 5e-324, 1.0, -3.0], dtype=torch.float64,
                       device="cuda")
