@@ -8,11 +8,11 @@
  * the tensor cores with warp-level mma.sync m16n8k16 (FP16 operands, FP32
  * accumulate): the lanes of a warp are the rows of the activation matrix
  * (two m16 tiles, or one when a warp vote finds at most 16 lanes that want a
- * proposal and a shuffle regroups their rows).  The layer-1 input K of 9 is zero-padded to 16, the
- * layer-3 output N of 1 to 8.  A layer's FP32 accumulators convert in place
- * into the next layer's FP16 A fragments (the C layout of two adjacent n8
- * tiles is the A layout of one k16 tile), so only the input and the output
- * cross lanes.
+ * proposal and a shuffle regroups their rows).  The layer-1 input K of 9 is
+ * zero-padded to 16, the layer-3 output N of 1 to 8.  A layer's FP32
+ * accumulators convert in place into the next layer's FP16 A fragments (the
+ * C layout of two adjacent n8 tiles is the A layout of one k16 tile), so
+ * only the input and the output cross lanes.
  *
  * Fragment layouts (PTX ISA, mma.m16n8k16 .f16): g = lane >> 2, q = lane & 3;
  *   A (16x16): a0a1 = A[g][2q..2q+1], a2a3 = A[g+8][2q..], a4a5 = A[g][2q+8..],
