@@ -752,6 +752,7 @@ def mixed_leg(args, dev, stream, peak):
     na = min(args.accuracy_particles, npart)
     res = {}
     w_ref = cfg["periods"]
+    t_acc = time.perf_counter()
     for name, prec in (MIXED_VARIANTS if na > 0 else ()):
         face = "_face" in name
         noise = "_noise" in name
@@ -784,6 +785,7 @@ def mixed_leg(args, dev, stream, peak):
         rep["ks_bound"] = ks_bound
         rep["ks_within_bound"] = all(r["ks_energy"] < ks_bound for r in rep["rows"].values())
         out["accuracy"][prec] = rep
+    out["accuracy_wall_seconds"] = time.perf_counter() - t_acc
     for mo in (model, model_face):
         if mo is not None:
             mo.close()
@@ -1441,6 +1443,8 @@ def main():
                        "steps": k_e2e, "api": "pt_integrate_fields (host pinned buffers: "
                        "state(8,m,np), counters, carry, status in and out every step)"}
 
+    leg_s = {}
+    t_leg = time.perf_counter()
     if (args.precision == "fp64" and args.controller == "classical" and rank == 0
             and "fma" in set(args.legs.split(",")) and args.workload == "dop853-256"):
         line["plain_fma"] = plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev, stream,
@@ -1448,25 +1452,35 @@ def main():
         line["plain_fma_face"] = plain_fma_leg(args, cfg, npart, window, prm, tg, out, s0, dev,
                                                stream, peak, rec_bytes, face=True)
         line["plain_fma_accuracy"] = headline_accuracy(cfg, prm, tg, out, s0, dev)
+        leg_s["fma"] = time.perf_counter() - t_leg
 
     if not args.no_cpu and rank == 0 and world == 1:
+        t_leg = time.perf_counter()
         line["cpu_baseline"], par = cpu_baseline(cfg, prm, tg, out, s0, window, args.warmup,
                                                  args.steps, args.cpu_seconds, gpu=snap)
         if par is not None:
             line["parity"] = par
         snap = None
+        leg_s["cpu_baseline"] = time.perf_counter() - t_leg
     legs = set(args.legs.split(","))
     if not args.no_mixed and "mixed" in legs and rank == 0 and args.workload == "dop853-256":
         f.close()
         del d_state, d_cnt, d_status, d_carry
         torch.cuda.empty_cache()
+        t_leg = time.perf_counter()
         line["mixed"] = mixed_leg(args, dev, stream, peak)
+        leg_s["mixed"] = time.perf_counter() - t_leg
     if not args.no_learned and "learned" in legs and rank == 0 and args.workload == "dop853-256":
         torch.cuda.empty_cache()
+        t_leg = time.perf_counter()
         line["learned"] = learned_leg(args, dev, stream)
+        leg_s["learned"] = time.perf_counter() - t_leg
     if not args.no_ensemble and "ensemble" in legs and rank == 0 and args.workload == "dop853-256":
         torch.cuda.empty_cache()
+        t_leg = time.perf_counter()
         line["ensemble"] = ensemble_leg(args, dev, stream)
+        leg_s["ensemble"] = time.perf_counter() - t_leg
+    line["leg_wall_seconds"] = leg_s
     if rank == 0:
         legs_out = Path(args.legs_out)
         legs_out.parent.mkdir(parents=True, exist_ok=True)
