@@ -32,8 +32,8 @@ Reported (one JSON line, rank 0):
              energy and position errors against the exact kernel
   learned    the learned controller against the classical one (DOP853)
   ensemble   three snapshots in one persistent launch per window, as
-             launches and as a CUDA graph, and with the FMA build and
-             face-capped steps
+             launches and as a CUDA graph, and with face-capped steps in
+             the FMA build and in FP32 with the noise-floor norm
   targets    the plain kernel's roofline fractions and the mixed + learned
              ratios with their accuracy, gathered from the legs above
 
@@ -173,7 +173,7 @@ def parse():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the ensemble leg")
     ap.add_argument("--ensemble-precision", choices=["fp64", "fp64_fma", "fp32"], default="fp64")
     ap.add_argument("--no-face-ensemble", action="store_true",
-                    help="skip the ensemble's FMA + face-capped-steps variant")
+                    help="skip the ensemble's face-capped variants (FMA, and FP32 with the noise-floor norm)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="launch every kernel in its default variant (3 blocks per SM)")
     ap.add_argument("--records", type=int, default=10_000_000)
@@ -811,7 +811,7 @@ def ensemble_leg(args, dev, stream):
     counts[-1] = tot - sum(counts[:-1])
     tmax = cfg["periods"] * T0
     tg = params.time_grid(cfg["periods"], tmax)
-    members, keep, fma_fields, s0s = [], [], [], []
+    members, keep, fma_fields, f32_fields, s0s = [], [], [], [], []
     for k in range(3):
         prm = params.pack_params(qom=QOM, vunit=VUN, tmax=tmax, dtmax=tmax, atol=cfg["tol"][k],
                                  rtol=cfg["tol"][k], facmin=0.333, facmax=6.0, safe=0.9, beta=0.0)
@@ -821,6 +821,7 @@ def ensemble_leg(args, dev, stream):
         f = Fields(uu, bb, precision=prec, stream=stream.cuda_stream)
         if not args.no_face_ensemble:
             fma_fields.append(Fields(uu, bb, precision="fp64_fma", stream=stream.cuda_stream))
+            f32_fields.append(Fields(uu, bb, precision="fp32", stream=stream.cuda_stream))
         del uu, bb
         torch.cuda.empty_cache()
         n = counts[k]
@@ -929,18 +930,17 @@ def ensemble_leg(args, dev, stream):
     ens.close()
     for f in keep:
         f.close()
-    if fma_fields:
-        # the same ensemble with the FMA build and face-capped trial steps, from
-        # the same initial states: warm-up and timed windows as launches
-        fm = [dict(mb, fields=fma_fields[k],
+    def fast_run(flds, fprec, noise):
+        """The same ensemble from the same initial states with face-capped
+        trial steps (and the noise-floor norm when `noise`): warm-up and
+        timed windows as launches.  Returns (result, ensemble, members, t)."""
+        fm = [dict(mb, fields=flds[k],
                    state=torch.zeros_like(mb["state"]), cnt=torch.zeros_like(mb["cnt"]),
                    status=torch.zeros_like(mb["status"]), carry=torch.zeros_like(mb["carry"]))
               for k, mb in enumerate(members)]
         for k, mb in enumerate(fm):
             mb["state"][:, 0, :6] = torch.tensor(s0s[k], device=dev)
-        del members
-        torch.cuda.empty_cache()
-        ef = Ensemble(cfg["method"], fm, precision="fp64_fma", face_steps=True)
+        ef = Ensemble(cfg["method"], fm, precision=fprec, face_steps=True, noise_floor=noise)
         tf = 0.0
         for _ in range(args.warmup):
             tf += win
@@ -956,14 +956,30 @@ def ensemble_leg(args, dev, stream):
         stream.synchronize()
         sec = e0.elapsed_time(e1) * 1e-3
         c = sum(m["cnt"].sum(0).cpu().numpy() for m in fm)
-        out["fma_face"] = {"accepted_steps_per_s": (int(c[1]) - a0) / sec,
-                           "ms_per_step": 1e3 * sec / args.steps,
-                           "over_exact_launches": (int(c[1]) - a0) / sec
-                           / res["launches"]["accepted_steps_per_s"],
-                           "simulated_time_per_s_over_exact_launches":
-                           res["launches"]["ms_per_step"] / (1e3 * sec / args.steps),
-                           "rejected_fraction": float(c[2] / max(c[0], 1)),
-                           "check": int(ef.check())}
+        r = {"accepted_steps_per_s": (int(c[1]) - a0) / sec,
+             "ms_per_step": 1e3 * sec / args.steps,
+             "over_exact_launches": (int(c[1]) - a0) / sec
+             / res["launches"]["accepted_steps_per_s"],
+             "simulated_time_per_s_over_exact_launches":
+             res["launches"]["ms_per_step"] / (1e3 * sec / args.steps),
+             "rejected_fraction": float(c[2] / max(c[0], 1)),
+             "check": int(ef.check())}
+        return r, ef, fm, tf
+
+    if f32_fields:
+        # FP32 store, face-capped steps and the noise-floor norm
+        r32, ef32, fm32, _ = fast_run(f32_fields, "fp32", True)
+        out["fp32_face_noise"] = r32
+        ef32.close()
+        del fm32
+        for f in f32_fields:
+            f.close()
+        torch.cuda.empty_cache()
+    if fma_fields:
+        # the FMA build with face-capped trial steps
+        out["fma_face"], ef, fm, tf = fast_run(fma_fields, "fp64_fma", False)
+        del members
+        torch.cuda.empty_cache()
         # the rest of the configuration's 10 gyro-periods, as one captured
         # graph of windows of half a gyro-period with compaction between them
         wf = 0.5 * T0
