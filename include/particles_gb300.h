@@ -393,6 +393,10 @@ int pt_debug_ctl_pow(int64_t n, const double *d_x, const double *d_y, double *d_
  * (Markstein's correction) next to the IEEE division: d_out[2i] =
  * qdiv(a[i], b[i]), d_out[2i + 1] = a[i] / b[i] (device pointers). */
 int pt_debug_qdiv(int64_t n, const double *d_a, const double *d_b, double *d_out, void *stream);
+/* The exact build's product on the integer pipes next to the FPU's
+ * multiply: d_out[2i] = smul(a[i], b[i]), d_out[2i + 1] = a[i] * b[i]
+ * (device pointers). */
+int pt_debug_smul(int64_t n, const double *d_a, const double *d_b, double *d_out, void *stream);
 /* The integer-pipe floor, node index and double -> int32 conversion next to
  * the FP64 instructions they replace (4 doubles and 2 ints per input). */
 int pt_debug_intpipe(int64_t n, const double *d_x, int32_t d, double *d_out, int32_t *d_idx,

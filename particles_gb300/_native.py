@@ -32,7 +32,7 @@ EXPORTS = [
     "pt_mlp_infer", "pt_mlp_loss_grad", "pt_mlp_adam", "pt_autotune",
     "pt_ensemble_create", "pt_ensemble_destroy", "pt_ensemble_run", "pt_ensemble_capture",
     "pt_ensemble_replay", "pt_ensemble_counts", "pt_ensemble_escaped", "pt_ensemble_check",
-    "pt_copy_rows", "pt_debug_ctl_pow", "pt_debug_qdiv", "pt_last_transfer_bytes", "pt_debug_intpipe",
+    "pt_copy_rows", "pt_debug_ctl_pow", "pt_debug_qdiv", "pt_debug_smul", "pt_last_transfer_bytes", "pt_debug_intpipe",
     "pt_initial_state", "pt_moments", "pt_debug_face_params", "pt_debug_face_cap",
 ]
 
@@ -123,6 +123,7 @@ def load():
     L.pt_debug_pow.argtypes = [i64, vp, vp, vp, vp]
     L.pt_debug_ctl_pow.argtypes = [i64, vp, vp, vp, vp]
     L.pt_debug_qdiv.argtypes = [i64, vp, vp, vp, vp]
+    L.pt_debug_smul.argtypes = [i64, vp, vp, vp, vp]
     L.pt_debug_intpipe.argtypes = [i64, vp, i32, vp, vp, vp]
     L.pt_debug_accel.argtypes = [vp, i64, vp, vp, vp, vp]
     L.pt_probe_peak.argtypes = [i32, i32, C.POINTER(d)]

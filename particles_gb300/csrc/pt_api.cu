@@ -581,6 +581,14 @@ extern "C" int pt_debug_qdiv(int64_t n, const double *d_a, const double *d_b, do
     return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_qdiv");
 }
 
+extern "C" int pt_debug_smul(int64_t n, const double *d_a, const double *d_b, double *d_out,
+                             void *stream)
+{
+    if (n < 0 || (n > 0 && (!d_a || !d_b || !d_out))) return set_err(PT_ERR_ARG, "bad argument%s");
+    const cudaError_t e = pt_launch_smul(n, d_a, d_b, d_out, (cudaStream_t)stream);
+    return e == cudaSuccess ? PT_OK : cuda_err(e, "pt_debug_smul");
+}
+
 extern "C" int pt_debug_ctl_pow(int64_t n, const double *d_x, const double *d_y, double *d_out,
                                 void *stream)
 {

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/particles_gb300.h"
+#include "pt_smul.h"
 
 /* Everything a particle-integration kernel reads, by value in the launch. */
 struct PtRun {
@@ -197,6 +198,32 @@ __device__ __forceinline__ double pt_qdiv(double a, double b, double y)
     return fma(r, y, q0);
 }
 
+/* a * b on the integer pipes where pt_smul_bits covers it (normal operands,
+ * normal product), else on the FPU: the correctly rounded product either
+ * way, so the exact build may route any multiply here.  The FP64 pipe is the
+ * GB300 kernels' bottleneck; this form spends integer-pipe issue slots,
+ * which those kernels leave idle, instead. */
+__device__ __forceinline__ double pt_smul(double a, double b)
+{
+    uint32_t rh, rl;
+    if (pt_smul_bits((uint32_t)__double2hiint(a), (uint32_t)__double2loint(a),
+                     (uint32_t)__double2hiint(b), (uint32_t)__double2loint(b), rh, rl))
+        return __hiloint2double((int)rh, (int)rl);
+    return __dmul_rn(a, b);
+}
+
+/* The integer-pipe product alone: `ok` is cleared when the operands or the
+ * product lie outside pt_smul_bits' domain (the value is then meaningless
+ * and the caller recomputes on the FPU).  No branch, so a run of such
+ * products schedules as one straight-line block. */
+__device__ __forceinline__ double pt_smul_raw(double a, double b, bool &ok)
+{
+    uint32_t rh, rl;
+    ok &= pt_smul_bits((uint32_t)__double2hiint(a), (uint32_t)__double2loint(a),
+                       (uint32_t)__double2hiint(b), (uint32_t)__double2loint(b), rh, rl);
+    return __hiloint2double((int)rh, (int)rl);
+}
+
 __device__ __forceinline__ uint64_t pt_globaltimer()
 {
     uint64_t t;
@@ -274,6 +301,8 @@ cudaError_t pt_launch_accel_mixed(const PtRun &P, int nc, int brick, int64_t n, 
 
 cudaError_t pt_launch_debug_pow(int64_t n, const double *x, const double *y, double *out,
                                 cudaStream_t s);
+cudaError_t pt_launch_smul(int64_t n, const double *a, const double *b, double *out,
+                           cudaStream_t s);
 cudaError_t pt_launch_qdiv(int64_t n, const double *a, const double *b, double *out,
                            cudaStream_t s);
 cudaError_t pt_launch_ctl_pow(int64_t n, const double *x, const double *y, double *out,

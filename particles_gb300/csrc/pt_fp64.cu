@@ -38,6 +38,15 @@
 #ifndef PT_PART
 #define PT_PART 0
 #endif
+/* Components of each gathered product formed on the integer pipes in the
+ * exact build (pt_smul_raw); the rest use the FP64 pipe. */
+#ifndef PT_SMUL_SPLIT
+#define PT_SMUL_SPLIT 9
+#endif
+/* Exact build: keep the gather's corner loop rolled. */
+#ifndef PT_GATHER_ROLLED
+#define PT_GATHER_ROLLED 1
+#endif
 #define PT_CAT2(a, b) a##_##b
 #define PT_CAT(a, b) PT_CAT2(a, b)
 #define PT_NAME(x) PT_CAT(x, PT_SFX)
@@ -137,12 +146,64 @@ struct EvalF64 {
 #pragma unroll
             for (int cc = 0; cc < NV; ++cc) acc[cc] = v[cc];
         } else {
+#if defined(PT_EXACT) && PT_GATHER_ROLLED
+            /* The corner loop kept rolled, one corner's products in the
+             * instruction stream instead of eight, with the next corner's
+             * record loaded one iteration ahead; corner q takes x from bit
+             * 2, y from bit 1 and z from bit 0 of q, its weight the same
+             * product (a*b)*c as w8[q]. */
+            auto node_of = [&](int q) {
+                return ((q & 4) ? (int64_t)r[0] : (int64_t)l[0]) + ((q & 2) ? yr : yl) + ((q & 1) ? zr : zl);
+            };
+            auto w_of = [&](int q) {
+                const double pxy = (q & 4) ? ((q & 2) ? pdd : pdu) : ((q & 2) ? pud : puu);
+                return pxy * ((q & 1) ? xd[2] : xu[2]);
+            };
+            bool ok = true;
+            double v[NC], vn[NC];
+            load_rec<NC>(P.fld, PT_CHK(P, node[0], P.nrec), v);
+            load_rec<NC>(P.fld, PT_CHK(P, node[1], P.nrec), vn);
+#pragma unroll
+            for (int cc = 0; cc < NV; ++cc)
+                acc[cc] = cc < PT_SMUL_SPLIT ? pt_smul_raw(w8[0], v[cc], ok) : w8[0] * v[cc];
+#pragma unroll 1
+            for (int q = 1; q < 8; ++q) {                         /* :212-220 in order */
+#pragma unroll
+                for (int c = 0; c < NC; ++c) v[c] = vn[c];
+                load_rec<NC>(P.fld, PT_CHK(P, node_of(q < 7 ? q + 1 : 7), P.nrec), vn);
+                const double w = w_of(q);
+#pragma unroll
+                for (int cc = 0; cc < NV; ++cc)
+                    acc[cc] = acc[cc] + (cc < PT_SMUL_SPLIT ? pt_smul_raw(w, v[cc], ok) : w * v[cc]);
+            }
+#else
+            bool ok = true;
 #pragma unroll
             for (int q = 0; q < 8; ++q) {                         /* :212-220 in order */
                 double v[NC];
                 load_rec<NC>(P.fld, PT_CHK(P, node[q], P.nrec), v);
+#if defined(PT_EXACT) && PT_SMUL_SPLIT > 0
+                /* the products of the first PT_SMUL_SPLIT components on the
+                 * integer pipes (pt_smul_raw: the FPU's bits) */
+#pragma unroll
+                for (int cc = 0; cc < NV; ++cc) {
+                    const double p = cc < PT_SMUL_SPLIT ? pt_smul_raw(w8[q], v[cc], ok) : w8[q] * v[cc];
+                    acc[cc] = (q == 0) ? p : acc[cc] + p;
+                }
+#else
 #pragma unroll
                 for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * v[cc] : acc[cc] + w8[q] * v[cc];
+#endif
+            }
+#endif
+            if (!ok) {            /* a zero, subnormal or extreme operand: the FPU */
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    double u[NC];
+                    load_rec<NC>(P.fld, PT_CHK(P, node[q], P.nrec), u);
+#pragma unroll
+                    for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * u[cc] : acc[cc] + w8[q] * u[cc];
+                }
             }
         }
 #ifdef PT_EXACT
@@ -210,6 +271,7 @@ __global__ void k_accel(const PtRun P, int64_t n, const double *vec, double *acc
     }
 }
 
+#if PT_PART != 2
 /* Echo of the launch parameters as the device sees them (layout check). */
 __global__ void k_echo(const PtRun P, double *out)
 {
@@ -222,6 +284,7 @@ __global__ void k_echo(const PtRun P, double *out)
     out[6] = (double)offsetof(PtRun, tend);
     out[7] = (double)P.np;
 }
+#endif
 
 template <int METHOD, int NC, bool LEARN, int MINB>
 cudaError_t launch1(const PtRun &P, cudaStream_t s)

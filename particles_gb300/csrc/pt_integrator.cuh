@@ -44,6 +44,12 @@
 #include "pt_mlp.cuh"
 #include "pt_tableau.h"
 
+/* Exact build: form the stage sums' coefficient products on the integer
+ * pipes (pt_smul_raw), which the FP64-bound kernel leaves idle. */
+#ifndef PT_SMUL_STAGE
+#define PT_SMUL_STAGE 1
+#endif
+
 namespace pt_sm {
 
 using namespace pt_tab;
@@ -275,6 +281,20 @@ __device__ __forceinline__ void stage_state(int j, const KRows &K, const double 
 #pragma unroll
             for (int c = 0; c < 6; ++c) { dl[c] = h * K(0, c); ss[c] = si[c] + dl[c]; }
         } else {                                                /* :371-415 */
+#if defined(PT_EXACT) && PT_SMUL_STAGE
+            /* the coefficient products on the integer pipes (pt_smul_raw:
+             * the FPU's bits; the tables hold no zero coefficient), the
+             * FPU again for a zero or extreme k entry */
+            bool ok = true;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                double acc = pt_smul_raw(S.a[0], K(S.r[0], c), ok);
+                for (int i = 1; i < S.n; ++i) acc = acc + pt_smul_raw(S.a[i], K(S.r[i], c), ok);
+                dl[c] = dt * acc;
+                ss[c] = si[c] + dl[c];
+            }
+            if (!ok)
+#endif
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
                 double acc = S.a[0] * K(S.r[0], c);
@@ -294,7 +314,16 @@ __device__ __forceinline__ void stage_state(int j, const KRows &K, const double 
                 ss[c] = si[c] + acc;
             } else {
                 double acc = si[c];
+#if defined(PT_EXACT) && PT_SMUL_STAGE
+                bool ok = true;
+                for (int i = 0; i < S.n; ++i) acc = acc + pt_smul_raw(S.a[i], K(S.r[i], c), ok);
+                if (!ok) {
+                    acc = si[c];
+                    for (int i = 0; i < S.n; ++i) acc = acc + S.a[i] * K(S.r[i], c);
+                }
+#else
                 for (int i = 0; i < S.n; ++i) acc = acc + S.a[i] * K(S.r[i], c);
+#endif
                 ss[c] = acc;
             }
         }

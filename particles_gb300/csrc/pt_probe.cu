@@ -60,6 +60,18 @@ __global__ void k_qdiv(int64_t n, const double *a, const double *b, double *out)
     }
 }
 
+/* pt_smul next to the FPU's multiply: out[2i] = pt_smul(a, b),
+ * out[2i + 1] = a * b. */
+__global__ void k_smul(int64_t n, const double *a, const double *b, double *out)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double x = a[i], y = b[i];
+        out[2 * i] = pt_smul(x, y);
+        out[2 * i + 1] = __dmul_rn(x, y);
+    }
+}
+
 /* The non-exact builds' controller power, for its accuracy test. */
 __global__ void k_ctl_pow(int64_t n, const double *x, const double *y, double *o)
 {
@@ -134,6 +146,15 @@ cudaError_t pt_launch_qdiv(int64_t n, const double *a, const double *b, double *
     if (n <= 0) return cudaSuccess;
     const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
     k_qdiv<<<grid, 256, 0, s>>>(n, a, b, out);
+    return cudaGetLastError();
+}
+
+cudaError_t pt_launch_smul(int64_t n, const double *a, const double *b, double *out,
+                           cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    const int grid = (int)((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    k_smul<<<grid, 256, 0, s>>>(n, a, b, out);
     return cudaGetLastError();
 }
 

@@ -277,6 +277,54 @@ def test_reciprocal_quotient_bitwise(cuda):
         assert bool(same.all()), (a[~same][:4].tolist(), b[~same][:4].tolist())
 
 
+def test_integer_pipe_product_bitwise(cuda):
+    """The exact build forms part of its products on the integer pipes
+    (pt_smul); they must equal the FPU's multiply bit for bit: random bit
+    patterns, moderate exponents, short significands (ties), all-ones and
+    single-bit significands, products near overflow and underflow, and
+    zeros, infinities, NaN and subnormals (which take the FPU)."""
+    torch = cuda
+    from particles_gb300 import _native as N
+    g = torch.Generator(device="cuda").manual_seed(11)
+    n = 1 << 24
+
+    def bits(sign, exp, man):
+        return ((sign << 63) | ((exp & 0x7ff) << 52) | (man & ((1 << 52) - 1))).view(torch.float64)
+
+    def ri(lo, hi):
+        return torch.randint(lo, hi, (n,), generator=g, device="cuda", dtype=torch.int64)
+
+    man = lambda: ri(0, 1 << 52)
+    sg = lambda: ri(0, 2)
+    cases = [(ri(-(1 << 63), (1 << 63) - 1).view(torch.float64),
+              ri(-(1 << 63), (1 << 63) - 1).view(torch.float64))]
+    cases.append((bits(sg(), ri(983, 1064), man()), bits(sg(), ri(983, 1064), man())))
+    mask = ~((1 << ri(20, 40)) - 1)
+    cases.append((bits(sg(), ri(1000, 1040), man() & mask),
+                  bits(sg(), ri(1000, 1040), man() & ~((1 << ri(20, 40)) - 1))))
+    ones = (1 << 52) - 1 - ri(0, 256)
+    cases.append((bits(sg(), torch.full_like(ones, 1023), torch.where(sg() == 1, ones, ri(0, 256))),
+                  bits(sg(), ri(1022, 1025), torch.where(sg() == 1, ones, ri(0, 256)))))
+    ea = ri(1023, 2046)
+    cases.append((bits(sg(), ea, man()), bits(sg(), 2046 + 1023 - ea - ri(0, 3), man())))
+    ea = ri(1, 1023)
+    cases.append((bits(sg(), ea, man()), bits(sg(), 1024 - ea + ri(-2, 3), man())))
+    sp = torch.tensor([0.0, -0.0, float("inf"), -float("inf"), float("nan"), 5e-324, 2.0 ** -1030,
+                       2.0 ** -1000, 2.0 ** 1000, 1.0, -3.0, 0.1], dtype=torch.float64,
+                      device="cuda")
+    aa, bb = torch.meshgrid(sp, sp, indexing="ij")
+    cases.append((aa.reshape(-1).contiguous(), bb.reshape(-1).contiguous()))
+    L = N.load()
+    for a, b in cases:
+        a, b = a.contiguous(), b.contiguous()
+        out = torch.empty(2 * a.numel(), dtype=torch.float64, device="cuda")
+        N.check(L.pt_debug_smul(a.numel(), C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
+                                C.c_void_p(out.data_ptr()), None), "pt_debug_smul")
+        p, d = out[0::2], out[1::2]
+        same = (p.view(torch.int64) == d.view(torch.int64)) | (torch.isnan(p) & torch.isnan(d))
+        assert bool(same.all()), (a[~same][:4].tolist(), b[~same][:4].tolist())
+
+
 def test_host_buffer_calls_move_only_the_rows_they_write(cuda, oracle_lib):
     """pt_integrate_fields copies in the first row (and the carry), copies out
     only the rows each particle wrote: host rows beyond the window keep their
