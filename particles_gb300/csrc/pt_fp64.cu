@@ -39,13 +39,11 @@
 #define PT_PART 0
 #endif
 /* Components of each gathered product formed on the integer pipes in the
- * exact build (pt_smul_raw); the rest use the FP64 pipe. */
+ * exact build (pt_smul_raw); the rest use the FP64 pipe.  All of them is
+ * fastest once the corner loop stays rolled (measured on GB300: 3 of 9 gain
+ * 5 %, all 9 gain 16 %, against 3 % for the rolled loop alone). */
 #ifndef PT_SMUL_SPLIT
 #define PT_SMUL_SPLIT 9
-#endif
-/* Exact build: keep the gather's corner loop rolled. */
-#ifndef PT_GATHER_ROLLED
-#define PT_GATHER_ROLLED 1
 #endif
 #define PT_CAT2(a, b) a##_##b
 #define PT_CAT(a, b) PT_CAT2(a, b)
@@ -146,12 +144,15 @@ struct EvalF64 {
 #pragma unroll
             for (int cc = 0; cc < NV; ++cc) acc[cc] = v[cc];
         } else {
-#if defined(PT_EXACT) && PT_GATHER_ROLLED
+#ifdef PT_EXACT
             /* The corner loop kept rolled, one corner's products in the
              * instruction stream instead of eight, with the next corner's
              * record loaded one iteration ahead; corner q takes x from bit
              * 2, y from bit 1 and z from bit 0 of q, its weight the same
-             * product (a*b)*c as w8[q]. */
+             * product (a*b)*c as w8[q].  The products of the first
+             * PT_SMUL_SPLIT components go to the integer pipes
+             * (pt_smul_raw: the FPU's bits); a zero, subnormal or extreme
+             * operand clears `ok`, and the FPU sums the corners again. */
             auto node_of = [&](int q) {
                 return ((q & 4) ? (int64_t)r[0] : (int64_t)l[0]) + ((q & 2) ? yr : yl) + ((q & 1) ? zr : zl);
             };
@@ -176,27 +177,7 @@ struct EvalF64 {
                 for (int cc = 0; cc < NV; ++cc)
                     acc[cc] = acc[cc] + (cc < PT_SMUL_SPLIT ? pt_smul_raw(w, v[cc], ok) : w * v[cc]);
             }
-#else
-            bool ok = true;
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {                         /* :212-220 in order */
-                double v[NC];
-                load_rec<NC>(P.fld, PT_CHK(P, node[q], P.nrec), v);
-#if defined(PT_EXACT) && PT_SMUL_SPLIT > 0
-                /* the products of the first PT_SMUL_SPLIT components on the
-                 * integer pipes (pt_smul_raw: the FPU's bits) */
-#pragma unroll
-                for (int cc = 0; cc < NV; ++cc) {
-                    const double p = cc < PT_SMUL_SPLIT ? pt_smul_raw(w8[q], v[cc], ok) : w8[q] * v[cc];
-                    acc[cc] = (q == 0) ? p : acc[cc] + p;
-                }
-#else
-#pragma unroll
-                for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * v[cc] : acc[cc] + w8[q] * v[cc];
-#endif
-            }
-#endif
-            if (!ok) {            /* a zero, subnormal or extreme operand: the FPU */
+            if (!ok) {
 #pragma unroll
                 for (int q = 0; q < 8; ++q) {
                     double u[NC];
@@ -205,6 +186,15 @@ struct EvalF64 {
                     for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * u[cc] : acc[cc] + w8[q] * u[cc];
                 }
             }
+#else
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {                         /* :212-220 in order */
+                double v[NC];
+                load_rec<NC>(P.fld, PT_CHK(P, node[q], P.nrec), v);
+#pragma unroll
+                for (int cc = 0; cc < NV; ++cc) acc[cc] = (q == 0) ? w8[0] * v[cc] : acc[cc] + w8[q] * v[cc];
+            }
+#endif
         }
 #ifdef PT_EXACT
         /* the quotients by g and vun through one correctly rounded
@@ -272,6 +262,7 @@ __global__ void k_accel(const PtRun P, int64_t n, const double *vec, double *acc
 }
 
 #if PT_PART != 2
+#if PT_PART != 2
 /* Echo of the launch parameters as the device sees them (layout check). */
 __global__ void k_echo(const PtRun P, double *out)
 {
@@ -284,6 +275,7 @@ __global__ void k_echo(const PtRun P, double *out)
     out[6] = (double)offsetof(PtRun, tend);
     out[7] = (double)P.np;
 }
+#endif
 #endif
 
 template <int METHOD, int NC, bool LEARN, int MINB>
