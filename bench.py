@@ -1391,8 +1391,9 @@ def main():
             "peak_no_fma": peak_split / 1e12,
             "frac_of_no_fma_peak": achieved / peak_split,
             "no_fma_note": "the exact kernel may not contract (bit identity with the CPU "
-                           "restatement), so separate FP64 multiply/add chains measured live "
-                           "bound it",
+                           "restatement): separate FP64 multiply/add chains measured live bound "
+                           "what its FP64 pipe alone can do; it exceeds that bound because part "
+                           "of its correctly rounded multiplies run on the integer pipes",
             "flops_per_step": flops / args.steps,
             "gather_bytes_per_step": roofline.gather_bytes(cfg["method"], np.array([dcnt_tot]),
                                                            record_bytes=rec_bytes) / args.steps}
